@@ -1,0 +1,382 @@
+"""Drop-in mirror of the reference's ``forte2.lib.ci_helpers`` module (CIStrings, CISigmaBuilder,
+CISpinAdapter; bound in forte2/api/ci_helpers_api.cc:35-200) backed by the GB300 CUDA library.
+
+Method names, argument meaning and error types/messages follow the reference. Vectors may be
+numpy arrays (host; copied to and from the device around the call, the reference's own calling
+convention) or torch CUDA float64 tensors (device-resident; no copies). Everything runs on the
+GPU through ``include/forte2_gb300.h``; there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import check, lib, stream_handle
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _is_cuda_tensor(x):
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        return False
+    return isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def _host_vec(x, what="np_vector"):
+    if not isinstance(x, np.ndarray) or x.dtype != np.float64:
+        raise TypeError(f"{what} must be a float64 numpy array or a CUDA float64 tensor")
+    if x.ndim != 1:
+        raise RuntimeError("np_vector must be 1-dimensional to convert to std::span.")
+    if x.strides[0] != 8:
+        raise RuntimeError("np_vector must have stride 1 to convert to std::span.")
+    return x
+
+
+def _dev_vec(x):
+    if x.dtype != _torch().float64:
+        raise TypeError("device vectors must be float64")
+    if not x.is_contiguous():
+        raise RuntimeError("device vectors must be contiguous")
+    return x
+
+
+class Determinants:
+    """The determinant list of a CIStrings object (CIStrings::make_determinants,
+    ci/ci_strings.cc:186-194): address order, each entry an (alpha mask, beta mask) pair."""
+
+    def __init__(self, strings: "CIStrings"):
+        self.strings = strings
+
+    def __len__(self):
+        return self.strings.ndet
+
+    def masks(self) -> np.ndarray:
+        a = self.strings.alpha_masks()
+        b = self.strings.beta_masks()
+        out = np.empty((len(a) * len(b), 2), dtype=np.uint64)
+        out[:, 0] = np.repeat(a, len(b))
+        out[:, 1] = np.tile(b, len(a))
+        return out
+
+    def __getitem__(self, i):
+        return self.strings.determinant(i)
+
+
+class CIStrings:
+    """CI strings of a CAS active space (forte2/ci/ci_strings.cc:26-184), built on the device.
+
+    Supported: one GAS space, all orbital irreps 0 and state symmetry 0 (C1). Point-group
+    blocks and multiple GAS spaces raise NotImplementedError.
+    """
+
+    def __init__(self, na, nb, symmetry, orbital_symmetry, gas_min, gas_max):
+        if not isinstance(orbital_symmetry, (list, tuple)) or not all(
+                isinstance(g, (list, tuple)) for g in orbital_symmetry):
+            raise TypeError("orbital_symmetry must be a list of lists of orbital irreps")
+        if int(na) < 0 or int(nb) < 0:
+            raise ValueError("CIStrings: the number of electrons must be non-negative")
+        if len(gas_min) > len(orbital_symmetry) or len(gas_max) > len(orbital_symmetry):
+            raise ValueError(
+                f"CIStrings: The number of GAS spaces specified by gas_min ({len(gas_min)}) and gas_max "
+                f"({len(gas_max)}) must be less than or equal to the number of orbital symmetries "
+                f"({len(orbital_symmetry)})")
+        nonempty = [g for g in orbital_symmetry if len(g) > 0]
+        if len(nonempty) > 1:
+            raise NotImplementedError("CIStrings: several GAS spaces are not supported by the GPU path")
+        if any(x != 0 for g in orbital_symmetry for x in g) or symmetry != 0:
+            raise NotImplementedError("CIStrings: point-group symmetry blocks are not supported by the GPU path")
+        norb = sum(len(g) for g in orbital_symmetry)
+        self._na, self._nb, self._norb = int(na), int(nb), int(norb)
+        self.symmetry = int(symmetry)
+        self.orbital_symmetry = [list(g) for g in orbital_symmetry]
+        self.gas_min, self.gas_max = list(gas_min), list(gas_max)
+        if self._na > norb or self._nb > norb:
+            # the reference produces an empty determinant space
+            self._empty = True
+            self.h = None
+            self._info = [norb, self._na, self._nb, 0, 0, 0, 0, 0, 0, 0]
+            return
+        self._empty = False
+        h = C.c_void_p()
+        check(lib().f2g_strings_create(self._na, self._nb, self._norb, C.byref(h)))
+        self.h = h
+        info = np.zeros(10, dtype=np.int64)
+        check(lib().f2g_strings_info(self.h, info.ctypes.data))
+        self._info = [int(x) for x in info]
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().f2g_strings_destroy(h)
+            self.h = None
+
+    # properties of the reference binding (api/ci_helpers_api.cc:55-86)
+    na = property(lambda self: self._na)
+    nb = property(lambda self: self._nb)
+    norb = property(lambda self: self._norb)
+    nas = property(lambda self: self._info[3])
+    nbs = property(lambda self: self._info[4])
+    ndet = property(lambda self: self._info[5])
+    ngas_spaces = property(lambda self: len(self.orbital_symmetry))
+    gas_size = property(lambda self: [len(g) for g in self.orbital_symmetry])
+
+    def _masks(self, spin):
+        n = self.nas if spin == 0 else self.nbs
+        out = np.zeros(n, dtype=np.uint64)
+        if n and not self._empty:
+            check(lib().f2g_strings_masks(self.h, spin, out.ctypes.data))
+        return out
+
+    def alpha_masks(self):
+        return self._masks(0)
+
+    def beta_masks(self):
+        return self._masks(1)
+
+    def determinant(self, address):
+        a = self.alpha_masks()
+        b = self.beta_masks()
+        return int(a[address // len(b)]), int(b[address % len(b)])
+
+    def determinant_index(self, det):
+        a, b = det
+        am, bm = self.alpha_masks(), self.beta_masks()
+        ia = int(np.nonzero(am == np.uint64(a))[0][0])
+        ib = int(np.nonzero(bm == np.uint64(b))[0][0])
+        return ia * len(bm) + ib
+
+    def make_determinants(self):
+        return Determinants(self)
+
+    def list_1h(self, spin):
+        """1-hole list rows (class_K, K, class_I, sign, p, I) in the reference's order."""
+        cnt = C.c_int64(0)
+        check(lib().f2g_strings_list1h(self.h, spin, None, C.byref(cnt)))
+        out = np.zeros((cnt.value, 6), dtype=np.int32)
+        if cnt.value:
+            check(lib().f2g_strings_list1h(self.h, spin, out.ctypes.data, C.byref(cnt)))
+        return out
+
+    def list_2h(self, spin):
+        """2-hole list rows (class_K, K, class_I, sign, p, q, I) in the reference's order."""
+        cnt = C.c_int64(0)
+        check(lib().f2g_strings_list2h(self.h, spin, None, C.byref(cnt)))
+        out = np.zeros((cnt.value, 7), dtype=np.int32)
+        if cnt.value:
+            check(lib().f2g_strings_list2h(self.h, spin, out.ctypes.data, C.byref(cnt)))
+        return out
+
+
+class CISpinAdapter:
+    """CSF <-> determinant transforms (forte2/determinant/ci_spin_adapter.cc:55-288) on the device."""
+
+    def __init__(self, twoS, twoMs, norb):
+        self.twoS, self.twoMs, self.norb = int(twoS), int(twoMs), int(norb)
+        self.h = None
+        self.log_level = 3
+        self._info = [0, 0, 0]
+
+    def set_log_level(self, level):
+        self.log_level = int(level)
+
+    def prepare_couplings(self, dets):
+        strings = dets.strings if isinstance(dets, Determinants) else dets
+        if self.h:
+            lib().f2g_spin_adapter_destroy(self.h)
+            self.h = None
+        self.strings = strings
+        h = C.c_void_p()
+        check(lib().f2g_spin_adapter_create(strings.h, self.twoS, self.twoMs, C.byref(h)))
+        self.h = h
+        info = np.zeros(3, dtype=np.int64)
+        check(lib().f2g_spin_adapter_info(self.h, info.ctypes.data))
+        self._info = [int(x) for x in info]
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().f2g_spin_adapter_destroy(h)
+            self.h = None
+
+    nconf = property(lambda self: self._info[0])
+    ncsf = property(lambda self: self._info[1])
+    ncoupling = property(lambda self: self._info[2])
+    ndet = property(lambda self: self.strings.ndet)
+
+    def _transform(self, fn, src, dst, nsrc, ndst):
+        torch = _torch()
+        if _is_cuda_tensor(src) and _is_cuda_tensor(dst):
+            _dev_vec(src)
+            _dev_vec(dst)
+            nvec = 1 if src.dim() == 1 else src.shape[0]
+            check(fn(self.h, src.data_ptr(), dst.data_ptr(), nvec, stream_handle()))
+            return dst
+        s = torch.from_numpy(np.ascontiguousarray(_host_vec(src) if src.ndim == 1 else src)).cuda()
+        d = torch.empty(ndst, dtype=torch.float64, device="cuda")
+        check(fn(self.h, s.data_ptr(), d.data_ptr(), 1, stream_handle()))
+        dst[:] = d.cpu().numpy()
+        return dst
+
+    def csf_C_to_det_C(self, csf_C, det_C):
+        return self._transform(lib().f2g_csf_to_det, csf_C, det_C, self.ncsf, self.ndet)
+
+    def det_C_to_csf_C(self, det_C, csf_C):
+        return self._transform(lib().f2g_det_to_csf, det_C, csf_C, self.ndet, self.ncsf)
+
+    def couplings(self):
+        """(bounds[ncsf+1], det_idx, coeff, conf_ranges[nconf, 2]) in the reference's order."""
+        b = np.zeros(self.ncsf + 1, dtype=np.int64)
+        d = np.zeros(max(1, self.ncoupling), dtype=np.int64)
+        c = np.zeros(max(1, self.ncoupling))
+        r = np.zeros(max(2, 2 * self.nconf), dtype=np.int64)
+        check(lib().f2g_spin_adapter_dump(self.h, b.ctypes.data, d.ctypes.data, c.ctypes.data, r.ctypes.data))
+        return b, d[: self.ncoupling], c[: self.ncoupling], r[: 2 * self.nconf].reshape(-1, 2)
+
+
+class CISigmaBuilder:
+    """sigma = H C for determinant vectors (forte2/ci/ci_sigma_builder.h:26-117), on the GPU.
+
+    ``set_algorithm`` accepts the reference's four names; both algorithms return the same
+    sigma (to rounding) and run the same device kernels. ``set_precision("fp32")`` selects
+    FP32 arithmetic for every term (the mixed-precision mode; FP64 is the default and matches
+    the reference's arithmetic).
+    """
+
+    def __init__(self, lists: CIStrings, E, H, V, log_level=3):
+        self.lists = lists
+        self.log_level = int(log_level)
+        H, V = self._validate(H, V)
+        self._E = float(E)
+        self.h = C.c_void_p()
+        self._H, self._V = H, V
+        check(lib().f2g_sigma_create(lists.h, self._E, H.ctypes.data, V.ctypes.data, self.log_level,
+                                     C.byref(self.h)))
+        self._algorithm = "Knowles-Handy"
+        self._precision = 0
+
+    def _validate(self, H, V):
+        H = np.asarray(H, dtype=np.float64)
+        V = np.asarray(V, dtype=np.float64)
+        n = self.lists.norb
+        if H.ndim != 2:
+            raise RuntimeError("H must be a 2D matrix.")
+        if H.shape != (n, n):
+            raise RuntimeError("H shape does not match the number of orbitals.")
+        if V.ndim != 4:
+            raise RuntimeError("V must be a 4D tensor.")
+        if V.shape != (n, n, n, n):
+            raise RuntimeError("V shape does not match the number of orbitals.")
+        return np.ascontiguousarray(H), np.ascontiguousarray(V)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().f2g_sigma_destroy(h)
+            self.h = None
+
+    def set_log_level(self, level):
+        self.log_level = int(level)
+
+    def set_memory(self, mb):
+        check(lib().f2g_sigma_set_memory(self.h, int(mb)))
+
+    def set_algorithm(self, algorithm):
+        check(lib().f2g_sigma_set_algorithm(self.h, algorithm.encode()))
+
+    def get_algorithm(self):
+        buf = C.create_string_buffer(64)
+        check(lib().f2g_sigma_get_algorithm(self.h, buf, 64))
+        return buf.value.decode()
+
+    def set_precision(self, precision):
+        p = {"fp64": 0, "fp32": 1, 0: 0, 1: 1}[precision]
+        check(lib().f2g_sigma_set_precision(self.h, p))
+        self._precision = p
+
+    def get_precision(self):
+        return "fp64" if self._precision == 0 else "fp32"
+
+    def set_Hamiltonian(self, E, H, V):
+        H, V = self._validate(H, V)
+        self._E, self._H, self._V = float(E), H, V
+        check(lib().f2g_sigma_set_hamiltonian(self.h, self._E, H.ctypes.data, V.ctypes.data))
+
+    def Hamiltonian(self, basis, sigma):
+        """sigma <- H basis. numpy (host) or CUDA float64 tensors; a (nvec, ndet) CUDA tensor
+        applies H to every row."""
+        if _is_cuda_tensor(basis) and _is_cuda_tensor(sigma):
+            _dev_vec(basis)
+            _dev_vec(sigma)
+            nvec = 1 if basis.dim() == 1 else basis.shape[0]
+            if basis.numel() != nvec * self.lists.ndet or sigma.numel() != basis.numel():
+                raise RuntimeError("vector length does not match the number of determinants")
+            check(lib().f2g_sigma_apply(self.h, basis.data_ptr(), sigma.data_ptr(), nvec, stream_handle()))
+            return
+        b = _host_vec(basis)
+        s = _host_vec(sigma, "sigma")
+        if b.shape[0] != self.lists.ndet or s.shape[0] != self.lists.ndet:
+            raise RuntimeError("vector length does not match the number of determinants")
+        check(lib().f2g_sigma_apply_host(self.h, b.ctypes.data, s.ctypes.data, 1))
+
+    def term(self, which, basis):
+        """One HZ term alone (device tensors): "h0", "h1_a", "h1_b", "aabb", "aaaa", "bbbb"."""
+        torch = _torch()
+        idx = {"h0": 0, "h1_a": 1, "h1_b": 2, "aabb": 3, "aaaa": 4, "bbbb": 5}[which]
+        out = torch.empty_like(basis)
+        check(lib().f2g_sigma_term(self.h, idx, basis.data_ptr(), out.data_ptr(), stream_handle()))
+        return out
+
+    def avg_build_time(self):
+        out = np.zeros(4)
+        check(lib().f2g_sigma_avg_build_time(self.h, out.ctypes.data))
+        return [float(x) for x in out]
+
+    def det_energies(self):
+        torch = _torch()
+        out = torch.empty(self.lists.ndet, dtype=torch.float64, device="cuda")
+        check(lib().f2g_sigma_det_energies(self.h, out.data_ptr(), stream_handle()))
+        return out
+
+    def hdiag_csf_device(self, spin_adapter: CISpinAdapter):
+        torch = _torch()
+        out = torch.empty(spin_adapter.ncsf, dtype=torch.float64, device="cuda")
+        check(lib().f2g_hdiag_csf(self.h, spin_adapter.h, out.data_ptr(), stream_handle()))
+        return out
+
+    def form_Hdiag_csf(self, dets, spin_adapter: CISpinAdapter, spin_adapt_full_preconditioner=False):
+        """Approximate CSF diagonal sum_i c_i^2 E(det_i) (ci_sigma_builder.cc:317-370). With
+        spin_adapt_full_preconditioner the exact <I|H|I> is used (ci_sigma_builder.cc:323-330)."""
+        if spin_adapt_full_preconditioner:
+            return np.array([self.energy_csf(dets, spin_adapter, i) for i in range(spin_adapter.ncsf)])
+        return self.hdiag_csf_device(spin_adapter).cpu().numpy()
+
+    def csf_matrix(self, spin_adapter: CISpinAdapter, indices):
+        idx = np.ascontiguousarray(indices, dtype=np.int64)
+        m = len(idx)
+        out = np.zeros((m, m))
+        if m:
+            check(lib().f2g_csf_matrix(self.h, spin_adapter.h, idx.ctypes.data, m, out.ctypes.data))
+        return out
+
+    def slater_rules_csf(self, dets, spin_adapter, I, J):
+        return float(self.csf_matrix(spin_adapter, [I, J])[0, 1]) if I != J else self.energy_csf(
+            dets, spin_adapter, I)
+
+    def energy_csf(self, dets, spin_adapter, I):
+        return float(self.csf_matrix(spin_adapter, [I])[0, 0])
+
+    def form_H_csf(self, dets, spin_adapter, memory_mb=1024):
+        ncsf = spin_adapter.ncsf
+        if ncsf * ncsf * 8 > memory_mb * 1024 * 1024:
+            raise RuntimeError(
+                "Not enough memory to form the full Hamiltonian matrix in the CSF basis. Increase the "
+                "memory limit or use a different algorithm.")
+        return self.csf_matrix(spin_adapter, np.arange(ncsf))

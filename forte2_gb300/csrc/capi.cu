@@ -1,0 +1,365 @@
+// C-ABI entry points (include/forte2_gb300.h). Every call catches exceptions and maps them to
+// status codes with a thread-local message; nothing here allocates on behalf of the caller's
+// vectors (C, sigma, CSF vectors are caller-owned device or host buffers).
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/forte2_gb300.h"
+#include "csf.cuh"
+
+namespace f2g {
+void dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n, double* out,
+              double* scratch, cudaStream_t st);
+int64_t dav_scratch_size(int64_t n);
+void dav_lincomb(const double* X, int nx, int64_t ldx, const double* coef, int ny, double* Y, int64_t ldy, double beta,
+                 int64_t n, cudaStream_t st);
+void dav_residual(const double* B, const double* S, int m, int64_t ld, const double* alpha, const double* lam, int nroot,
+                  const double* hdiag, int64_t n, double thresh, double* R, int64_t ldr, double* norms2, double* scratch,
+                  cudaStream_t st);
+void dav_eigh(int m, const double* G, double* evals, double* evecs, cudaStream_t st);
+} // namespace f2g
+
+using namespace f2g;
+
+namespace {
+thread_local std::string g_err;
+
+template <typename F> int guard(F&& f) {
+    try {
+        f();
+        return 0;
+    } catch (const Error& e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_err = "host out of memory";
+        return 1;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
+}
+
+inline cudaStream_t S(void* p) { return static_cast<cudaStream_t>(p); }
+
+void need(const void* p, const char* what) {
+    if (!p)
+        throw Error(2, std::string(what) + " is NULL");
+}
+} // namespace
+
+extern "C" {
+
+const char* f2g_last_error(void) { return g_err.c_str(); }
+
+const char* f2g_version(void) { return "forte2_gb300 0.1 (sm_103a)"; }
+
+int f2g_strings_create(int na, int nb, int norb, void** out) {
+    return guard([&] {
+        need(out, "out");
+        if (na < 0 || nb < 0)
+            throw Error(2, "CIStrings: the number of electrons must be non-negative");
+        if (na > norb || nb > norb)
+            throw Error(2, "CIStrings: more electrons than orbitals");
+        *out = new CIStrings(na, nb, norb);
+    });
+}
+
+int f2g_strings_destroy(void* s) {
+    return guard([&] { delete static_cast<CIStrings*>(s); });
+}
+
+int f2g_strings_info(void* h, int64_t* out) {
+    return guard([&] {
+        need(h, "strings");
+        auto* s = static_cast<CIStrings*>(h);
+        const int64_t v[10] = {s->norb, s->na, s->nb, s->a.N0, s->b.N0, s->ndet, s->a.N1, s->b.N1, s->a.N2, s->b.N2};
+        std::memcpy(out, v, sizeof(v));
+    });
+}
+
+int f2g_strings_masks(void* h, int spin, uint64_t* host_out) {
+    return guard([&] {
+        need(h, "strings");
+        const auto& ss = static_cast<CIStrings*>(h)->spin(spin);
+        if (ss.N0)
+            F2G_CUDA(cudaMemcpy(host_out, ss.str.get(), ss.N0 * 8, cudaMemcpyDeviceToHost));
+    });
+}
+
+int f2g_strings_list1h(void* h, int spin, int32_t* rows, int64_t* count) {
+    return guard([&] {
+        need(h, "strings");
+        const auto& ss = static_cast<CIStrings*>(h)->spin(spin);
+        const int64_t nent = ss.N1 * ss.m1;
+        *count = nent;
+        if (!rows || nent == 0)
+            return;
+        std::vector<uint32_t> e(nent);
+        F2G_CUDA(cudaMemcpy(e.data(), ss.up1.get(), nent * 4, cudaMemcpyDeviceToHost));
+        for (int64_t K = 0; K < ss.N1; ++K)
+            for (int j = 0; j < ss.m1; ++j) {
+                const uint32_t x = e[K * ss.m1 + j];
+                int32_t* r = rows + 6 * (K * ss.m1 + j);
+                r[0] = 0;
+                r[1] = (int32_t)K;
+                r[2] = 0;
+                r[3] = e_neg(x) ? -1 : 1;
+                r[4] = e_orb(x);
+                r[5] = (int32_t)e_addr(x);
+            }
+    });
+}
+
+int f2g_strings_list2h(void* h, int spin, int32_t* rows, int64_t* count) {
+    return guard([&] {
+        need(h, "strings");
+        auto* s = static_cast<CIStrings*>(h);
+        auto& ss = s->spin(spin);
+        const int64_t nent = ss.N2 * ss.m2;
+        *count = nent;
+        if (!rows || nent == 0)
+            return;
+        ss.build_up2(s->binom.get(), 0);
+        std::vector<uint64_t> e(nent);
+        F2G_CUDA(cudaMemcpy(e.data(), ss.up2.get(), nent * 8, cudaMemcpyDeviceToHost));
+        for (int64_t K = 0; K < ss.N2; ++K)
+            for (int j = 0; j < ss.m2; ++j) {
+                const uint64_t x = e[K * ss.m2 + j];
+                int32_t* r = rows + 7 * (K * ss.m2 + j);
+                r[0] = 0;
+                r[1] = (int32_t)K;
+                r[2] = 0;
+                r[3] = (x >> 48 & 1) ? -1 : 1;
+                r[4] = (int32_t)(x >> 32 & 0xff);
+                r[5] = (int32_t)(x >> 40 & 0xff);
+                r[6] = (int32_t)(x & 0xffffffffu);
+            }
+    });
+}
+
+int f2g_sigma_create(void* strings, double E, const double* H, const double* V, int log_level, void** out) {
+    return guard([&] {
+        need(strings, "strings");
+        need(out, "out");
+        auto* s = static_cast<CIStrings*>(strings);
+        if (s->norb > 0) {
+            need(H, "H");
+            need(V, "V");
+        }
+        *out = new SigmaBuilder(s, E, H, V, log_level);
+    });
+}
+
+int f2g_sigma_destroy(void* sb) {
+    return guard([&] { delete static_cast<SigmaBuilder*>(sb); });
+}
+
+int f2g_sigma_set_hamiltonian(void* sb, double E, const double* H, const double* V) {
+    return guard([&] {
+        need(sb, "sigma");
+        static_cast<SigmaBuilder*>(sb)->set_hamiltonian(E, H, V);
+    });
+}
+
+int f2g_sigma_set_algorithm(void* sb, const char* name) {
+    return guard([&] {
+        need(sb, "sigma");
+        need(name, "name");
+        const std::string a(name);
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        if (a == "kh" || a == "knowles-handy")
+            b->algorithm = 0;
+        else if (a == "hz" || a == "harrison-zarrabian")
+            b->algorithm = 1;
+        else
+            throw Error(1, "CI algorithm " + a + " not valid.");
+    });
+}
+
+int f2g_sigma_get_algorithm(void* sb, char* buf, int buflen) {
+    return guard([&] {
+        need(sb, "sigma");
+        const char* name = static_cast<SigmaBuilder*>(sb)->algorithm == 0 ? "Knowles-Handy" : "Harrison-Zarrabian";
+        std::strncpy(buf, name, buflen);
+        if (buflen > 0)
+            buf[buflen - 1] = 0;
+    });
+}
+
+int f2g_sigma_set_memory(void* sb, int mb) {
+    return guard([&] {
+        need(sb, "sigma");
+        if (mb < 0)
+            throw Error(2, "CI builder memory must be non-negative.");
+        static_cast<SigmaBuilder*>(sb)->memory = (size_t)mb * 1024 * 1024;
+    });
+}
+
+int f2g_sigma_set_precision(void* sb, int precision) {
+    return guard([&] {
+        need(sb, "sigma");
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        if (precision != kFP64 && precision != kFP32)
+            throw Error(2, "precision must be 0 (FP64) or 1 (FP32)");
+        if (precision != b->precision) {
+            b->precision = precision;
+            if (precision == kFP32)
+                b->set_hamiltonian(b->E, b->H.data(), b->V.data());
+        }
+    });
+}
+
+int f2g_sigma_apply(void* sb, const double* C, double* sigma, int nvec, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        const int64_t nd = b->s->ndet;
+        if (nd && (!C || !sigma))
+            throw Error(2, "NULL vector");
+        for (int v = 0; v < nvec; ++v)
+            b->hamiltonian(C + v * nd, sigma + v * nd, S(stream));
+    });
+}
+
+int f2g_sigma_apply_host(void* sb, const double* C, double* sigma, int nvec) {
+    return guard([&] {
+        need(sb, "sigma");
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        const int64_t nd = b->s->ndet;
+        if (nd == 0)
+            return;
+        DevBuf<double> dc, ds;
+        dc.reserve(nd);
+        ds.reserve(nd);
+        for (int v = 0; v < nvec; ++v) {
+            F2G_CUDA(cudaMemcpy(dc.get(), C + v * nd, nd * 8, cudaMemcpyHostToDevice));
+            b->hamiltonian(dc.get(), ds.get(), 0);
+            F2G_CUDA(cudaMemcpy(sigma + v * nd, ds.get(), nd * 8, cudaMemcpyDeviceToHost));
+        }
+    });
+}
+
+int f2g_sigma_term(void* sb, int term, const double* C, double* sigma, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        if (term < 0 || term > 5)
+            throw Error(2, "term must be 0..5");
+        static_cast<SigmaBuilder*>(sb)->term(term, C, sigma, S(stream));
+    });
+}
+
+int f2g_sigma_avg_build_time(void* sb, double* out) {
+    return guard([&] {
+        need(sb, "sigma");
+        static_cast<SigmaBuilder*>(sb)->avg_build_time(out);
+    });
+}
+
+int f2g_sigma_det_energies(void* sb, double* out, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        static_cast<SigmaBuilder*>(sb)->det_energies(out, S(stream));
+    });
+}
+
+int f2g_spin_adapter_create(void* strings, int twoS, int twoMs, void** out) {
+    return guard([&] {
+        need(strings, "strings");
+        need(out, "out");
+        *out = new SpinAdapter(static_cast<CIStrings*>(strings), twoS, twoMs);
+    });
+}
+
+int f2g_spin_adapter_destroy(void* sa) {
+    return guard([&] { delete static_cast<SpinAdapter*>(sa); });
+}
+
+int f2g_spin_adapter_info(void* h, int64_t* out) {
+    return guard([&] {
+        need(h, "spin adapter");
+        auto* a = static_cast<SpinAdapter*>(h);
+        out[0] = a->nconf;
+        out[1] = a->ncsf;
+        out[2] = a->ncoupling;
+    });
+}
+
+int f2g_csf_to_det(void* h, const double* csf, double* det, int nvec, void* stream) {
+    return guard([&] {
+        need(h, "spin adapter");
+        auto* a = static_cast<SpinAdapter*>(h);
+        for (int v = 0; v < nvec; ++v)
+            a->csf_to_det(csf + v * a->ncsf, det + v * a->s->ndet, S(stream));
+    });
+}
+
+int f2g_det_to_csf(void* h, const double* det, double* csf, int nvec, void* stream) {
+    return guard([&] {
+        need(h, "spin adapter");
+        auto* a = static_cast<SpinAdapter*>(h);
+        for (int v = 0; v < nvec; ++v)
+            a->det_to_csf(det + v * a->s->ndet, csf + v * a->ncsf, S(stream));
+    });
+}
+
+int f2g_hdiag_csf(void* sb, void* h, double* out, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        need(h, "spin adapter");
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        auto* a = static_cast<SpinAdapter*>(h);
+        DevBuf<double> e;
+        e.reserve(std::max<int64_t>(1, b->s->ndet));
+        b->det_energies(e.get(), S(stream));
+        a->hdiag(e.get(), out, S(stream));
+        F2G_CUDA(cudaStreamSynchronize(S(stream)));
+    });
+}
+
+int f2g_csf_matrix(void* sb, void* h, const int64_t* idx, int m, double* out) {
+    return guard([&] {
+        need(sb, "sigma");
+        need(h, "spin adapter");
+        auto* a = static_cast<SpinAdapter*>(h);
+        for (int i = 0; i < m; ++i)
+            if (idx[i] < 0 || idx[i] >= a->ncsf)
+                throw Error(2, "CSF index out of range");
+        a->csf_matrix(*static_cast<SigmaBuilder*>(sb), idx, m, out);
+    });
+}
+
+int f2g_spin_adapter_dump(void* h, int64_t* bounds, int64_t* det_idx, double* coeff, int64_t* ranges) {
+    return guard([&] {
+        need(h, "spin adapter");
+        static_cast<SpinAdapter*>(h)->dump(bounds, det_idx, coeff, ranges);
+    });
+}
+
+int64_t f2g_dav_scratch_size(int64_t n) { return dav_scratch_size(n); }
+
+int f2g_dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n, double* out,
+                 double* scratch, void* stream) {
+    return guard([&] { dav_dots(A, na, lda, B, nb, ldb, n, out, scratch, S(stream)); });
+}
+
+int f2g_dav_lincomb(const double* X, int nx, int64_t ldx, const double* coef, int ny, double* Y, int64_t ldy,
+                    double beta, int64_t n, void* stream) {
+    return guard([&] { dav_lincomb(X, nx, ldx, coef, ny, Y, ldy, beta, n, S(stream)); });
+}
+
+int f2g_dav_residual(const double* B, const double* Sv, int m, int64_t ld, const double* alpha, const double* lam,
+                     int nroot, const double* hdiag, int64_t n, double thresh, double* R, int64_t ldr, double* norms2,
+                     double* scratch, void* stream) {
+    return guard([&] {
+        dav_residual(B, Sv, m, ld, alpha, lam, nroot, hdiag, n, thresh, R, ldr, norms2, scratch, S(stream));
+    });
+}
+
+int f2g_dav_eigh(int m, const double* G, double* evals, double* evecs, void* stream) {
+    return guard([&] { dav_eigh(m, G, evals, evecs, S(stream)); });
+}
+
+} // extern "C"

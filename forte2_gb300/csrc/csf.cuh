@@ -1,0 +1,34 @@
+// CSF spin adaptation on the device (see csf.cu).
+#pragma once
+
+#include <vector>
+
+#include "sigma.cuh"
+
+namespace f2g {
+
+struct SpinAdapter {
+    const CIStrings* s;
+    int twoS, twoMs, norb;
+    int64_t nconf = 0, ncsf = 0, nslot = 0, ncoupling = 0;
+    bool covers_all_dets = true;
+    // per number of open shells N: CSF count, determinant-pattern count, dense overlap table
+    std::vector<int> ncsfN, ndetN;
+    std::vector<int64_t> offN;             // offset of table N in O
+    DevBuf<double> O;                      // concatenated [ncsfN][ndetN] tables
+    DevBuf<int64_t> dOff;                  // offN on the device
+    DevBuf<int> dNcsf, dNdet;
+    DevBuf<uint64_t> conf_d, conf_s;       // [nconf] doubly / singly occupied masks (insertion order)
+    DevBuf<int64_t> conf_csf, conf_slot;   // [nconf + 1] exclusive offsets
+    DevBuf<uint32_t> perm;                 // [nslot] determinant address | negative sign << 31
+
+    SpinAdapter(const CIStrings* s, int twoS, int twoMs);
+    void csf_to_det(const double* csf, double* det, cudaStream_t st) const;
+    void det_to_csf(const double* det, double* csf, cudaStream_t st) const;
+    void hdiag(const double* det_energy, double* out, cudaStream_t st) const;
+    // dense <I|H|J> over CSFs idx[0..m) (slater_rules_csf, ci_sigma_builder.cc:278-297)
+    void csf_matrix(const SigmaBuilder& sb, const int64_t* idx, int m, double* out_host) const;
+    void dump(int64_t* bounds, int64_t* det_idx, double* coeff, int64_t* ranges) const;
+};
+
+} // namespace f2g

@@ -1,0 +1,647 @@
+// Sigma = H C on the device for a CAS space (C1, one determinant block), FP64 or FP32.
+//
+// The operator is the reference's Harrison-Zarrabian split (CISigmaBuilder::Hamiltonian,
+// forte2/ci/ci_sigma_builder.cc:187-218): H0 + H1(alpha) + H1(beta) + H2(alpha beta)
+// + H2(alpha alpha) + H2(beta beta), with the same coupling-list sign conventions, organised for
+// the GPU as follows (C and sigma are row-major: index Ia * N0b + Ib):
+//
+// * Same spin, alpha: the one-electron and same-spin two-electron operators restricted to alpha
+//   strings form a sparse "string Hamiltonian" Haa(Ja, Ia) with 1 + k(n-k) + C(k,2)C(n-k,2)
+//   entries per row (diagonal, single and double replacements). Its values are built once per
+//   set of integrals from the HZ lists' signs (hz.cc:14-195): a single Ja <- Ia (p <- q) carries
+//   s1(Ja,p) s1(Ia,q) h_pq + sum_t s2(Ja;p,t) s2(Ia;q,t) <(p,t)||(q,t)>, a double carries
+//   s2(Ja;p,r) s2(Ia;q,s) <pr||qs>, with s1/s2 the 1-hole/2-hole list signs. The scalar energy E
+//   (H0) is folded into the alpha diagonal. sigma(Ja,:) += sum_k Haa(Ja,Ia_k) C(Ia_k,:) is a row
+//   SpMM with coalesced row reads.
+// * Same spin, beta: the same SpMM on the transposed vector (the reference's gather_block /
+//   scatter_block transposes, ci_sigma_builder.cc:224-276).
+// * Opposite spin (hz.cc:197-308): one CTA owns an output alpha row Ja and keeps sigma(Ja,:) in
+//   shared memory. For each p in Ja (Ka = Ja - p) it stages the integral slice V[p, r, q, s]
+//   (q unoccupied in Ka) and, per beta 1-hole string Kb, gathers D[q][s] = sgn C(Ka+q, Kb+s),
+//   forms E[r] = sum_{q,s} V[p,r,q,s] D[q][s] for the (n - nb + 1) r unoccupied in Kb and adds
+//   sgn E[r] to sigma(Ja, Kb+r) with shared-memory atomics. Only the non-zero rows of the
+//   reference's D([qs],[Ka Kb]) are touched, so the FLOP count is 2 N1a N1b (ma mb)^2 with
+//   ma = n-na+1, mb = n-nb+1 (10x fewer than the dense n^2 x n^2 product). Owner-writes over
+//   Ja rows: no global atomics.
+#include <algorithm>
+#include <cstring>
+
+#include "sigma.cuh"
+
+namespace f2g {
+
+int ss_row_nnz(int n, int k) {
+    if (k < 0 || k > n)
+        return 0;
+    return int(1 + (int64_t)k * (n - k) + host_binom(k, 2) * host_binom(n - k, 2));
+}
+
+// ---- same-spin string Hamiltonian ------------------------------------------------------------
+
+__device__ inline double vphys(const double* V, int n, int p, int q, int r, int s) {
+    return V[(((size_t)p * n + q) * n + r) * n + s];
+}
+// <ab||cd> = V[a,b,c,d] - V[a,b,d,c]
+__device__ inline double vanti(const double* V, int n, int a, int b, int c, int d) {
+    return vphys(V, n, a, b, c, d) - vphys(V, n, a, b, d, c);
+}
+// 2-hole list sign <X - hi - lo| a_hi a_lo |X> (ci_strings_makers.cc:255-262)
+__device__ inline int s2neg(uint64_t X, int hi, int lo) {
+    return parity_below(X, lo) ^ parity_below(X & ~(uint64_t(1) << lo), hi);
+}
+
+// parts: bit 0 one-electron, bit 1 same-spin two-electron; e0 is added to the diagonal.
+template <typename T>
+__global__ void k_build_ss(int n, int k, int64_t N0, int nnz, const uint64_t* str, const uint64_t* binom,
+                           const double* h, const double* V, double e0, int parts, int32_t* col,
+                           T* val) {
+    const int64_t J = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (J >= N0)
+        return;
+    const uint64_t mJ = str[J];
+    const bool one = parts & 1, two = parts & 2;
+    int32_t* c = col + J * (int64_t)nnz;
+    T* v = val + J * (int64_t)nnz;
+    int e = 0;
+    // diagonal
+    double d = e0;
+    for (int t = 0; t < n; ++t) {
+        if (!(mJ >> t & 1))
+            continue;
+        if (one)
+            d += h[t * n + t];
+        if (two)
+            for (int u = 0; u < t; ++u)
+                if (mJ >> u & 1)
+                    d += vanti(V, n, t, u, t, u);
+    }
+    c[e] = (int32_t)J;
+    v[e] = (T)d;
+    ++e;
+    // single replacements Ja <- Ia: p in J, q not in J
+    for (int p = 0; p < n; ++p) {
+        if (!(mJ >> p & 1))
+            continue;
+        for (int q = 0; q < n; ++q) {
+            if (mJ >> q & 1)
+                continue;
+            const uint64_t mI = (mJ & ~(uint64_t(1) << p)) | (uint64_t(1) << q);
+            double x = 0.0;
+            if (one) {
+                const int neg = parity_below(mJ, p) ^ parity_below(mI, q);
+                x = neg ? -h[p * n + q] : h[p * n + q];
+            }
+            if (two) {
+                for (int t = 0; t < n; ++t) {
+                    if (t == p || !(mJ >> t & 1))
+                        continue;
+                    const int ph = p > t ? p : t, pl = p > t ? t : p;
+                    const int qh = q > t ? q : t, ql = q > t ? t : q;
+                    const int neg = s2neg(mJ, ph, pl) ^ s2neg(mI, qh, ql);
+                    const double a = vanti(V, n, ph, pl, qh, ql);
+                    x += neg ? -a : a;
+                }
+            }
+            c[e] = (int32_t)string_rank(mI, n, k, binom);
+            v[e] = (T)x;
+            ++e;
+        }
+    }
+    // double replacements: p > r in J, q > s not in J
+    for (int p = 0; p < n; ++p) {
+        if (!(mJ >> p & 1))
+            continue;
+        for (int r = 0; r < p; ++r) {
+            if (!(mJ >> r & 1))
+                continue;
+            for (int q = 0; q < n; ++q) {
+                if (mJ >> q & 1)
+                    continue;
+                for (int s = 0; s < q; ++s) {
+                    if (mJ >> s & 1)
+                        continue;
+                    const uint64_t mI =
+                        (mJ & ~((uint64_t(1) << p) | (uint64_t(1) << r))) | (uint64_t(1) << q) | (uint64_t(1) << s);
+                    double x = 0.0;
+                    if (two) {
+                        const int neg = s2neg(mJ, p, r) ^ s2neg(mI, q, s);
+                        const double a = vanti(V, n, p, r, q, s);
+                        x = neg ? -a : a;
+                    }
+                    c[e] = (int32_t)string_rank(mI, n, k, binom);
+                    v[e] = (T)x;
+                    ++e;
+                }
+            }
+        }
+    }
+}
+
+// Y[J, :] = (accumulate ? Y[J, :] : 0) + sum_k val[J,k] X[col[J,k], :]
+// grid (rows, column tiles of blockDim * VEC); the row's (col, val) list is staged in shared memory.
+template <typename T, int VEC>
+__global__ void __launch_bounds__(128) k_spmm_rows(int64_t nrows, int ncols, int nnz, const int32_t* col,
+                                                   const T* val, const T* X, T* Y, int accumulate) {
+    extern __shared__ unsigned char smem_raw[];
+    T* sval = reinterpret_cast<T*>(smem_raw);
+    int32_t* scol = reinterpret_cast<int32_t*>(sval + nnz);
+    const int64_t J = blockIdx.x;
+    for (int i = threadIdx.x; i < nnz; i += blockDim.x) {
+        sval[i] = val[J * nnz + i];
+        scol[i] = col[J * nnz + i];
+    }
+    __syncthreads();
+    const int c0 = blockIdx.y * (blockDim.x * VEC) + threadIdx.x;
+    T acc[VEC];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+        acc[j] = T(0);
+#pragma unroll 4
+    for (int i = 0; i < nnz; ++i) {
+        const T v = sval[i];
+        const T* x = X + (int64_t)scol[i] * ncols;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const int c = c0 + j * blockDim.x;
+            if (c < ncols)
+                acc[j] += v * __ldg(x + c);
+        }
+    }
+    T* y = Y + J * (int64_t)ncols;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        const int c = c0 + j * blockDim.x;
+        if (c < ncols)
+            y[c] = accumulate ? y[c] + acc[j] : acc[j];
+    }
+}
+
+// out (cols x rows) = in (rows x cols)^T, 32x32 tiles
+template <typename T>
+__global__ void k_transpose(int64_t rows, int64_t cols, const T* __restrict__ in, T* __restrict__ out) {
+    __shared__ T tile[32][33];
+    const int64_t bx = (int64_t)blockIdx.x * 32, by = (int64_t)blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t r = by + j, c = bx + threadIdx.x;
+        if (r < rows && c < cols)
+            tile[j][threadIdx.x] = in[r * cols + c];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t c = bx + j, r = by + threadIdx.x;
+        if (r < rows && c < cols)
+            out[c * rows + r] = tile[threadIdx.x][j];
+    }
+}
+
+template <typename TI, typename TO> __global__ void k_convert(int64_t n, const TI* in, TO* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (TO)in[i];
+}
+
+__global__ void k_scale(int64_t n, double a, const double* in, double* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = a * in[i];
+}
+
+// ---- opposite spin ----------------------------------------------------------------------------
+// One CTA per output alpha string Ja. MB bounds mb = n - nb + 1 (beta holes per 1-hole string).
+// SMROW: sigma(Ja,:) lives in shared memory; otherwise updates go to global memory atomically.
+template <typename T, int MB, bool SMROW>
+__global__ void __launch_bounds__(512, 1)
+    k_opposite(int n, int na, int N0b, int64_t N1b, int ma, int mb, const uint32_t* __restrict__ down_a,
+               const uint32_t* __restrict__ up_a, const uint32_t* __restrict__ up_b, const T* __restrict__ V,
+               const T* __restrict__ C, T* sig) {
+    extern __shared__ unsigned char smem_raw[];
+    T* vs = reinterpret_cast<T*>(smem_raw);                 // [n][ma][n]: V[p, r, q_i, s]
+    T* row = vs + (size_t)n * ma * n;                       // [N0b] (SMROW)
+    uint32_t* ua = reinterpret_cast<uint32_t*>(row + (SMROW ? N0b : 0)); // [ma]
+    const int64_t Ja = blockIdx.x;
+    T* srow = sig + Ja * (int64_t)N0b;
+    if (SMROW) {
+        for (int c = threadIdx.x; c < N0b; c += blockDim.x)
+            row[c] = srow[c];
+    }
+    for (int pi = 0; pi < na; ++pi) {
+        __syncthreads(); // previous slice fully consumed
+        const uint32_t ep = down_a[Ja * na + pi];
+        const int64_t Ka = e_addr(ep);
+        const int p = e_orb(ep);
+        const int negp = e_neg(ep);
+        for (int i = threadIdx.x; i < ma; i += blockDim.x)
+            ua[i] = up_a[Ka * ma + i];
+        __syncthreads();
+        const int nslice = n * ma * n;
+        for (int idx = threadIdx.x; idx < nslice; idx += blockDim.x) {
+            const int r = idx / (ma * n);
+            const int rem = idx - r * (ma * n);
+            const int qi = rem / n;
+            const int s = rem - qi * n;
+            const int q = e_orb(ua[qi]);
+            vs[idx] = V[(((size_t)p * n + r) * n + q) * n + s];
+        }
+        __syncthreads();
+        for (int64_t Kb = threadIdx.x; Kb < N1b; Kb += blockDim.x) {
+            uint32_t ub[MB];
+            int so[MB];
+            T acc[MB];
+#pragma unroll
+            for (int si = 0; si < MB; ++si) {
+                ub[si] = si < mb ? __ldg(up_b + Kb * mb + si) : 0u;
+                so[si] = e_orb(ub[si]);
+                acc[si] = T(0);
+            }
+            for (int qi = 0; qi < ma; ++qi) {
+                const uint32_t eq = ua[qi];
+                const T* crow = C + (int64_t)e_addr(eq) * N0b;
+                const int negq = e_neg(eq);
+                T d[MB];
+#pragma unroll
+                for (int si = 0; si < MB; ++si) {
+                    if (si < mb) {
+                        const T x = __ldg(crow + e_addr(ub[si]));
+                        d[si] = (negq ^ e_neg(ub[si])) ? -x : x;
+                    } else {
+                        d[si] = T(0);
+                    }
+                }
+                const T* vq = vs + qi * n;
+#pragma unroll
+                for (int ri = 0; ri < MB; ++ri) {
+                    if (ri < mb) {
+                        const T* vr = vq + so[ri] * (ma * n);
+                        T a = acc[ri];
+#pragma unroll
+                        for (int si = 0; si < MB; ++si)
+                            if (si < mb)
+                                a += vr[so[si]] * d[si];
+                        acc[ri] = a;
+                    }
+                }
+            }
+#pragma unroll
+            for (int ri = 0; ri < MB; ++ri) {
+                if (ri < mb) {
+                    const T x = (negp ^ e_neg(ub[ri])) ? -acc[ri] : acc[ri];
+                    if (SMROW)
+                        atomicAdd(row + e_addr(ub[ri]), x);
+                    else
+                        atomicAdd(srow + e_addr(ub[ri]), x);
+                }
+            }
+        }
+    }
+    if (SMROW) {
+        __syncthreads();
+        for (int c = threadIdx.x; c < N0b; c += blockDim.x)
+            srow[c] = row[c];
+    }
+}
+
+// ---- determinant energies (Slater rules diagonal, slater_rules.cc:86-121) -----------------------
+// Per string: e_same = sum_{p in X} h_pp + sum_{q<p in X} (<pq|pq> - <pq|qp>); per alpha string the
+// Coulomb row jrow[q] = sum_{p in Ia} <pq|pq>. E(Ia,Ib) = E0 + ea + eb + sum_{q in Ib} jrow_a[q].
+__global__ void k_string_energy(int n, int64_t N0, const uint64_t* str, const double* h, const double* V,
+                                double* e_same, double* jrow) {
+    const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (I >= N0)
+        return;
+    const uint64_t m = str[I];
+    double e = 0.0;
+    for (int p = 0; p < n; ++p) {
+        if (!(m >> p & 1))
+            continue;
+        e += h[p * n + p];
+        for (int q = 0; q < p; ++q)
+            if (m >> q & 1)
+                e += vphys(V, n, q, p, q, p) - vphys(V, n, q, p, p, q);
+    }
+    e_same[I] = e;
+    if (jrow) {
+        for (int q = 0; q < n; ++q) {
+            double j = 0.0;
+            for (int p = 0; p < n; ++p)
+                if (m >> p & 1)
+                    j += vphys(V, n, p, q, p, q);
+            jrow[I * n + q] = j;
+        }
+    }
+}
+
+__global__ void k_det_energy(int n, int64_t N0a, int64_t N0b, double E0, const uint64_t* strb, const double* ea,
+                             const double* eb, const double* jrow, double* out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N0a * N0b)
+        return;
+    const int64_t Ia = i / N0b, Ib = i - Ia * N0b;
+    uint64_t mb = strb[Ib];
+    double e = E0 + ea[Ia] + eb[Ib];
+    const double* jr = jrow + Ia * n;
+    while (mb) {
+        const int q = __ffsll((long long)mb) - 1;
+        e += jr[q];
+        mb &= mb - 1;
+    }
+    out[i] = e;
+}
+
+// ---- host side ---------------------------------------------------------------------------------
+
+SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const double* V_, int ll)
+    : s(s_), n(s_->norb), log_level(ll) {
+    for (auto& e : ev)
+        F2G_CUDA(cudaEventCreate(&e));
+    set_hamiltonian(E_, H_, V_);
+}
+
+SigmaBuilder::~SigmaBuilder() {
+    for (auto& e : ev)
+        if (e)
+            cudaEventDestroy(e);
+}
+
+void SigmaBuilder::build_string_hamiltonian(int spin, StringHamiltonian& sh, bool with_e0, cudaStream_t st) {
+    const SpinStrings& ss = s->spin(spin);
+    sh.nnz = ss_row_nnz(n, ss.k);
+    if (ss.N0 == 0 || sh.nnz == 0)
+        return;
+    const size_t total = (size_t)ss.N0 * sh.nnz;
+    sh.col.reserve(total);
+    sh.val.reserve(total);
+    k_build_ss<double><<<ceil_div(ss.N0, 128), 128, 0, st>>>(n, ss.k, ss.N0, sh.nnz, ss.str.get(), s->binom.get(),
+                                                            dH.get(), dV.get(), with_e0 ? E : 0.0, 3,
+                                                            sh.col.get(), sh.val.get());
+    F2G_LAUNCH("k_build_ss");
+    if (precision == kFP32) {
+        sh.valf.reserve(total);
+        k_convert<double, float><<<1024, 256, 0, st>>>((int64_t)total, sh.val.get(), sh.valf.get());
+        F2G_LAUNCH("k_convert");
+    }
+}
+
+void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_) {
+    E = E_;
+    H.assign(H_, H_ + (size_t)n * n);
+    V.assign(V_, V_ + (size_t)n * n * n * n);
+    dH.reserve(std::max<size_t>(1, H.size()));
+    dV.reserve(std::max<size_t>(1, V.size()));
+    if (!H.empty())
+        F2G_CUDA(cudaMemcpy(dH.get(), H.data(), H.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (!V.empty())
+        F2G_CUDA(cudaMemcpy(dV.get(), V.data(), V.size() * sizeof(double), cudaMemcpyHostToDevice));
+    fV.reserve(std::max<size_t>(1, V.size()));
+    if (!V.empty()) {
+        k_convert<double, float><<<64, 256>>>((int64_t)V.size(), dV.get(), fV.get());
+        F2G_LAUNCH("k_convert V");
+    }
+    build_string_hamiltonian(0, ha, true, 0);
+    build_string_hamiltonian(1, hb, false, 0);
+    F2G_CUDA(cudaDeviceSynchronize());
+}
+
+// The reference's K-block memory contract (ci_sigma_builder_knowles_handy.cc:15-32): every term
+// needs at least one K-block column of nrows doubles in each of its two buffers. The device path
+// keeps the same validation and error text; its own scratch is two determinant vectors.
+void SigmaBuilder::check_memory() const {
+    const int64_t NA = s->a.N0, NB = s->b.N0;
+    const size_t maxel = memory / (2 * sizeof(double));
+    auto need = [&](int64_t nrows, int64_t ncols) {
+        if (nrows == 0 || ncols == 0)
+            return;
+        if (maxel < (size_t)nrows)
+            throw Error(1, "The CI builder memory limit (" + std::to_string(memory) +
+                               " bytes) is too small for one K-block column of " + std::to_string(nrows) +
+                               " elements per buffer.");
+    };
+    const int64_t npairs = (int64_t)n * (n - 1) / 2;
+    if (algorithm == 1) {
+        if (s->na >= 1)
+            need((int64_t)n * NB, s->a.N1);
+        if (s->nb >= 1)
+            need((int64_t)n * NA, s->b.N1);
+        if (s->na >= 1 && s->nb >= 1)
+            need((int64_t)n * n * s->b.N1, s->a.N1);
+        if (s->na >= 2)
+            need(npairs * NB, s->a.N2);
+        if (s->nb >= 2)
+            need(npairs * NA, s->b.N2);
+    } else {
+        // Knowles-Handy: one (n(n+1)/2 x N(1h1p beta)) block per Ka chunk (kh.cc:88-171)
+        const int64_t ngeq = (int64_t)n * (n + 1) / 2;
+        need(ngeq * NB, NA);
+    }
+}
+
+template <typename T> static int64_t opposite_smem(int n, int ma, int N0b, bool smrow) {
+    return (int64_t)n * ma * n * sizeof(T) + (smrow ? (int64_t)N0b * sizeof(T) : 0) + (int64_t)ma * 4 + 16;
+}
+
+template <typename T, int MB, bool SMROW>
+static void launch_opposite_mb(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st) {
+    const int n = s->norb, ma = s->a.m1, mb = s->b.m1;
+    const int64_t smem = opposite_smem<T>(n, ma, (int)s->b.N0, SMROW);
+    auto kern = k_opposite<T, MB, SMROW>;
+    F2G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<(unsigned)s->a.N0, 512, smem, st>>>(n, s->na, (int)s->b.N0, s->b.N1, ma, mb, s->a.down1.get(),
+                                               s->a.up1.get(), s->b.up1.get(), V, C, sig);
+    F2G_LAUNCH("k_opposite");
+}
+
+template <typename T, bool SMROW>
+static void launch_opposite_r(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st) {
+    const int mb = s->b.m1;
+    if (mb <= 4)
+        launch_opposite_mb<T, 4, SMROW>(s, V, C, sig, st);
+    else if (mb <= 8)
+        launch_opposite_mb<T, 8, SMROW>(s, V, C, sig, st);
+    else if (mb <= 9)
+        launch_opposite_mb<T, 9, SMROW>(s, V, C, sig, st);
+    else if (mb <= 12)
+        launch_opposite_mb<T, 12, SMROW>(s, V, C, sig, st);
+    else if (mb <= 16)
+        launch_opposite_mb<T, 16, SMROW>(s, V, C, sig, st);
+    else if (mb <= 24)
+        launch_opposite_mb<T, 24, SMROW>(s, V, C, sig, st);
+    else
+        throw Error(1, "opposite-spin kernel supports at most 24 beta holes per 1-hole string");
+}
+
+template <typename T>
+static void launch_opposite(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st) {
+    if (s->na < 1 || s->nb < 1 || s->a.N0 == 0 || s->b.N1 == 0)
+        return;
+    const bool smrow = opposite_smem<T>(s->norb, s->a.m1, (int)s->b.N0, true) <= 200 * 1024;
+    if (smrow)
+        launch_opposite_r<T, true>(s, V, C, sig, st);
+    else
+        launch_opposite_r<T, false>(s, V, C, sig, st);
+}
+
+template <typename T>
+static void launch_spmm(const StringHamiltonian& sh, const T* val, int64_t nrows, int ncols, const T* X, T* Y,
+                        bool accumulate, cudaStream_t st) {
+    if (nrows == 0 || ncols == 0 || sh.nnz == 0)
+        return;
+    constexpr int VEC = sizeof(T) == 8 ? 4 : 8;
+    const int tile = 128 * VEC;
+    const size_t smem = (size_t)sh.nnz * (sizeof(T) + sizeof(int32_t));
+    if (smem > 48 * 1024)
+        F2G_CUDA(cudaFuncSetAttribute(k_spmm_rows<T, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)nrows, (unsigned)ceil_div(ncols, tile));
+    k_spmm_rows<T, VEC><<<grid, 128, smem, st>>>(nrows, ncols, sh.nnz, sh.col.get(), val, X, Y, accumulate ? 1 : 0);
+    F2G_LAUNCH("k_spmm_rows");
+}
+
+template <typename T>
+static void launch_transpose(int64_t rows, int64_t cols, const T* in, T* out, cudaStream_t st) {
+    if (rows == 0 || cols == 0)
+        return;
+    dim3 grid((unsigned)ceil_div(cols, 32), (unsigned)ceil_div(rows, 32));
+    k_transpose<T><<<grid, dim3(32, 8), 0, st>>>(rows, cols, in, out);
+    F2G_LAUNCH("k_transpose");
+}
+
+// mask bits: 1 alpha same-spin (+H0 +H1a), 2 beta same-spin (+H1b), 4 opposite spin
+template <typename T> void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed) {
+    const int64_t NA = s->a.N0, NB = s->b.N0, nd = NA * NB;
+    const T* valb = nullptr;
+    const T* vala = nullptr;
+    const T* Vt = nullptr;
+    T *Ct_, *Tt_;
+    if constexpr (sizeof(T) == 8) {
+        vala = ha.val.get();
+        valb = hb.val.get();
+        Vt = dV.get();
+        Ct_ = Ct.reserve(nd);
+        Tt_ = Tt.reserve(nd);
+    } else {
+        vala = ha.valf.get();
+        valb = hb.valf.get();
+        Vt = fV.get();
+        Ct_ = fCt.reserve(nd);
+        Tt_ = fTt.reserve(nd);
+    }
+    if (timed)
+        F2G_CUDA(cudaEventRecord(ev[0], st));
+    // beta same spin: sigma = (Hbb C^T)^T
+    if ((mask & 2) && s->nb >= 1) {
+        launch_transpose<T>(NA, NB, C, Ct_, st);
+        launch_spmm<T>(hb, valb, NB, (int)NA, Ct_, Tt_, false, st);
+        launch_transpose<T>(NB, NA, Tt_, sig, st);
+    } else {
+        F2G_CUDA(cudaMemsetAsync(sig, 0, nd * sizeof(T), st));
+    }
+    if (timed)
+        F2G_CUDA(cudaEventRecord(ev[1], st));
+    // alpha same spin + H0
+    if (mask & 1)
+        launch_spmm<T>(ha, vala, NA, (int)NB, C, sig, true, st);
+    if (timed)
+        F2G_CUDA(cudaEventRecord(ev[2], st));
+    if (mask & 4)
+        launch_opposite<T>(s, Vt, C, sig, st);
+    if (timed)
+        F2G_CUDA(cudaEventRecord(ev[3], st));
+}
+
+void SigmaBuilder::flush_timers() {
+    if (!ev_pending)
+        return;
+    F2G_CUDA(cudaEventSynchronize(ev[3]));
+    float bb = 0, aa = 0, ab = 0;
+    F2G_CUDA(cudaEventElapsedTime(&bb, ev[0], ev[1]));
+    F2G_CUDA(cudaEventElapsedTime(&aa, ev[1], ev[2]));
+    F2G_CUDA(cudaEventElapsedTime(&ab, ev[2], ev[3]));
+    t_acc[0] += (bb + aa + ab) * 1e-3;
+    t_acc[1] += ab * 1e-3;
+    t_acc[2] += aa * 1e-3;
+    t_acc[3] += bb * 1e-3;
+    builds += 1;
+    ev_pending = false;
+}
+
+void SigmaBuilder::avg_build_time(double* out) {
+    flush_timers();
+    for (int i = 0; i < 4; ++i)
+        out[i] = builds ? t_acc[i] / builds : 0.0;
+}
+
+void SigmaBuilder::hamiltonian(const double* C, double* sigma, cudaStream_t st) {
+    check_memory();
+    flush_timers();
+    const int64_t nd = s->ndet;
+    if (nd == 0)
+        return;
+    if (precision == kFP64) {
+        run<double>(C, sigma, st, 7, true);
+    } else {
+        float* c = fC.reserve(nd);
+        float* sg = fS.reserve(nd);
+        k_convert<double, float><<<1024, 256, 0, st>>>(nd, C, c);
+        F2G_LAUNCH("k_convert C");
+        run<float>(c, sg, st, 7, true);
+        k_convert<float, double><<<1024, 256, 0, st>>>(nd, sg, sigma);
+        F2G_LAUNCH("k_convert sigma");
+    }
+    ev_pending = true;
+}
+
+void SigmaBuilder::term(int which, const double* C, double* sigma, cudaStream_t st) {
+    const int64_t nd = s->ndet;
+    if (nd == 0)
+        return;
+    if (which == 0) {
+        k_scale<<<1024, 256, 0, st>>>(nd, E, C, sigma);
+        F2G_LAUNCH("k_scale");
+        return;
+    }
+    if (which == 3) {
+        F2G_CUDA(cudaMemsetAsync(sigma, 0, nd * sizeof(double), st));
+        launch_opposite<double>(s, dV.get(), C, sigma, st);
+        return;
+    }
+    // one-electron or same-spin two-electron part alone, through a temporary string Hamiltonian
+    const int spin = (which == 1 || which == 4) ? 0 : 1;
+    const int parts = (which == 1 || which == 2) ? 1 : 2;
+    const SpinStrings& ss = s->spin(spin);
+    StringHamiltonian tmp;
+    tmp.nnz = ss_row_nnz(n, ss.k);
+    F2G_CUDA(cudaMemsetAsync(sigma, 0, nd * sizeof(double), st));
+    if (ss.k < 1 || tmp.nnz == 0)
+        return;
+    const size_t total = (size_t)ss.N0 * tmp.nnz;
+    tmp.col.reserve(total);
+    tmp.val.reserve(total);
+    k_build_ss<double><<<ceil_div(ss.N0, 128), 128, 0, st>>>(n, ss.k, ss.N0, tmp.nnz, ss.str.get(), s->binom.get(),
+                                                            dH.get(), dV.get(), 0.0, parts, tmp.col.get(),
+                                                            tmp.val.get());
+    F2G_LAUNCH("k_build_ss term");
+    const int64_t NA = s->a.N0, NB = s->b.N0;
+    if (spin == 0) {
+        launch_spmm<double>(tmp, tmp.val.get(), NA, (int)NB, C, sigma, false, st);
+    } else {
+        double* ct = Ct.reserve(nd);
+        double* tt = Tt.reserve(nd);
+        launch_transpose<double>(NA, NB, C, ct, st);
+        launch_spmm<double>(tmp, tmp.val.get(), NB, (int)NA, ct, tt, false, st);
+        launch_transpose<double>(NB, NA, tt, sigma, st);
+    }
+    F2G_CUDA(cudaStreamSynchronize(st));
+}
+
+void SigmaBuilder::det_energies(double* out, cudaStream_t st) {
+    const int64_t NA = s->a.N0, NB = s->b.N0;
+    if (NA * NB == 0)
+        return;
+    DevBuf<double> ea, eb, jr;
+    ea.reserve(NA);
+    eb.reserve(NB);
+    jr.reserve((size_t)NA * std::max(1, n));
+    k_string_energy<<<ceil_div(NA, 128), 128, 0, st>>>(n, NA, s->a.str.get(), dH.get(), dV.get(), ea.get(), jr.get());
+    k_string_energy<<<ceil_div(NB, 128), 128, 0, st>>>(n, NB, s->b.str.get(), dH.get(), dV.get(), eb.get(), nullptr);
+    k_det_energy<<<ceil_div(NA * NB, 256), 256, 0, st>>>(n, NA, NB, E, s->b.str.get(), ea.get(), eb.get(), jr.get(), out);
+    F2G_LAUNCH("k_det_energy");
+    F2G_CUDA(cudaStreamSynchronize(st));
+}
+
+} // namespace f2g

@@ -1,0 +1,64 @@
+// The sigma builder: sigma = H C for one or more determinant vectors, resident on the device.
+#pragma once
+
+#include <vector>
+
+#include "strings.cuh"
+
+namespace f2g {
+
+enum Precision : int { kFP64 = 0, kFP32 = 1 };
+
+// Same-spin string Hamiltonian of one spin: for every string J the list of (I, value) with
+// value = <J| sum_pq h_pq a+_p a_q + sum_{p>r,q>s} <pr||qs> a+_r a+_p a_q a_s |I>, i.e. the
+// reference's H1_hz + H2_hz_same_spin operator restricted to one spin's strings.
+struct StringHamiltonian {
+    int nnz = 0; // entries per row
+    DevBuf<int32_t> col;
+    DevBuf<double> val;
+    DevBuf<float> valf;
+};
+
+struct SigmaBuilder {
+    CIStrings* s;
+    int n;
+    double E = 0.0;
+    std::vector<double> H, V; // host copies (row-major h[p*n+q], physicist V[p][q][r][s])
+    DevBuf<double> dH, dV;
+    DevBuf<float> fV;
+    StringHamiltonian ha, hb;
+    int algorithm = 0;       // 0 Knowles-Handy (the C++ default, ci_sigma_builder.h:288),
+                             // 1 Harrison-Zarrabian (what the Python driver selects)
+    size_t memory = size_t(1) << 30;
+    int precision = kFP64;
+    int log_level = 3;
+
+    // scratch (grown on demand)
+    DevBuf<double> Ct, Tt;
+    DevBuf<float> fC, fCt, fTt, fS;
+
+    // timing: [total, aabb, aaaa, bbbb] accumulated from CUDA events
+    double t_acc[4] = {0, 0, 0, 0};
+    int builds = 0;
+    cudaEvent_t ev[5] = {};
+    bool ev_pending = false;
+
+    SigmaBuilder(CIStrings* s, double E, const double* H, const double* V, int log_level);
+    ~SigmaBuilder();
+    void set_hamiltonian(double E, const double* H, const double* V);
+    void check_memory() const;
+    void hamiltonian(const double* C, double* sigma, cudaStream_t st);
+    // one HZ term into sigma (overwrites): 0 H0, 1 H1a, 2 H1b, 3 aabb, 4 aaaa(+H1a? no), 5 bbbb
+    void term(int which, const double* C, double* sigma, cudaStream_t st);
+    void det_energies(double* out, cudaStream_t st);
+    void flush_timers();
+    void avg_build_time(double* out);
+
+  private:
+    void build_string_hamiltonian(int spin, StringHamiltonian& sh, bool with_e0, cudaStream_t st);
+    template <typename T> void run(const T* C, T* sig, cudaStream_t st, int mask, bool timed);
+};
+
+int ss_row_nnz(int n, int k);
+
+} // namespace f2g

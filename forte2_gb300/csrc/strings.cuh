@@ -1,0 +1,34 @@
+// Device-resident CI strings and coupling lists (see strings.cu).
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace f2g {
+
+struct SpinStrings {
+    int n = 0, k = 0;            // orbitals, electrons of this spin
+    int64_t N0 = 0, N1 = 0, N2 = 0; // strings with k, k-1, k-2 electrons
+    int m1 = 0;                  // entries per 1-hole string: n - k + 1
+    int m2 = 0;                  // entries per 2-hole string: C(n - k + 2, 2)
+    DevBuf<uint64_t> str;        // [N0] occupation masks in address order
+    DevBuf<uint32_t> up1;        // [N1][m1] packed (I, p, sign)
+    DevBuf<uint32_t> down1;      // [N0][k]  packed (K, p, sign)
+    DevBuf<uint64_t> up2;        // [N2][m2] I | p<<32 | q<<40 | negative<<48 (built on demand)
+
+    void build(int norb, int nel, const uint64_t* d_binom, cudaStream_t st);
+    void build_up2(const uint64_t* d_binom, cudaStream_t st);
+};
+
+struct CIStrings {
+    int norb, na, nb;
+    int64_t ndet = 0;
+    DevBuf<uint64_t> binom; // C(a, b) at [a * kBinomLd + b]
+    SpinStrings a, b;
+    CIStrings(int na, int nb, int norb);
+    const SpinStrings& spin(int s) const { return s == 0 ? a : b; }
+    SpinStrings& spin(int s) { return s == 0 ? a : b; }
+};
+
+} // namespace f2g

@@ -1,0 +1,120 @@
+/*
+ * forte2_gb300 C ABI: determinant-CI sigma build and Davidson-Liu helpers on one GB300 GPU.
+ *
+ * The entry points replace the nanobind module forte2.lib.ci_helpers that the reference's
+ * Python CI driver binds (forte2/api/ci_helpers_api.cc:35-200). Plain pointers and sizes only;
+ * "dev" pointers are device (cudaMalloc / torch CUDA) memory, "host" pointers are host memory,
+ * `stream` is a cudaStream_t (NULL = legacy default stream).
+ *
+ * Every function returns a status: 0 ok, 1 runtime error (Python RuntimeError), 2 invalid
+ * argument (ValueError), 3 CUDA error, 4 out of device memory. The message of the last failure
+ * on the calling thread is returned by f2g_last_error(). Errors use the reference's messages
+ * where the reference defines one.
+ *
+ * Supported determinant spaces: one CAS/GAS space in C1 symmetry (all orbital irreps 0),
+ * 0 <= na, nb <= norb <= 62.
+ */
+#ifndef FORTE2_GB300_H
+#define FORTE2_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Message of the last failing call on this thread. */
+const char* f2g_last_error(void);
+
+/* Library version string. */
+const char* f2g_version(void);
+
+/* ---- CI strings: replaces CIStrings(na, nb, symmetry, orbital_symmetry, gas_min, gas_max)
+ *      (forte2/ci/ci_strings.cc:26-184; binding api/ci_helpers_api.cc:55-86). Strings, 1-hole
+ *      and 2-hole lists are built on the device. */
+int f2g_strings_create(int na, int nb, int norb, void** out);
+int f2g_strings_destroy(void* strings);
+/* out[10]: norb, na, nb, nas, nbs, ndet, N1a, N1b, N2a, N2b */
+int f2g_strings_info(void* strings, int64_t* out);
+/* Occupation masks (bit p = orbital p) of one spin (0 alpha, 1 beta) in address order. */
+int f2g_strings_masks(void* strings, int spin, uint64_t* host_out);
+/* 1-hole list rows (class_K, K, class_I, sign, p, I), the reference's get_*_1h_list2 content
+ * (ci_strings_makers.cc:163-241); host_rows = NULL returns the row count only. */
+int f2g_strings_list1h(void* strings, int spin, int32_t* host_rows, int64_t* count);
+/* 2-hole list rows (class_K, K, class_I, sign, p, q, I) (ci_strings_makers.cc:243-274). */
+int f2g_strings_list2h(void* strings, int spin, int32_t* host_rows, int64_t* count);
+
+/* ---- sigma builder: replaces CISigmaBuilder (forte2/ci/ci_sigma_builder.h:26-117;
+ *      binding api/ci_helpers_api.cc:89-148). H is (norb, norb) row-major, V is the physicist
+ *      tensor V[p][q][r][s] = <pq|rs> = (pr|qs), both host FP64. */
+int f2g_sigma_create(void* strings, double E, const double* host_H, const double* host_V, int log_level,
+                     void** out);
+int f2g_sigma_destroy(void* sigma);
+/* set_Hamiltonian (ci_sigma_builder.cc:102-185) */
+int f2g_sigma_set_hamiltonian(void* sigma, double E, const double* host_H, const double* host_V);
+/* set_algorithm: "kh", "knowles-handy", "hz", "harrison-zarrabian" (ci_sigma_builder.cc:49-57) */
+int f2g_sigma_set_algorithm(void* sigma, const char* name);
+/* get_algorithm: "Knowles-Handy" or "Harrison-Zarrabian" (ci_sigma_builder.cc:59-68) */
+int f2g_sigma_get_algorithm(void* sigma, char* buf, int buflen);
+/* set_memory in MB (ci_sigma_builder.cc:70-78); negative -> status 2 */
+int f2g_sigma_set_memory(void* sigma, int mb);
+/* 0 = FP64 (the reference's arithmetic), 1 = FP32 compute for every sigma term (mixed mode;
+ * the caller refines in FP64). No reference counterpart. */
+int f2g_sigma_set_precision(void* sigma, int precision);
+/* Hamiltonian(basis, sigma) for nvec vectors of length ndet stored back to back
+ * (ci_sigma_builder.cc:187-218); sigma is overwritten. */
+int f2g_sigma_apply(void* sigma, const double* dev_C, double* dev_sigma, int nvec, void* stream);
+/* The same through host buffers: H2D copy, apply, D2H copy (end-to-end path). */
+int f2g_sigma_apply_host(void* sigma, const double* host_C, double* host_sigma, int nvec);
+/* One HZ term alone, overwriting dev_sigma: 0 H0, 1 H1 alpha, 2 H1 beta, 3 opposite spin,
+ * 4 same-spin alpha (two-electron only), 5 same-spin beta (hz.cc:14-308). */
+int f2g_sigma_term(void* sigma, int term, const double* dev_C, double* dev_sigma, void* stream);
+/* avg_build_time: [total, aabb, aaaa, bbbb] seconds per build (ci_sigma_builder.h:93-102);
+ * aaaa includes H0 and H1 alpha, bbbb includes H1 beta. */
+int f2g_sigma_avg_build_time(void* sigma, double* host_out4);
+/* Slater-rule energy of every determinant, address order (slater_rules.cc:86-121). */
+int f2g_sigma_det_energies(void* sigma, double* dev_out, void* stream);
+
+/* ---- spin adapter: replaces CISpinAdapter(twoS, twoMs, norb) + prepare_couplings(dets)
+ *      (forte2/determinant/ci_spin_adapter.cc:55-235; binding api/ci_helpers_api.cc:190-200). */
+int f2g_spin_adapter_create(void* strings, int twoS, int twoMs, void** out);
+int f2g_spin_adapter_destroy(void* sa);
+/* out[3]: nconf, ncsf, ncoupling (non-zero CSF-determinant overlaps) */
+int f2g_spin_adapter_info(void* sa, int64_t* out);
+/* csf_C_to_det_C (ci_spin_adapter.cc:84-97), nvec vectors back to back */
+int f2g_csf_to_det(void* sa, const double* dev_csf, double* dev_det, int nvec, void* stream);
+/* det_C_to_csf_C (ci_spin_adapter.cc:69-82) */
+int f2g_det_to_csf(void* sa, const double* dev_det, double* dev_csf, int nvec, void* stream);
+/* form_Hdiag_csf(dets, spin_adapter, false) (ci_sigma_builder.cc:317-370) */
+int f2g_hdiag_csf(void* sigma, void* sa, double* dev_out, void* stream);
+/* Dense <I|H|J> over CSF indices idx[0..m) (slater_rules_csf, ci_sigma_builder.cc:278-315),
+ * host_out is m x m row-major. */
+int f2g_csf_matrix(void* sigma, void* sa, const int64_t* host_idx, int m, double* host_out);
+/* The CSF->determinant couplings in the reference's order (bounds[ncsf+1], det index and
+ * coefficient per coupling, conf_ranges[2*nconf]) for parity checks. */
+int f2g_spin_adapter_dump(void* sa, int64_t* host_bounds, int64_t* host_det_idx, double* host_coeff,
+                          int64_t* host_conf_ranges);
+
+/* ---- Davidson-Liu device kernels (forte2/helpers/davidsonliu.py:184-484). Vectors are rows
+ *      of length n with leading dimension ld. All FP64. `scratch` holds at least
+ *      f2g_dav_scratch_size(n) doubles. */
+int64_t f2g_dav_scratch_size(int64_t n);
+/* out[i * nb + j] = <A_i, B_j> */
+int f2g_dav_dots(const double* dev_A, int na, int64_t lda, const double* dev_B, int nb, int64_t ldb, int64_t n,
+                 double* dev_out, double* dev_scratch, void* stream);
+/* Y_j = beta Y_j + sum_i coef[i * ny + j] X_i (Y must not alias X) */
+int f2g_dav_lincomb(const double* dev_X, int nx, int64_t ldx, const double* dev_coef, int ny, double* dev_Y,
+                    int64_t ldy, double beta, int64_t n, void* stream);
+/* R_r = (S alpha_r - lam_r B alpha_r) / (lam_r - hdiag) where |lam_r - hdiag| > thresh else 0;
+ * norms2[r] = ||S alpha_r - lam_r B alpha_r||^2 (before preconditioning); alpha is m x nroot. */
+int f2g_dav_residual(const double* dev_B, const double* dev_S, int m, int64_t ld, const double* dev_alpha,
+                     const double* dev_lam, int nroot, const double* dev_hdiag, int64_t n, double thresh,
+                     double* dev_R, int64_t ldr, double* dev_norms2, double* dev_scratch, void* stream);
+/* Symmetric eigensolver for m <= 64: eigenvalues ascending, eigenvectors as columns (row-major). */
+int f2g_dav_eigh(int m, const double* dev_G, double* dev_evals, double* dev_evecs, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FORTE2_GB300_H */

@@ -1,0 +1,279 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a checkout that has the reference sources (default /root/reference):
+
+    oracle/build_ref.sh /root/reference
+    python tests/golden/make_golden.py [--big]
+
+Everything here comes from the reference's own code: its C++ CIStrings / CISigmaBuilder /
+CISpinAdapter compiled unmodified by oracle/build_ref.sh, and its helpers/davidsonliu.py
+driven exactly as forte2/ci/ci.py:245-303 drives it (CSF basis, Hdiag from form_Hdiag_csf,
+guess vectors from ci.py:411-452, sigma closure from ci.py:221-235). Integrals are the seeded
+synthetic recipe of forte2_gb300.synthetic. The fixtures are small .npz files; large cases are
+stored as checksums (norms, dot products with seeded vectors, sampled entries, SHA-256 of the
+integer lists) so they can be checked at full size without committing the full vectors.
+"""
+
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from forte2_gb300.synthetic import make_integrals, random_ci_vector  # noqa: E402
+from oracle import reference as ref  # noqa: E402
+from oracle.ref_davidson import load as load_davidson  # noqa: E402
+
+# (na, nb, norb) for the string/list fixtures, including empty and one-electron edge cases.
+LIST_CASES = [(0, 0, 3), (1, 0, 3), (0, 1, 3), (1, 1, 1), (1, 1, 2), (2, 2, 4), (3, 3, 6),
+              (2, 4, 7), (4, 4, 8), (3, 5, 9), (5, 5, 10), (6, 6, 12), (7, 7, 14)]
+LIST_HASH_CASES = [(8, 8, 16)]
+
+# (na, nb, norb, integral seed, vector seed) for sigma fixtures.
+SIGMA_CASES = [(1, 1, 2, 11, 101), (2, 2, 4, 12, 102), (3, 3, 6, 13, 103), (2, 3, 6, 14, 104),
+               (3, 1, 6, 15, 105), (1, 4, 6, 16, 106), (4, 0, 6, 17, 107), (0, 3, 5, 18, 108),
+               (4, 4, 8, 19, 109), (5, 5, 10, 1000, 110), (4, 5, 9, 21, 111)]
+SIGMA_CHECKSUM_CASES = [(6, 6, 12, 22, 112), (7, 7, 14, 2000, 113)]
+SIGMA_CHECKSUM_BIG = [(8, 8, 16, 3000, 114)]
+
+# (na, nb, norb, multiplicity, twice_ms, nroot, integral seed, e_tol, maxiter). The CAS(10,10)
+# four-root case does not converge within the reference's default 100 iterations on these
+# integrals, so it is also run with a larger iteration cap.
+DAVIDSON_CASES = [(2, 2, 4, 1, 0, 2, 31, 1e-12, 100), (3, 3, 6, 1, 0, 3, 32, 1e-12, 100),
+                  (3, 3, 6, 3, 0, 2, 33, 1e-12, 100), (4, 3, 7, 2, 1, 2, 34, 1e-12, 100),
+                  (4, 4, 8, 1, 0, 4, 35, 1e-12, 100), (4, 4, 8, 3, 0, 3, 36, 1e-12, 100),
+                  (5, 5, 10, 1, 0, 4, 1000, 1e-10, 100), (5, 5, 10, 1, 0, 4, 1000, 1e-10, 1000)]
+
+
+def list_rows(s: ref.RefCIStrings, spin: int):
+    return s.list_1h(spin), s.list_2h(spin)
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def gen_lists(out):
+    data = {}
+    meta = {}
+    for na, nb, n in LIST_CASES:
+        s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+        key = f"{na}_{nb}_{n}"
+        for spin, tag in ((0, "a"), (1, "b")):
+            masks, classes = s.strings(spin)
+            l1, l2 = list_rows(s, spin)
+            l1k = s.list_1h(spin, keyed=True)
+            assert np.array_equal(l1, l1k), "1h list2 and keyed 1h list disagree"
+            data[f"{key}_{tag}_strings"] = masks
+            data[f"{key}_{tag}_1h"] = l1
+            data[f"{key}_{tag}_2h"] = l2
+        meta[key] = dict(nas=s.nas, nbs=s.nbs, ndet=s.ndet)
+    for na, nb, n in LIST_HASH_CASES:
+        s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+        key = f"{na}_{nb}_{n}"
+        for spin, tag in ((0, "a"), (1, "b")):
+            masks, _ = s.strings(spin)
+            l1, l2 = list_rows(s, spin)
+            meta[f"{key}_{tag}"] = dict(strings_sha=sha(masks), l1_sha=sha(l1), l2_sha=sha(l2),
+                                        n_strings=len(masks), n_1h=len(l1), n_2h=len(l2))
+        meta[key] = dict(nas=s.nas, nbs=s.nbs, ndet=s.ndet)
+    np.savez_compressed(os.path.join(out, "lists.npz"), **data)
+    with open(os.path.join(out, "lists_meta.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+
+
+def spin_of(na, nb):
+    return abs(na - nb)
+
+
+def gen_sigma(out):
+    data = {}
+    for na, nb, n, iseed, cseed in SIGMA_CASES:
+        ints = make_integrals(n, iseed)
+        s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+        sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
+        sb.set_algorithm("hz")
+        c = random_ci_vector(s.ndet, cseed)
+        sig = np.zeros(s.ndet)
+        sb.Hamiltonian(c, sig)
+        key = f"{na}_{nb}_{n}"
+        small = s.ndet <= 5000
+        # C is regenerated from its seed by random_ci_vector; its hash guards the recipe.
+        data[f"{key}_C_sha"] = np.frombuffer(sha(c).encode(), dtype=np.uint8)
+        data[f"{key}_sigma"] = sig
+        for t in sb.TERMS if small else ("aabb", "aaaa", "bbbb"):
+            data[f"{key}_term_{t}"] = sb.term(t, c)
+        if small:
+            sbk = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
+            sbk.set_algorithm("kh")
+            sk = np.zeros(s.ndet)
+            sbk.Hamiltonian(c, sk)
+            data[f"{key}_sigma_kh"] = sk
+        if small:
+            data[f"{key}_det_energies"] = sb.det_energies()
+        data[f"{key}_V_sha"] = np.frombuffer(sha(ints.V).encode(), dtype=np.uint8)
+        data[f"{key}_seeds"] = np.array([iseed, cseed])
+        # spin adaptation: lowest multiplicity compatible with Ms, and the next one
+        twice_ms = na - nb
+        for twoS in (abs(twice_ms), abs(twice_ms) + 2):
+            if twoS > na + nb or (na + nb) == 0:
+                continue
+            sa = ref.RefSpinAdapter(twoS, twice_ms, n)
+            sa.prepare_couplings(s)
+            if sa.ncsf == 0:
+                continue
+            tag = f"{key}_S{twoS}"
+            if not small and twoS != abs(twice_ms):
+                continue
+            if small:
+                bounds, det_idx, coeff, ranges = sa.couplings()
+                data[f"{tag}_bounds"] = bounds
+                data[f"{tag}_det_idx"] = det_idx
+                data[f"{tag}_coeff"] = coeff
+                data[f"{tag}_conf_ranges"] = ranges
+            data[f"{tag}_info"] = np.array([sa.nconf, sa.ncsf, sa.ncoupling])
+            data[f"{tag}_hdiag"] = sb.form_Hdiag_csf(sa)
+            csf = random_ci_vector(sa.ncsf, cseed + 7)
+            data[f"{tag}_csf_to_det"] = sa.csf_C_to_det_C(csf)
+            data[f"{tag}_det_to_csf"] = sa.det_C_to_csf_C(sig)
+            m = min(sa.ncsf, 12)
+            data[f"{tag}_slater_csf"] = np.array(
+                [[sb.slater_rules_csf(sa, i, j) for j in range(m)] for i in range(m)])
+    np.savez_compressed(os.path.join(out, "sigma.npz"), **data)
+
+
+def checksums(sig, ndet, seed):
+    rng = np.random.default_rng(seed)
+    w = rng.normal(size=ndet)
+    idx = np.sort(rng.choice(ndet, size=min(4096, ndet), replace=False))
+    return dict(norm=float(np.linalg.norm(sig)), dot_w=float(sig @ w), idx=idx.tolist(),
+                vals=sig[idx].tolist(), sum=float(sig.sum()))
+
+
+def gen_sigma_checksums(out, cases, fname):
+    meta = {}
+    for na, nb, n, iseed, cseed in cases:
+        t0 = time.time()
+        ints = make_integrals(n, iseed)
+        s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+        sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
+        sb.set_algorithm("hz")
+        c = random_ci_vector(s.ndet, cseed)
+        sig = np.zeros(s.ndet)
+        sb.Hamiltonian(c, sig)
+        meta[f"{na}_{nb}_{n}"] = dict(iseed=iseed, cseed=cseed, ndet=s.ndet, V_sha=sha(ints.V),
+                                      seconds=time.time() - t0, **checksums(sig, s.ndet, cseed + 1))
+        print(f"sigma checksum {na},{nb},{n}: {time.time() - t0:.1f}s", flush=True)
+    with open(os.path.join(out, fname), "w") as f:
+        json.dump(meta, f)
+
+
+def reference_casci(na, nb, n, mult, twice_ms, nroot, iseed, e_tol, DavidsonLiuSolver, Params,
+                    maxiter=100):
+    """Drive the reference Davidson exactly as forte2/ci/ci.py:_do_iterative_ci does."""
+    ints = make_integrals(n, iseed)
+    s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+    sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
+    sb.set_algorithm("hz")
+    sa = ref.RefSpinAdapter(mult - 1, twice_ms, n)
+    sa.prepare_couplings(s)
+    hdiag = sb.form_Hdiag_csf(sa)
+    params = Params(e_tol=e_tol, maxiter=maxiter)
+    solver = DavidsonLiuSolver(size=sa.ncsf, nroot=nroot, davidson_liu_params=params, log_level=0)
+    solver.add_h_diag(hdiag)
+    # guess vectors (ci.py:411-452)
+    nguess = min(params.guess_per_root * nroot, sa.ncsf)
+    nguess_dets = min(params.ndets_per_guess * nguess, sa.ncsf)
+    indices = np.argsort(hdiag)[:nguess_dets]
+    Hg = np.zeros((nguess_dets, nguess_dets))
+    for i, I in enumerate(indices):
+        for j, J in enumerate(indices):
+            if i >= j:
+                v = sb.slater_rules_csf(sa, I, J)
+                Hg[i, j] = v
+                Hg[j, i] = v
+    _, vecs = np.linalg.eigh(Hg)
+    guess = np.zeros((sa.ncsf, nguess))
+    for i in range(nguess):
+        for j, d in enumerate(indices):
+            guess[d, i] = vecs[j, i]
+    solver.add_guesses(guess)
+
+    def sigma_builder(B, S):
+        for i in range(B.shape[1]):
+            bd = sa.csf_C_to_det_C(np.ascontiguousarray(B[:, i]))
+            sd = np.zeros(s.ndet)
+            sb.Hamiltonian(bd, sd)
+            S[:, i] = sa.det_C_to_csf_C(sd)
+
+    solver.add_sigma_builder(sigma_builder)
+    t0 = time.time()
+    evals, evecs = solver.solve()
+    seconds = time.time() - t0
+    # independent cross-check: Lanczos on the same reference sigma in the CSF basis
+    from scipy.sparse.linalg import LinearOperator, eigsh
+
+    def mv(x):
+        x = np.asarray(x, dtype=np.float64).reshape(-1)
+        sd = np.zeros(s.ndet)
+        sb.Hamiltonian(sa.csf_C_to_det_C(x), sd)
+        return sa.det_C_to_csf_C(sd)
+
+    if sa.ncsf <= 400:
+        Hd = np.column_stack([mv(e) for e in np.eye(sa.ncsf)])
+        lanczos = np.linalg.eigvalsh(0.5 * (Hd + Hd.T))[:nroot]
+    else:
+        op = LinearOperator((sa.ncsf, sa.ncsf), matvec=mv, dtype=np.float64)
+        lanczos = np.sort(eigsh(op, k=nroot, which="SA", tol=1e-14, ncv=max(4 * nroot, 40))[0])
+    return dict(evals=[float(x) for x in evals], converged=bool(solver.converged),
+                iterations=int(solver.iter), ncsf=sa.ncsf, ndet=s.ndet, seconds=seconds,
+                hdiag_min=float(hdiag.min()), nguess_dets=int(nguess_dets), maxiter=maxiter,
+                lanczos=[float(x) for x in lanczos],
+                max_dev_vs_lanczos=float(np.max(np.abs(np.sort(evals) - lanczos))))
+
+
+def gen_davidson(out, ref_root):
+    DL, Params = load_davidson(ref_root)
+    meta = {}
+    for case in DAVIDSON_CASES:
+        na, nb, n, mult, tms, nroot, iseed, e_tol, maxiter = case
+        r = reference_casci(na, nb, n, mult, tms, nroot, iseed, e_tol, DL, Params, maxiter)
+        r.update(dict(na=na, nb=nb, norb=n, multiplicity=mult, twice_ms=tms, nroot=nroot,
+                      iseed=iseed, e_tol=e_tol))
+        meta[f"{na}_{nb}_{n}_m{mult}_r{nroot}_it{maxiter}"] = r
+        print("davidson", case, r["evals"], r["iterations"], flush=True)
+    with open(os.path.join(out, "davidson.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--big", action="store_true", help="also the CAS(16,16) sigma checksum")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    ref.open_blas(threads=os.cpu_count())
+    steps = {"lists": lambda: gen_lists(HERE), "sigma": lambda: gen_sigma(HERE),
+             "checksums": lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_CASES, "sigma_checksums.json"),
+             "davidson": lambda: gen_davidson(HERE, a.reference)}
+    if a.big:
+        steps["big"] = lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_BIG, "sigma_checksums_16.json")
+    for name, f in steps.items():
+        if a.only and name not in a.only.split(","):
+            continue
+        t0 = time.time()
+        f()
+        print(f"{name}: {time.time() - t0:.1f}s", flush=True)
+
+
+if __name__ == "__main__":
+    main()
