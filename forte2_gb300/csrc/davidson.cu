@@ -9,6 +9,7 @@
 //   eigh      cyclic Jacobi on the small subspace matrix, eigenvalues ascending (replaces eigh,
 //             davidsonliu.py:259)
 // All reductions are two-stage with a fixed order, so results are bitwise reproducible.
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -256,16 +257,21 @@ void dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int
               double* scratch, cudaStream_t st) {
     if (na * nb == 0)
         return;
-    if (na * nb > 4 * 256)
-        throw Error(2, "dots: at most 1024 vector pairs per call");
+    if (nb > 64 || na > 64)
+        throw Error(2, "dots: at most 64 vectors per operand");
+    // rows of A in chunks so that one launch holds at most 1024 pairs (4 per thread)
+    const int chunk = std::max(1, std::min(na, std::min(32, 1024 / nb)));
     const int nbk = dots_blocks(n);
-    const size_t smem = (size_t)(na + nb) * (kTile + 1) * sizeof(double);
-    if (smem > 48 * 1024)
-        F2G_CUDA(cudaFuncSetAttribute(k_dots_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_dots_partial<<<nbk, 256, smem, st>>>(A, na, lda, B, nb, ldb, n, scratch);
-    F2G_LAUNCH("k_dots_partial");
-    k_reduce_partials<<<ceil_div(na * nb, 128), 128, 0, st>>>(nbk, na * nb, scratch, out);
-    F2G_LAUNCH("k_reduce_partials");
+    for (int i0 = 0; i0 < na; i0 += chunk) {
+        const int ni = std::min(chunk, na - i0);
+        const size_t smem = (size_t)(ni + nb) * (kTile + 1) * sizeof(double);
+        if (smem > 48 * 1024)
+            F2G_CUDA(cudaFuncSetAttribute(k_dots_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_dots_partial<<<nbk, 256, smem, st>>>(A + (int64_t)i0 * lda, ni, lda, B, nb, ldb, n, scratch);
+        F2G_LAUNCH("k_dots_partial");
+        k_reduce_partials<<<ceil_div(ni * nb, 128), 128, 0, st>>>(nbk, ni * nb, scratch, out + (int64_t)i0 * nb);
+        F2G_LAUNCH("k_reduce_partials");
+    }
 }
 
 int64_t dav_scratch_size(int64_t n) { return (int64_t)dots_blocks(n) * 4 * 256 + 64; }

@@ -1,0 +1,89 @@
+"""CPU checks of the boundary: the CUDA library builds for sm_103a, loads, and exports every symbol
+include/forte2_gb300.h declares; host-side validation mirrors the reference (no GPU calls)."""
+
+import ctypes
+import os
+import re
+import shutil
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    hdr = open(os.path.join(ROOT, "include", "forte2_gb300.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"\b(f2g_[a-z0-9_]+)\s*\(", hdr)))
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    from forte2_gb300.build import LIB_PATH, build
+
+    if not os.path.exists(LIB_PATH):
+        if not shutil.which("nvcc") and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+            pytest.skip("nvcc not available")
+        build()
+    return LIB_PATH
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    lib = ctypes.CDLL(libpath)
+    syms = declared_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_version_and_error_calls_need_no_gpu(libpath):
+    from forte2_gb300._lib import lib
+
+    assert b"sm_103a" in lib().f2g_version()
+    # invalid arguments are rejected on the host before any CUDA call
+    out = ctypes.c_void_p()
+    assert lib().f2g_strings_create(-1, 0, 3, ctypes.byref(out)) == 2
+    assert b"non-negative" in lib().f2g_last_error()
+
+
+def test_cistrings_input_validation():
+    """tests/ci/test_ci_strings.py:6-19 of the reference: negative counts -> ValueError, a flat
+    orbital-symmetry list -> TypeError. Both are raised before any device work."""
+    from forte2_gb300.ci_helpers import CIStrings
+
+    with pytest.raises(ValueError):
+        CIStrings(-1, 0, 0, [[]], [], [])
+    with pytest.raises(ValueError):
+        CIStrings(-1, -1, 0, [[]], [], [])
+    with pytest.raises(ValueError):
+        CIStrings(1, -1, 0, [[]], [], [])
+    with pytest.raises(TypeError):
+        CIStrings(1, 1, 0, [0], [], [])
+    with pytest.raises(NotImplementedError):
+        CIStrings(2, 2, 0, [[0, 0], [0, 0]], [0, 0], [4, 4])
+    with pytest.raises(NotImplementedError):
+        CIStrings(2, 2, 1, [[0, 1, 0, 1]], [], [])
+
+
+def test_params_validation():
+    from forte2_gb300.params import CIParams, DavidsonLiuParams
+
+    with pytest.raises(ValueError):
+        DavidsonLiuParams(collapse_per_root=0)
+    with pytest.raises(ValueError):
+        DavidsonLiuParams(collapse_per_root=3, basis_per_root=3)
+    with pytest.raises(ValueError):
+        CIParams(ci_algorithm="sparse-not-here")
+    assert CIParams().ci_algorithm == "hz" and CIParams().ci_builder_memory == 1024
+    p = DavidsonLiuParams()
+    assert (p.guess_per_root, p.ndets_per_guess, p.collapse_per_root, p.basis_per_root, p.maxiter,
+            p.e_tol, p.r_tol) == (2, 10, 2, 4, 100, 1e-12, 1e-6)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    import forte2_gb300._lib as L
+
+    monkeypatch.setattr(L, "_lib", None)
+    monkeypatch.setattr(L, "LIB_PATH", str(tmp_path / "nope.so"))
+    with pytest.raises(L.CudaLibraryMissing):
+        L.lib()
