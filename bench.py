@@ -1,0 +1,307 @@
+"""Benchmark: determinant-CI sigma builds per second at CAS(16e,16o), one GB300 per rank.
+
+One step = one sigma = H C build over the full CAS(16e,16o) Ms=0 determinant space
+(12870 x 12870 = 165,636,900 determinants, FP64 vectors of 1.32 GB, larger than L2, so no
+L2 flush is needed between steps), seeded synthetic integrals (naux = 64) and a seeded C.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value     sigma builds/s of the FP64 path with C and sigma resident in HBM (whole job: N ranks
+          run independent replicas, weak scaling).
+e2e       the same through the public host-buffer API: CISigmaBuilder.Hamiltonian(numpy C,
+          numpy sigma) from pinned host memory, H2D + build + D2H inside the timed region.
+roofline  the dominant kernel (opposite-spin k_opposite): algorithmic FLOPs per launch
+          2 N1a N1b (ma mb)^2 over its CUDA-event duration, against the measured FP64 peak.
+--impl reference times the reference algorithm's CPU implementation (the oracle port of the
+          Harrison-Zarrabian sigma, all host threads, BLAS from numpy's OpenBLAS) on a bounded
+          sample of the same build.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from forte2_gb300.synthetic import cas_dims, hz_flops, make_integrals, random_ci_vector, sparse_flops  # noqa: E402
+
+NORB, NEL = 16, 16
+ISEED, CSEED = 3000, 114
+FP64_PEAK_TFLOPS = 1.098  # measured torch.matmul FP64 8192^3 on this GB300 pool
+FP32_PEAK_TFLOPS = 69.70  # measured torch.matmul FP32 (no TF32) 8192^3
+METRIC = "CAS(16,16) sigma-builds/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--norb", type=int, default=NORB)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    return ap.parse_args()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (SM clock, max clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.strip() == "Active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count()
+
+
+def cpu_baseline(norb, budget_s, na, nb, ints, c):
+    """Reference algorithm (HZ, BLAS K-blocks, 1 GiB) on all host cores, bounded sample: the first
+    fraction f of every term's K-block chunks; rate = f / time. Returns (builds/s, sample text)."""
+    from oracle.port import PortCI, build_port, open_blas
+
+    build_port()
+    cores = cpu_cores()
+    os.environ["ORACLE_THREADS"] = str(cores)
+    blas = open_blas(threads=cores)
+    p = PortCI(norb, na, nb)
+    p.set_hamiltonian(ints.E, ints.H, ints.V)
+    # Two timed samples f0 < f1 of every term's K-block chunks. Time is linear in f with a fixed
+    # per-call part O (vector fills and transposes): t = O + f T, so one full build takes O + T.
+    f0 = 0.002
+    p.set_fraction(f0)
+    t = time.perf_counter()
+    p.sigma(c)
+    t0 = time.perf_counter() - t
+    f1 = min(1.0, max(4 * f0, f0 * budget_s / max(t0, 1e-3)))
+    p.set_fraction(f1)
+    t = time.perf_counter()
+    p.sigma(c)
+    t1 = time.perf_counter() - t
+    T = max((t1 - t0) / (f1 - f0), 1e-9)
+    O = max(t0 - f0 * T, 0.0)
+    full = O + T
+    sample = (f"two samples of one CAS({2 * na}e,{norb}o) FP64 HZ sigma build: the first {f0:.4f} and {f1:.4f} of "
+              f"every term's 1 GiB K-block chunks ({t0:.1f} s, {t1:.1f} s); full build = fixed {O:.2f} s + "
+              f"{T:.1f} s linear part; OpenBLAS {'numpy-bundled' if blas else 'absent: plain loops'}, {cores} threads")
+    return 1.0 / full, sample, cores
+
+
+def dist_setup(n_gpus):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        return rank, world, local, dist
+    torch.cuda.set_device(0)
+    return 0, 1, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(x, dist):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_gb300(a):
+    import torch
+
+    from forte2_gb300.ci_helpers import CISigmaBuilder, CIStrings
+
+    rank, world, local, dist = dist_setup(a.gpus)
+    na, nb, n0a, n0b, ndet = cas_dims(a.norb, a.norb, 0)
+    ints = make_integrals(a.norb, ISEED)
+    strings = CIStrings(na, nb, 0, [[0] * a.norb], [], [])
+    sb = CISigmaBuilder(strings, ints.E, ints.H, ints.V, 0)
+    sb.set_algorithm("hz")
+    c_host = random_ci_vector(ndet, CSEED)
+    C = torch.as_tensor(c_host, device="cuda")
+    S = torch.empty_like(C)
+    stream = torch.cuda.current_stream()
+    for _ in range(a.warmup):
+        sb.Hamiltonian(C, S)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    barrier(dist)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(a.steps):
+        sb.Hamiltonian(C, S)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clk = clocks.stop()
+    t_local = ev0.elapsed_time(ev1) / 1e3
+    t = max_over_ranks(t_local, dist)
+    value = world * a.steps / t
+    # per-term averages over warmup + timed builds (CUDA events around each phase)
+    tot, t_ab, t_aa, t_bb = sb.avg_build_time()
+    f_sp = sparse_flops(a.norb, na, nb)
+    f_hz = hz_flops(a.norb, na, nb)
+    achieved = f_sp["ab"] / t_ab / 1e12
+    # e2e through the public host-buffer API, pinned host memory
+    pin_c = torch.empty(ndet, dtype=torch.float64).pin_memory()
+    pin_s = torch.empty(ndet, dtype=torch.float64).pin_memory()
+    pin_c.numpy()[:] = c_host
+    hc, hs = pin_c.numpy(), pin_s.numpy()
+    sb.Hamiltonian(hc, hs)
+    barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        sb.Hamiltonian(hc, hs)
+    e2e_t = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e = world * a.steps / e2e_t
+    check = float(np.linalg.norm(hs))
+    # mixed mode (FP32 sigma) throughput, same workload
+    mixed = None
+    if not a.no_mixed:
+        sb.set_precision("fp32")
+        for _ in range(2):
+            sb.Hamiltonian(C, S)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            sb.Hamiltonian(C, S)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        mixed = world * a.steps / max_over_ranks(e0.elapsed_time(e1) / 1e3, dist)
+        sb.set_precision("fp64")
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        v, sample, cores = cpu_baseline(a.norb, a.cpu_seconds, na, nb, ints, c_host)
+        cpu = {"value": v, "unit": "sigma-builds/s", "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        line = {
+            "metric": METRIC if a.norb == NORB else f"CAS({a.norb},{a.norb}) sigma-builds/s",
+            "value": value, "unit": "sigma-builds/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * t / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded integrals, naux=4n; seeded C)",
+            "config": {"workload": f"CAS({a.norb}e,{a.norb}o) Ms=0 FP64 sigma build, {ndet} determinants",
+                       "ndet": ndet, "norb": a.norb, "na": na, "nb": nb, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (1.32 GB vectors), no flush"},
+            "e2e": {"value": e2e, "unit": "sigma-builds/s", "h2d_bytes_per_step": 8 * ndet,
+                    "d2h_bytes_per_step": 8 * ndet},
+            "gpu_launches": 5 * a.steps,
+            "roofline": {"bound": "compute", "pipe": "fp64", "kernel": "k_opposite (opposite-spin sigma)",
+                         "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                         "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+                         "peak_source": "measured FP64 DGEMM, profiles/gb300_gemm_peaks.md",
+                         "flops_per_launch": f_sp["ab"], "launch_ms": 1e3 * t_ab},
+            "terms_ms": {"total": 1e3 * tot, "aabb": 1e3 * t_ab, "aaaa_h1a_h0": 1e3 * t_aa, "bbbb_h1b": 1e3 * t_bb},
+            "hz_dense_flops": f_hz, "sparse_flops": f_sp,
+            "mixed_fp32_sigma_builds_per_s": mixed,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "sigma_norm": check,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(a):
+    """Reference arm: the reference's HZ algorithm on the host cores (oracle port), rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    na, nb, n0a, n0b, ndet = cas_dims(a.norb, a.norb, 0)
+    ints = make_integrals(a.norb, ISEED)
+    c = random_ci_vector(ndet, CSEED)
+    budget = max(2.0, min(a.cpu_seconds, 150.0 / max(1, a.steps + a.warmup)))
+    vals = []
+    sample = cores = None
+    for i in range(a.warmup + a.steps):
+        v, sample, cores = cpu_baseline(a.norb, budget, na, nb, ints, c)
+        if i >= a.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC if a.norb == NORB else f"CAS({a.norb},{a.norb}) sigma-builds/s",
+        "value": value, "unit": "sigma-builds/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded integrals, naux=4n; seeded C)",
+        "config": {"workload": f"CAS({a.norb}e,{a.norb}o) Ms=0 FP64 sigma build, {ndet} determinants", "ndet": ndet},
+        "cpu_baseline": {"value": value, "unit": "sigma-builds/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "sigma-builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+if __name__ == "__main__":
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)

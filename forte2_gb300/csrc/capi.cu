@@ -231,13 +231,12 @@ int f2g_sigma_apply_host(void* sb, const double* C, double* sigma, int nvec) {
         const int64_t nd = b->s->ndet;
         if (nd == 0)
             return;
-        DevBuf<double> dc, ds;
-        dc.reserve(nd);
-        ds.reserve(nd);
+        double* dc = b->hostC.reserve(nd);
+        double* ds = b->hostS.reserve(nd);
         for (int v = 0; v < nvec; ++v) {
-            F2G_CUDA(cudaMemcpy(dc.get(), C + v * nd, nd * 8, cudaMemcpyHostToDevice));
-            b->hamiltonian(dc.get(), ds.get(), 0);
-            F2G_CUDA(cudaMemcpy(sigma + v * nd, ds.get(), nd * 8, cudaMemcpyDeviceToHost));
+            F2G_CUDA(cudaMemcpy(dc, C + v * nd, nd * 8, cudaMemcpyHostToDevice));
+            b->hamiltonian(dc, ds, 0);
+            F2G_CUDA(cudaMemcpy(sigma + v * nd, ds, nd * 8, cudaMemcpyDeviceToHost));
         }
     });
 }

@@ -36,6 +36,7 @@ struct SigmaBuilder {
     // scratch (grown on demand)
     DevBuf<double> Ct, Tt;
     DevBuf<float> fC, fCt, fTt, fS;
+    DevBuf<double> hostC, hostS; // device staging for host-buffer calls
 
     // timing: [total, aabb, aaaa, bbbb] accumulated from CUDA events
     double t_acc[4] = {0, 0, 0, 0};

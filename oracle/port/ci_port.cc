@@ -309,12 +309,11 @@ struct Port {
         return std::min({maxel / nrows, ncols, (size_t)2147483647});
     }
 
-    size_t chunk_limit(size_t maxK, size_t chunk) const {
+    // number of K strings processed in a bounded timing sample (all of them when frac >= 1)
+    size_t chunk_limit(size_t maxK, size_t /*chunk*/) const {
         if (frac >= 1.0)
             return maxK;
-        size_t nchunks = (maxK + chunk - 1) / chunk;
-        size_t keep = std::max<size_t>(1, (size_t)std::ceil(frac * nchunks));
-        return std::min(maxK, keep * chunk);
+        return std::min(maxK, std::max<size_t>(1, (size_t)std::llround(frac * (double)maxK)));
     }
 
     // C (rows x cols) -> T (cols x rows)
@@ -337,7 +336,7 @@ struct Port {
         const size_t Kend = chunk_limit(maxK, chunk);
         std::vector<double> D, Eb;
         for (size_t K0 = 0; K0 < Kend; K0 += chunk) {
-            const size_t Ks = std::min(chunk, maxK - K0), dimKL = Ks * L;
+            const size_t Ks = std::min(chunk, Kend - K0), dimKL = Ks * L;
             D.assign((size_t)n * dimKL, 0.0);
             Eb.assign((size_t)n * dimKL, 0.0);
             parallel_for(Ks, [&](size_t b, size_t e) {
@@ -373,7 +372,7 @@ struct Port {
         const size_t Kend = chunk_limit(maxK, chunk);
         std::vector<double> D, Eb;
         for (size_t K0 = 0; K0 < Kend; K0 += chunk) {
-            const size_t Ks = std::min(chunk, maxK - K0), dimKL = Ks * L;
+            const size_t Ks = std::min(chunk, Kend - K0), dimKL = Ks * L;
             D.assign(np * dimKL, 0.0);
             Eb.assign(np * dimKL, 0.0);
             parallel_for(Ks, [&](size_t b, size_t e) {
@@ -406,7 +405,7 @@ struct Port {
         const size_t Kend = chunk_limit(maxKa, chunk);
         std::vector<double> D, Eb;
         for (size_t Ka0 = 0; Ka0 < Kend; Ka0 += chunk) {
-            const size_t Kas = std::min(chunk, maxKa - Ka0), Kdim = Kas * maxKb;
+            const size_t Kas = std::min(chunk, Kend - Ka0), Kdim = Kas * maxKb;
             D.assign(n2 * Kdim, 0.0);
             Eb.assign(n2 * Kdim, 0.0);
             parallel_for(Kas, [&](size_t b, size_t e) {
