@@ -53,6 +53,7 @@ def _declare(L):
         "f2g_spin_adapter_dump": (i32, [vp, P, P, P, P]),
         "f2g_dav_scratch_size": (i64, [i64]),
         "f2g_dav_dots": (i32, [P, i32, i64, P, i32, i64, i64, P, P, vp]),
+        "f2g_dav_dots_noalloc": (i32, [P, i32, i64, P, i32, i64, i64, P, vp]),
         "f2g_dav_lincomb": (i32, [P, i32, i64, P, i32, P, i64, d, i64, vp]),
         "f2g_dav_residual": (i32, [P, P, i32, i64, P, P, i32, P, i64, d, P, i64, P, P, vp]),
         "f2g_dav_eigh": (i32, [i32, P, P, P, vp]),

@@ -19,6 +19,8 @@ void dav_residual(const double* B, const double* S, int m, int64_t ld, const dou
                   const double* hdiag, int64_t n, double thresh, double* R, int64_t ldr, double* norms2, double* scratch,
                   cudaStream_t st);
 void dav_eigh(int m, const double* G, double* evals, double* evecs, cudaStream_t st);
+void dav_dots_noalloc(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n,
+                      double* out, cudaStream_t st);
 } // namespace f2g
 
 using namespace f2g;
@@ -342,6 +344,11 @@ int64_t f2g_dav_scratch_size(int64_t n) { return dav_scratch_size(n); }
 int f2g_dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n, double* out,
                  double* scratch, void* stream) {
     return guard([&] { dav_dots(A, na, lda, B, nb, ldb, n, out, scratch, S(stream)); });
+}
+
+int f2g_dav_dots_noalloc(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n,
+                         double* out, void* stream) {
+    return guard([&] { dav_dots_noalloc(A, na, lda, B, nb, ldb, n, out, S(stream)); });
 }
 
 int f2g_dav_lincomb(const double* X, int nx, int64_t ldx, const double* coef, int ny, double* Y, int64_t ldy,

@@ -11,6 +11,8 @@
 // All reductions are two-stage with a fixed order, so results are bitwise reproducible.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "common.cuh"
 
@@ -275,6 +277,67 @@ void dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int
 }
 
 int64_t dav_scratch_size(int64_t n) { return (int64_t)dots_blocks(n) * 4 * 256 + 64; }
+
+// ---- dots without a caller-provided scratch buffer --------------------------------------------
+// Some callers cannot allocate device memory when they need these dot products: a host program
+// whose device memory is handed out by its own pool (cudaMalloc would bypass the pool, and fails
+// once the pool has reserved the GPU's memory), or one that must not add the device-wide
+// synchronisation a cudaMalloc/cudaFree can cause in the middle of its iteration loop. For them
+// the per-block partial sums live in this file-scope static array instead of a caller buffer.
+// It is 304 blocks x 256 vector pairs of doubles (608 KB); every GPU that loads the library holds
+// it until the process exits. Each call overwrites exactly the partials it then reads, so nothing
+// has to start at zero. All calls share the array: calls that overlap on the GPU (different
+// streams, or several host threads) race on it and must be serialised by the caller.
+constexpr int kStaticBlocks = 304;
+constexpr int kStaticPairs = 256;
+static __device__ __align__(256) double g_static_partials[kStaticBlocks * kStaticPairs];
+
+namespace {
+std::mutex g_static_mu;
+double* g_static_ptr[128] = {};
+} // namespace
+
+// Device address of g_static_partials on the current device. In host code the array's name is only
+// a host-side stand-in, so the address is looked up once per device with that device current; the
+// first call on a device therefore does this set-up (it should come before any stream capture).
+static double* static_partials() {
+    int dev = 0;
+    F2G_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128)
+        throw Error(1, "dots_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_partials);
+        if (e != cudaSuccess || p == nullptr)
+            throw Error(3, std::string("dots_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+        g_static_ptr[dev] = static_cast<double*>(p);
+    }
+    return g_static_ptr[dev];
+}
+
+void dav_dots_noalloc(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n,
+                      double* out, cudaStream_t st) {
+    if (na < 0 || nb < 0 || n < 0)
+        throw Error(2, "dots_noalloc: negative size");
+    if (na * nb == 0)
+        return;
+    if (na > 64 || nb > 64)
+        throw Error(2, "dots_noalloc: at most 64 vectors per operand");
+    if ((int64_t)na * nb > kStaticPairs)
+        throw Error(2, "dots_noalloc: na * nb = " + std::to_string((int64_t)na * nb) +
+                           " vector pairs exceeds the static scratch limit of " + std::to_string(kStaticPairs) +
+                           " pairs per call");
+    double* partial = static_partials();
+    const int nbk = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTile - 1) / kTile, kStaticBlocks));
+    const size_t smem = (size_t)(na + nb) * (kTile + 1) * sizeof(double);
+    if (smem > 48 * 1024)
+        F2G_CUDA(cudaFuncSetAttribute(k_dots_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_dots_partial<<<nbk, 256, smem, st>>>(A, na, lda, B, nb, ldb, n, partial);
+    F2G_LAUNCH("k_dots_partial (static scratch)");
+    k_reduce_partials<<<ceil_div(na * nb, 128), 128, 0, st>>>(nbk, na * nb, partial, out);
+    F2G_LAUNCH("k_reduce_partials (static scratch)");
+}
 
 void dav_lincomb(const double* X, int nx, int64_t ldx, const double* coef, int ny, double* Y, int64_t ldy, double beta,
                  int64_t n, cudaStream_t st) {

@@ -102,6 +102,18 @@ int64_t f2g_dav_scratch_size(int64_t n);
 /* out[i * nb + j] = <A_i, B_j> */
 int f2g_dav_dots(const double* dev_A, int na, int64_t lda, const double* dev_B, int nb, int64_t ldb, int64_t n,
                  double* dev_out, double* dev_scratch, void* stream);
+/* The same dot products for callers that cannot allocate device memory when they need them: a host
+ * program whose device memory comes from its own pool (a cudaMalloc would bypass the pool and fails
+ * once the pool has reserved the GPU), or one that must not add the device-wide synchronisation
+ * a cudaMalloc/cudaFree can cause inside its iteration loop. No counterpart in the reference.
+ * Allocates nothing and takes no scratch argument: the partial sums live in a 608 KB static
+ * device array (304 blocks x 256 pairs) that every GPU loading the library holds until exit.
+ * Limit: na * nb <= 256 vector pairs per call (status 2 beyond), na, nb <= 64, any n. The first
+ * call on each device looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture. Every call reuses the same array, so
+ * calls that overlap on the GPU (other streams, other host threads) race and must be serialised. */
+int f2g_dav_dots_noalloc(const double* dev_A, int na, int64_t lda, const double* dev_B, int nb, int64_t ldb,
+                         int64_t n, double* dev_out, void* stream);
 /* Y_j = beta Y_j + sum_i coef[i * ny + j] X_i (Y must not alias X) */
 int f2g_dav_lincomb(const double* dev_X, int nx, int64_t ldx, const double* dev_coef, int ny, double* dev_Y,
                     int64_t ldy, double beta, int64_t n, void* stream);
