@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mode", default="sigma", choices=["sigma", "davidson"],
+                    help="sigma: sigma-builds/s (default); davidson: time to solution, FP64 vs mixed")
+    ap.add_argument("--nroot", type=int, default=1)
+    ap.add_argument("--e-tol", type=float, default=1e-10)
     return ap.parse_args()
 
 
@@ -225,6 +229,7 @@ def run_gb300(a):
     check = float(np.linalg.norm(hs))
     # mixed mode (FP32 sigma) throughput, same workload
     mixed = None
+    mixed_terms = None
     if not a.no_mixed:
         sb.set_precision("fp32")
         for _ in range(2):
@@ -237,6 +242,8 @@ def run_gb300(a):
         e1.record(stream)
         torch.cuda.synchronize()
         mixed = world * a.steps / max_over_ranks(e0.elapsed_time(e1) / 1e3, dist)
+        mt = sb.avg_build_time()
+        mixed_terms = {"total": 1e3 * mt[0], "aabb": 1e3 * mt[1], "aaaa_h1a_h0": 1e3 * mt[2], "bbbb_h1b": 1e3 * mt[3]}
         sb.set_precision("fp64")
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -262,6 +269,7 @@ def run_gb300(a):
             "terms_ms": {"total": 1e3 * tot, "aabb": 1e3 * t_ab, "aaaa_h1a_h0": 1e3 * t_aa, "bbbb_h1b": 1e3 * t_bb},
             "hz_dense_flops": f_hz, "sparse_flops": f_sp,
             "mixed_fp32_sigma_builds_per_s": mixed,
+            "mixed_fp32_terms_ms": mixed_terms,
             "clocks": clk,
             "cpu_baseline": cpu,
             "sigma_norm": check,
@@ -299,9 +307,43 @@ def run_reference(a):
     }), flush=True)
 
 
+def run_davidson(a):
+    """Davidson-Liu CASCI time to solution on one GPU: plain FP64 and mixed (FP32 iterations then
+    FP64 refinement), same seeded integrals; energies of the mixed run against the FP64 run."""
+    import torch
+
+    from forte2_gb300.ci import CASCISolver
+    from forte2_gb300.params import CIParams, DavidsonLiuParams
+
+    torch.cuda.set_device(0)
+    na, nb, _, _, ndet = cas_dims(a.norb, a.norb, 0)
+    ints = make_integrals(a.norb, ISEED if a.norb == NORB else 1000 + a.norb)
+    out = {"metric": f"CAS({a.norb},{a.norb}) Davidson time to solution", "unit": "s", "higher_is_better": False,
+           "config": {"workload": f"CAS({a.norb}e,{a.norb}o) Ms=0 singlet, {a.nroot} root(s), e_tol {a.e_tol}, "
+                                  f"r_tol 1e-6", "ndet": ndet}}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sol = CASCISolver(norb=a.norb, na=na, nb=nb, multiplicity=1, nroot=a.nroot, E=ints.E, H=ints.H, V=ints.V,
+                          ci_params=CIParams(precision=prec),
+                          davidson_liu_params=DavidsonLiuParams(e_tol=a.e_tol, maxiter=400)).run()
+        torch.cuda.synchronize()
+        res[prec] = {"seconds_total": time.perf_counter() - t0, "seconds_davidson": sol.timings["davidson"],
+                     "seconds_setup": sol.timings.get("startup", 0.0) + sol.timings.get("setup", 0.0),
+                     "converged": bool(sol.converged), "phases": sol.phases, "energies": [float(e) for e in sol.evals],
+                     "ncsf": sol.basis_size}
+    d = [abs(x - y) for x, y in zip(res["mixed"]["energies"], res["fp64"]["energies"])]
+    out.update({"fp64": res["fp64"], "mixed": res["mixed"], "mixed_vs_fp64_abs_dE": d,
+                "speedup_mixed_over_fp64_davidson": res["fp64"]["seconds_davidson"] / res["mixed"]["seconds_davidson"]})
+    print(json.dumps(out), flush=True)
+
+
 if __name__ == "__main__":
     args = parse()
-    if args.impl == "reference":
+    if args.mode == "davidson":
+        run_davidson(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

@@ -207,6 +207,10 @@ int f2g_sigma_set_precision(void* sb, int precision) {
         if (precision != kFP64 && precision != kFP32)
             throw Error(2, "precision must be 0 (FP64) or 1 (FP32)");
         if (precision != b->precision) {
+            b->flush_timers();
+            b->builds = 0;
+            for (double& t : b->t_acc)
+                t = 0.0;
             b->precision = precision;
             if (precision == kFP32)
                 b->set_hamiltonian(b->E, b->H.data(), b->V.data());
