@@ -7,10 +7,10 @@ CSF diagonal, build guess vectors from the lowest diagonal CSFs (ci.py:411-452),
 Davidson-Liu solver with the closure csf -> det -> H -> det -> csf (ci.py:221-235). Here every
 vector stays on the GPU and each Davidson block is transformed and sigma-built in one call.
 
-``precision="mixed"`` runs the Davidson iterations with FP32 sigma builds and then continues
-from the converged FP32 vectors with FP64 sigma builds until the requested tolerances are met
-(the final FP64 refinement); orthogonalisation, residual norms and the subspace eigensolve are
-FP64 throughout.
+``precision="mixed"`` runs the Davidson iterations with FP32 sigma builds, then refines the
+Ritz vectors by FP64 defect correction (``_solve_mixed``): a few FP64 sigma builds per root
+instead of FP64 Davidson iterations. Orthogonalisation, residual norms and the subspace
+eigensolves are FP64 throughout, and the reported energies come from an FP64 Rayleigh-Ritz step.
 """
 
 from __future__ import annotations
@@ -48,6 +48,7 @@ class CASCISolver:
     # FP32 phase tolerances of the mixed mode (the FP64 phase uses davidson_liu_params)
     mixed_e_tol: float = 1e-7
     mixed_r_tol: float = 1e-4
+    mixed_max_outer: int = 6
     seed: int = 12345
 
     def __post_init__(self):
@@ -152,24 +153,14 @@ class CASCISolver:
         t0 = time.perf_counter()
         self.phases = []
         if self.ci_params.precision == "mixed":
-            es = self.eigensolver
-            e_tol, r_tol = es.e_tol, es.r_tol
-            self.sigma_builder.set_precision("fp32")
-            es.e_tol, es.r_tol = max(e_tol, self.mixed_e_tol), max(r_tol, self.mixed_r_tol)
-            ev32, _ = es.solve()
-            self.phases.append(("fp32", es.iter + 1, es.sigma_builds, list(ev32)))
-            self.sigma_builder.set_precision("fp64")
-            es.e_tol, es.r_tol = e_tol, r_tol
-            b0 = es.sigma_builds
-            self.evals, evecs = es.solve()
-            self.phases.append(("fp64", es.iter + 1, es.sigma_builds - b0, list(self.evals)))
+            self.evals, evecs, self.converged = self._solve_mixed()
         else:
             self.evals, evecs = self.eigensolver.solve()
+            self.converged = self.eigensolver.converged
             self.phases.append(("fp64", self.eigensolver.iter + 1, self.eigensolver.sigma_builds, list(self.evals)))
         torch.cuda.synchronize()
         self.timings["davidson"] = time.perf_counter() - t0
         self.evecs = evecs
-        self.converged = self.eigensolver.converged
         if not self.converged and self.die_if_not_converged:
             raise RuntimeError("Davidson-Liu solver did not converge.")
         self.E_roots = self.evals
@@ -189,6 +180,92 @@ class CASCISolver:
         self.converged = True
         self.executed = True
         return self
+
+    def _solve_mixed(self):
+        """FP32 Davidson, then FP64 defect correction of the Ritz vectors.
+
+        Phase 1 runs the Davidson iterations with FP32 sigma builds. Then, for the current Ritz
+        vectors X (rows), each outer step builds S64 = H X in FP64 and S32 = H X in FP32 (nroot
+        builds each), performs an FP64 Rayleigh-Ritz in span(X) and checks the FP64 residual. If
+        not converged it continues the Davidson iterations, with FP32 sigma builds, on the
+        corrected operator H' = H32 + D X^T + X D^T - X (X^T D) X^T with D = S64 - S32, which
+        acts exactly as FP64 H on span(X) (its sigma for X is S64 itself) and as FP32 H elsewhere.
+        The error of X then shrinks by about |H64 - H32| / gap per outer step, so a solve needs a
+        few FP64 builds per root instead of FP64 Davidson iterations. Returns (evals, evecs
+        (size, nroot), converged) with the energies from the final FP64 Rayleigh-Ritz step.
+        """
+        torch = _torch()
+        es, sb = self.eigensolver, self.sigma_builder
+        e_tol, r_tol = es.e_tol, es.r_tol
+        k = self.nroot
+        plain = es._build_sigma
+        sb.set_precision("fp32")
+        es.e_tol, es.r_tol = max(e_tol, self.mixed_e_tol), max(r_tol, self.mixed_r_tol)
+        es.stall_window, es.stall_floor = 25, 1e-3
+        ev, _ = es.solve()
+        self.phases.append(("fp32", es.iter + 1, es.sigma_builds, [float(x) for x in ev]))
+        X = es.b[:k].clone()
+        S64 = torch.empty_like(X)
+        S32 = torch.empty_like(X)
+        lam_prev = None
+        converged = False
+        w = np.asarray(ev, dtype=np.float64)
+        for outer in range(self.mixed_max_outer):
+            sb.set_precision("fp64")
+            plain(X, S64)
+            sb.set_precision("fp32")
+            plain(X, S32)
+            # FP64 Rayleigh-Ritz in span(X)
+            G = es._dots(X, S64)
+            w, U = np.linalg.eigh(0.5 * (G + G.T))
+            if self.ci_params.energy_shift is not None:
+                o = np.argsort(np.abs(w - self.ci_params.energy_shift))
+                w, U = w[o], U[:, o]
+            for M in (X, S64, S32):
+                tmp = torch.empty_like(M)
+                es._lincomb(M, U, tmp, 0.0)
+                M.copy_(tmp)
+            R = S64.clone()
+            es._lincomb(X, -np.diag(w), R, 1.0)
+            rn = np.sqrt(np.maximum(np.diag(es._dots(R, R)), 0.0))
+            de = np.inf if lam_prev is None else float(np.max(np.abs(w - lam_prev)))
+            self.phases.append(("fp64-check", outer, 2 * k, [float(x) for x in w], float(rn.max()), de))
+            if rn.max() < r_tol and de < e_tol:
+                converged = True
+                break
+            lam_prev = w.copy()
+            D = S64 - S32
+            Mxd = es._dots(X, D)
+            Mxd = 0.5 * (Mxd + Mxd.T)
+
+            def corrected(B, S, X=X, D=D, Mxd=Mxd):
+                plain(B, S)
+                A = es._dots(X, B)  # (k, m): <x_i, b_l>
+                Bd = es._dots(D, B)  # (k, m): <d_i, b_l>
+                es._lincomb(D, A, S, 1.0)
+                es._lincomb(X, Bd - Mxd @ A, S, 1.0)
+
+            corrected.device_rows = True
+            es.add_sigma_builder(corrected)
+            # warm start from X with its exact corrected sigma (S64): no FP32 rebuild of X
+            es.b[:k].copy_(X)
+            es.sigma[:k].copy_(S64)
+            es.basis_size = es.sigma_size = k
+            es.lam_old[:k] = w
+            es.e_tol, es.r_tol = e_tol, 0.3 * r_tol
+            es.stall_window, es.stall_floor = 40, 1e-5
+            b0 = es.sigma_builds
+            ev, _ = es.solve()
+            self.phases.append(("fp32-corrected", es.iter + 1, es.sigma_builds - b0, [float(x) for x in ev]))
+            X = es.b[:k].clone()
+        es.add_sigma_builder(plain)
+        es.e_tol, es.r_tol = e_tol, r_tol
+        es.stall_window, es.stall_floor = 0, 0.0
+        sb.set_precision("fp64")
+        es.b[:k].copy_(X)
+        es.basis_size, es.sigma_size = k, 0
+        es.converged = converged
+        return w[:k], X.T, converged
 
     def avg_build_time(self):
         return self.sigma_builder.avg_build_time()

@@ -213,7 +213,7 @@ int f2g_sigma_set_precision(void* sb, int precision) {
                 t = 0.0;
             b->precision = precision;
             if (precision == kFP32)
-                b->set_hamiltonian(b->E, b->H.data(), b->V.data());
+                b->ensure_fp32();
         }
     });
 }

@@ -372,11 +372,23 @@ void SigmaBuilder::build_string_hamiltonian(int spin, StringHamiltonian& sh, boo
                                                             dH.get(), dV.get(), with_e0 ? E : 0.0, 3,
                                                             sh.col.get(), sh.val.get());
     F2G_LAUNCH("k_build_ss");
-    if (precision == kFP32) {
-        sh.valf.reserve(total);
-        k_convert<double, float><<<1024, 256, 0, st>>>((int64_t)total, sh.val.get(), sh.valf.get());
-        F2G_LAUNCH("k_convert");
+}
+
+// FP32 copies of the string-Hamiltonian values, made once per set of integrals on first use.
+void SigmaBuilder::ensure_fp32() {
+    if (fp32_ready)
+        return;
+    for (StringHamiltonian* sh : {&ha, &hb}) {
+        const int s_ = sh == &ha ? 0 : 1;
+        const size_t total = (size_t)s->spin(s_).N0 * sh->nnz;
+        if (total == 0)
+            continue;
+        sh->valf.reserve(total);
+        k_convert<double, float><<<1024, 256>>>((int64_t)total, sh->val.get(), sh->valf.get());
+        F2G_LAUNCH("k_convert string Hamiltonian");
     }
+    F2G_CUDA(cudaDeviceSynchronize());
+    fp32_ready = true;
 }
 
 void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_) {
@@ -397,6 +409,9 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
     build_string_hamiltonian(0, ha, true, 0);
     build_string_hamiltonian(1, hb, false, 0);
     F2G_CUDA(cudaDeviceSynchronize());
+    fp32_ready = false;
+    if (precision == kFP32)
+        ensure_fp32();
 }
 
 // The reference's K-block memory contract (ci_sigma_builder_knowles_handy.cc:15-32): every term

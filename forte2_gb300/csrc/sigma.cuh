@@ -47,6 +47,8 @@ struct SigmaBuilder {
     SigmaBuilder(CIStrings* s, double E, const double* H, const double* V, int log_level);
     ~SigmaBuilder();
     void set_hamiltonian(double E, const double* H, const double* V);
+    void ensure_fp32();
+    bool fp32_ready = false;
     void check_memory() const;
     void hamiltonian(const double* C, double* sigma, cudaStream_t st);
     // one HZ term into sigma (overwrites): 0 H0, 1 H1a, 2 H1b, 3 aabb, 4 aaaa(+H1a? no), 5 bbbb

@@ -51,6 +51,11 @@ class DavidsonLiuSolver:
     dtype: type = np.float64
     seed: int = 12345
     logger: object = None
+    # stop (unconverged) when the largest residual norm has not halved over this many iterations;
+    # 0 disables. Used by the FP32 phase of the mixed-precision driver, whose residuals stall at
+    # the FP32 rounding level.
+    stall_window: int = 0
+    stall_floor: float = 0.0  # the stall rule applies only once the residual is below this
 
     def __post_init__(self):
         p = self.davidson_liu_params
@@ -316,6 +321,12 @@ class DavidsonLiuSolver:
             if (max_de < self.e_tol and max_r < self.r_tol) or self.basis_size == self.size:
                 self.converged = True
                 break
+            w = self.stall_window
+            if w and len(self.history) > w:
+                recent = min(h[3] for h in self.history[-w:])
+                before = min(h[3] for h in self.history[:-w])
+                if recent > 0.5 * before and recent < self.stall_floor:
+                    break
             if self.iter == self.maxiter - 1:
                 break
             self.lam_old[:nroot] = lamr
