@@ -52,7 +52,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
-    ap.add_argument("--mode", default="sigma", choices=["sigma", "davidson"],
+    ap.add_argument("--instances", type=int, default=64, help="batched mode: number of instances")
+    ap.add_argument("--requests", type=int, default=10000, help="serve mode: number of requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve mode: mean arrivals per second")
+    ap.add_argument("--mode", default="sigma", choices=["sigma", "davidson", "batched", "serve"],
                     help="sigma: sigma-builds/s (default); davidson: time to solution, FP64 vs mixed")
     ap.add_argument("--nroot", type=int, default=1)
     ap.add_argument("--e-tol", type=float, default=1e-10)
@@ -341,9 +344,57 @@ def run_davidson(a):
     print(json.dumps(out), flush=True)
 
 
+def run_batched(a):
+    """64 independent CASCI instances, (8e,8o)-(12e,12o), multiplicities 1/3, 1-4 roots, solved
+    concurrently by the step scheduler, against a loop of plain single solves."""
+    import torch
+
+    from forte2_gb300.batch import batched_instances, solve_batched, solve_loop
+
+    torch.cuda.set_device(0)
+    inst = batched_instances(a.instances)
+    solve_batched(inst[:4])  # warm-up: library load, kernel attributes, allocator
+    out = {"metric": "batched CASCI instances/s", "unit": "instances/s", "higher_is_better": True,
+           "config": {"workload": f"{len(inst)} CASCI instances, (8e,8o)-(12e,12o), Ms=0, multiplicity 1/3, "
+                                  "1-4 roots, e_tol 1e-10", "sizes": {n: sum(1 for x in inst if x['norb'] == n)
+                                                                      for n in (8, 10, 12)}}}
+    for prec in a.precisions.split(","):
+        res_b, t_b, rounds = solve_batched(inst, prec)
+        res_l, t_l = solve_loop(inst, prec)
+        dev = max(max(abs(x - y) for x, y in zip(res_b[i].evals, res_l[i].evals)) for i in range(len(inst)))
+        out[prec] = {"batched_s": t_b, "loop_s": t_l, "instances_per_s": len(inst) / t_b,
+                     "loop_instances_per_s": len(inst) / t_l, "speedup": t_l / t_b, "rounds": rounds,
+                     "all_converged": all(res_b[i].converged for i in range(len(inst))),
+                     "max_abs_dE_batched_vs_loop": dev}
+    print(json.dumps(out), flush=True)
+
+
+def run_serve(a):
+    """Poisson stream of CASCI solves (6e,6o)-(16e,16o) weighted 1/Ndet, continuous batching under
+    an HBM budget; p50/p99 latency from arrival to result, and solves/s."""
+    import torch
+
+    from forte2_gb300.serve import poisson_stream, serve
+
+    torch.cuda.set_device(0)
+    reqs = poisson_stream(a.requests, rate=a.rate)
+    serve(poisson_stream(20, rate=1000.0, seed=99, sizes=(6, 8)))  # warm-up
+    out = {"metric": "solve-stream p50/p99 latency", "unit": "s", "higher_is_better": False,
+           "config": {"workload": f"{len(reqs)} requests, Poisson {a.rate}/s, (6e,6o)-(16e,16o) weight 1/Ndet, "
+                                  "multiplicity 1/3, 1-3 roots, e_tol 1e-10"}}
+    for prec in a.precisions.split(","):
+        stats, _, _ = serve(reqs, precision=prec)
+        out[prec] = stats
+    print(json.dumps(out), flush=True)
+
+
 if __name__ == "__main__":
     args = parse()
-    if args.mode == "davidson":
+    if args.mode == "batched":
+        run_batched(args)
+    elif args.mode == "serve":
+        run_serve(args)
+    elif args.mode == "davidson":
         run_davidson(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -21,7 +21,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .ci_helpers import CISigmaBuilder, CISpinAdapter, CIStrings
-from .davidson import DavidsonLiuSolver
+from .davidson import DavidsonLiuSolver, drive
 from .params import CIParams, DavidsonLiuParams
 
 
@@ -120,6 +120,13 @@ class CASCISolver:
         self.eigensolver.add_guesses(guess)
 
     def run(self):
+        """Solve (ci.py:185-208); returns self with evals, evecs, converged."""
+        out = drive(self.run_steps())
+        _torch().cuda.synchronize()
+        return out
+
+    def run_steps(self):
+        """Step generator of run() (see forte2_gb300.davidson.drive and forte2_gb300.batch)."""
         torch = _torch()
         t_all = time.perf_counter()
         if not self.executed:
@@ -149,16 +156,14 @@ class CASCISolver:
             self._build_guess(hdiag)
             self.rebuild_guess = False
         self.eigensolver.add_sigma_builder(self._make_sigma_closure())
-        torch.cuda.synchronize()
         t0 = time.perf_counter()
         self.phases = []
         if self.ci_params.precision == "mixed":
-            self.evals, evecs, self.converged = self._solve_mixed()
+            self.evals, evecs, self.converged = yield from self._solve_mixed_steps()
         else:
-            self.evals, evecs = self.eigensolver.solve()
+            self.evals, evecs = yield from self.eigensolver.solve_steps()
             self.converged = self.eigensolver.converged
             self.phases.append(("fp64", self.eigensolver.iter + 1, self.eigensolver.sigma_builds, list(self.evals)))
-        torch.cuda.synchronize()
         self.timings["davidson"] = time.perf_counter() - t0
         self.evecs = evecs
         if not self.converged and self.die_if_not_converged:
@@ -181,7 +186,7 @@ class CASCISolver:
         self.executed = True
         return self
 
-    def _solve_mixed(self):
+    def _solve_mixed_steps(self):
         """FP32 Davidson, then FP64 defect correction of the Ritz vectors.
 
         Phase 1 runs the Davidson iterations with FP32 sigma builds. Then, for the current Ritz
@@ -202,7 +207,7 @@ class CASCISolver:
         sb.set_precision("fp32")
         es.e_tol, es.r_tol = max(e_tol, self.mixed_e_tol), max(r_tol, self.mixed_r_tol)
         es.stall_window, es.stall_floor = 25, 1e-3
-        ev, _ = es.solve()
+        ev, _ = yield from es.solve_steps()
         self.phases.append(("fp32", es.iter + 1, es.sigma_builds, [float(x) for x in ev]))
         X = es.b[:k].clone()
         S64 = torch.empty_like(X)
@@ -216,7 +221,7 @@ class CASCISolver:
             sb.set_precision("fp32")
             plain(X, S32)
             # FP64 Rayleigh-Ritz in span(X)
-            G = es._dots(X, S64)
+            (G,) = yield [es._dots_dev(X, S64)]
             w, U = np.linalg.eigh(0.5 * (G + G.T))
             if self.ci_params.energy_shift is not None:
                 o = np.argsort(np.abs(w - self.ci_params.energy_shift))
@@ -227,7 +232,8 @@ class CASCISolver:
                 M.copy_(tmp)
             R = S64.clone()
             es._lincomb(X, -np.diag(w), R, 1.0)
-            rn = np.sqrt(np.maximum(np.diag(es._dots(R, R)), 0.0))
+            (RR,) = yield [es._dots_dev(R, R)]
+            rn = np.sqrt(np.maximum(np.diag(RR), 0.0))
             de = np.inf if lam_prev is None else float(np.max(np.abs(w - lam_prev)))
             self.phases.append(("fp64-check", outer, 2 * k, [float(x) for x in w], float(rn.max()), de))
             if rn.max() < r_tol and de < e_tol:
@@ -235,13 +241,14 @@ class CASCISolver:
                 break
             lam_prev = w.copy()
             D = S64 - S32
-            Mxd = es._dots(X, D)
+            Mxd = es._dots_dev(X, D)
             Mxd = 0.5 * (Mxd + Mxd.T)
 
             def corrected(B, S, X=X, D=D, Mxd=Mxd):
+                # enqueue only: H' B = H32 B + D (X B) + X (D B) - X Mxd (X B)
                 plain(B, S)
-                A = es._dots(X, B)  # (k, m): <x_i, b_l>
-                Bd = es._dots(D, B)  # (k, m): <d_i, b_l>
+                A = es._dots_dev(X, B)  # (k, m): <x_i, b_l>
+                Bd = es._dots_dev(D, B)  # (k, m): <d_i, b_l>
                 es._lincomb(D, A, S, 1.0)
                 es._lincomb(X, Bd - Mxd @ A, S, 1.0)
 
@@ -255,7 +262,7 @@ class CASCISolver:
             es.e_tol, es.r_tol = e_tol, 0.3 * r_tol
             es.stall_window, es.stall_floor = 40, 1e-5
             b0 = es.sigma_builds
-            ev, _ = es.solve()
+            ev, _ = yield from es.solve_steps()
             self.phases.append(("fp32-corrected", es.iter + 1, es.sigma_builds - b0, [float(x) for x in ev]))
             X = es.b[:k].clone()
         es.add_sigma_builder(plain)

@@ -2,13 +2,20 @@
 (forte2/helpers/davidsonliu.py:12-515).
 
 Basis, sigma and residual vectors live on the device as rows of (m, size) FP64 tensors; the
-subspace matrix, its eigendecomposition (Jacobi), residuals, preconditioner and
-Gram-Schmidt all run in the library's CUDA kernels. The host only reads back the handful of
-scalars that decide convergence (eigenvalues, residual norms, overlaps).
+subspace matrix, its eigendecomposition (Jacobi), residuals, preconditioner and Gram-Schmidt all
+run in the library's CUDA kernels. The host only reads back the handful of scalars that decide
+convergence (eigenvalues, residual norms, overlaps).
+
+The algorithm is written as a step generator (``solve_steps``): it enqueues device work and
+yields the list of small device tensors whose values it needs next; the driver copies them to
+the host after one synchronisation and sends the numpy arrays back. ``solve()`` drives one
+generator; ``forte2_gb300.batch`` interleaves many of them (batched and serving workloads), so
+that all solves in flight share one device synchronisation per round.
 
 Sigma builders: ``add_sigma_builder(f)`` takes ``f(basis_block, sigma_block)``. If ``f`` has the
-attribute ``device_rows = True`` it receives CUDA tensors of shape (m, size) (rows are vectors);
-otherwise it receives numpy arrays of shape (size, m) exactly as the reference passes them.
+attribute ``device_rows = True`` it receives CUDA tensors of shape (m, size) (rows are vectors)
+and only enqueues work; otherwise it receives numpy arrays of shape (size, m) exactly as the
+reference passes them.
 
 Differences from the reference, all at the level of rounding or documented choices:
   * Gram-Schmidt projects against all accepted vectors at once (classical Gram-Schmidt applied
@@ -21,7 +28,6 @@ Differences from the reference, all at the level of rounding or documented choic
 
 from __future__ import annotations
 
-import ctypes as C
 import time
 from dataclasses import dataclass, field
 
@@ -39,6 +45,18 @@ def _torch():
 
 def _ptr(t):
     return t.data_ptr()
+
+
+def drive(gen):
+    """Run a step generator to completion on the current stream; returns its return value."""
+    torch = _torch()
+    try:
+        req = next(gen)
+        while True:
+            torch.cuda.current_stream().synchronize()
+            req = gen.send([t.cpu().numpy() for t in req])
+    except StopIteration as e:
+        return e.value
 
 
 @dataclass
@@ -83,9 +101,6 @@ class DavidsonLiuSolver:
         self.r = torch.zeros((max(self.nroot, m), n), dtype=f64, device=dev)
         self.tmp = torch.zeros((max(self.nroot, m), n), dtype=f64, device=dev)
         self.scratch = torch.zeros(int(lib().f2g_dav_scratch_size(n)), dtype=f64, device=dev)
-        self.dbuf = torch.zeros(4096, dtype=f64, device=dev)  # results of dots
-        self.gbuf = torch.zeros(2 * 64 * 64 + 64, dtype=f64, device=dev)  # subspace matrix + eigenpairs
-        self.nbuf = torch.zeros(64, dtype=f64, device=dev)  # residual norms
         self.h_diag = None
         self.lam = np.zeros(m)
         self.lam_old = np.zeros(m)
@@ -110,7 +125,9 @@ class DavidsonLiuSolver:
 
     def add_h_diag(self, h_diag):
         torch = _torch()
-        t = torch.as_tensor(h_diag, dtype=torch.float64).reshape(-1)
+        if not isinstance(h_diag, torch.Tensor):
+            h_diag = torch.as_tensor(np.array(h_diag, dtype=np.float64))
+        t = h_diag.to(torch.float64).reshape(-1)
         if t.shape != (self.size,):
             raise ValueError("h_diag must be shape (size,)")
         self.h_diag = t.to("cuda").contiguous().clone()
@@ -123,6 +140,7 @@ class DavidsonLiuSolver:
         self._guesses = G.to("cuda").T.contiguous()  # rows
 
     def add_project_out(self, project_out):
+        """Vectors to project out (davidsonliu.py:150-172); shorter vectors are zero-padded."""
         torch = _torch()
         if len(project_out) == 0:
             return
@@ -130,78 +148,97 @@ class DavidsonLiuSolver:
             if len(v) > self.size:
                 raise ValueError(
                     f"Each project_out vector must have length at most {self.size}, but got {len(v)}")
-        lens = {len(v) for v in project_out}
-        L = max(lens)
         A = torch.zeros((len(project_out), self.size), dtype=torch.float64, device="cuda")
         for i, v in enumerate(project_out):
             A[i, : len(v)] = torch.as_tensor(np.asarray(v, dtype=np.float64), device="cuda")
-        # orthonormalise (the reference uses a QR of the stacked vectors)
         Q = torch.zeros_like(A)
         k = 0
         for i in range(A.shape[0]):
-            ok, v = self._orthonormalize(Q[:k], A[i].clone())
+            ok, v = drive(self._orthonormalize_steps(Q[:k], A[i].clone()))
             if ok:
                 Q[k] = v
                 k += 1
         self._proj_out = Q[:k].contiguous()
-        self._proj_len = L
 
-    # ---- device primitives ----
-    def _dots(self, A, B):
-        """<A_i, B_j> for row blocks A (na, n), B (nb, n) -> numpy (na, nb)."""
+    # ---- device primitives (enqueue only) ----
+    def _dots_dev(self, A, B):
+        """Device tensor (na, nb) of <A_i, B_j> for row blocks A, B."""
+        torch = _torch()
         na, nb = A.shape[0], B.shape[0]
-        if na == 0 or nb == 0:
-            return np.zeros((na, nb))
-        out = self.dbuf[: na * nb]
-        check(lib().f2g_dav_dots(_ptr(A), na, A.stride(0), _ptr(B), nb, B.stride(0), self.size, _ptr(out),
-                                 _ptr(self.scratch), stream_handle()))
-        return out.cpu().numpy().reshape(na, nb)
+        out = torch.empty((max(na, 1), max(nb, 1)), dtype=torch.float64, device="cuda")
+        if na and nb:
+            check(lib().f2g_dav_dots(_ptr(A), na, A.stride(0), _ptr(B), nb, B.stride(0), self.size, _ptr(out),
+                                     _ptr(self.scratch), stream_handle()))
+        return out[:na, :nb]
 
     def _lincomb(self, X, coef, Y, beta):
-        """Y_j = beta Y_j + sum_i coef[i, j] X_i (coef numpy (nx, ny))."""
+        """Y_j = beta Y_j + sum_i coef[i, j] X_i; coef is numpy (nx, ny) or a device tensor."""
         torch = _torch()
         nx, ny = coef.shape
         if nx == 0 or ny == 0:
             if beta != 1.0 and ny:
                 Y.mul_(beta)
             return
-        c = torch.as_tensor(np.ascontiguousarray(coef, dtype=np.float64)).to("cuda", non_blocking=False)
+        if isinstance(coef, torch.Tensor):
+            c = coef.contiguous()
+        else:
+            c = torch.as_tensor(np.ascontiguousarray(coef, dtype=np.float64)).to("cuda", non_blocking=False)
         check(lib().f2g_dav_lincomb(_ptr(X), nx, X.stride(0), _ptr(c), ny, _ptr(Y), Y.stride(0), float(beta),
                                     self.size, stream_handle()))
 
+    def _dots(self, A, B):
+        """Blocking <A_i, B_j> -> numpy (na, nb) (for callers outside a step generator)."""
+        return drive(self._read_steps(self._dots_dev(A, B)))
+
+    @staticmethod
+    def _read_steps(t):
+        (h,) = yield [t]
+        return h
+
+    # ---- step routines: enqueue device work, `yield [tensors]` to read values on the host ----
     def do_project_out(self, A):
-        """A_i -> (1 - u u^T) A_i for every stored project-out vector u (davidsonliu.py:174-182)."""
+        """A_i -> (1 - u u^T) A_i for every stored project-out vector u (davidsonliu.py:174-182).
+        Enqueue only: the projections are consumed on the device."""
         if not hasattr(self, "_proj_out") or A.shape[0] == 0:
             return
         for k in range(self._proj_out.shape[0]):
             u = self._proj_out[k : k + 1]
-            v = self._dots(u, A)  # (1, nA)
+            v = self._dots_dev(u, A)  # (1, nA)
             self._lincomb(u, -v, A, 1.0)
 
-    def orthonormality_check(self, b, msg="Orthonormality check failed."):
+    def _orthonormality_steps(self, b, msg="Orthonormality check failed."):
         if b.shape[0] == 0:
             return
-        S = self._dots(b, b)
+        (S,) = yield [self._dots_dev(b, b)]
         if not np.allclose(S, np.eye(S.shape[0]), atol=1e-11):
             raise ValueError(msg + f" Largest deviation from orthonormality: {np.max(np.abs(S - np.eye(S.shape[0])))}")
 
-    def _orthonormalize(self, A, v):
+    def orthonormality_check(self, b, msg="Orthonormality check failed."):
+        drive(self._orthonormality_steps(b, msg))
+
+    def _orthonormalize_steps(self, A, v):
         """Orthonormalise v against the rows of A (davidsonliu.py:438-484). Returns (ok, v)."""
+        vr = v[None, :]
         for _ in range(10):
             if A.shape[0]:
-                d = self._dots(A, v[None, :])  # (nA, 1)
-                self._lincomb(A, -d, v[None, :], 1.0)
-            nrm = float(np.sqrt(max(self._dots(v[None, :], v[None, :])[0, 0], 0.0)))
+                d = self._dots_dev(A, vr)
+                self._lincomb(A, -d, vr, 1.0)
+            (nrm2,) = yield [self._dots_dev(vr, vr)]
+            nrm = float(np.sqrt(max(nrm2[0, 0], 0.0)))
             if nrm < self.schmidt_discard_threshold:
                 return False, v
             v.mul_(1.0 / nrm)
-            max_overlap = float(np.abs(self._dots(A, v[None, :])).max()) if A.shape[0] else 0.0
-            norm2 = float(self._dots(v[None, :], v[None, :])[0, 0])
-            if max_overlap < self.schmidt_orthogonality_threshold and abs(norm2 - 1.0) < self.schmidt_orthogonality_threshold:
+            if A.shape[0]:
+                ov, n2 = yield [self._dots_dev(A, vr), self._dots_dev(vr, vr)]
+                max_overlap = float(np.abs(ov).max())
+            else:
+                (n2,) = yield [self._dots_dev(vr, vr)]
+                max_overlap = 0.0
+            if max_overlap < self.schmidt_orthogonality_threshold and abs(float(n2[0, 0]) - 1.0) < self.schmidt_orthogonality_threshold:
                 return True, v
         return False, v
 
-    def add_rows_and_orthonormalize(self, n_existing, candidates):
+    def _add_rows_steps(self, n_existing, candidates):
         """Append orthonormalised candidate rows after the first n_existing basis rows."""
         added = 0
         cap = self.max_subspace_size - n_existing
@@ -209,7 +246,7 @@ class DavidsonLiuSolver:
             raise ValueError(f"Cannot add {candidates.shape[0]} candidates into {cap} slots")
         for j in range(candidates.shape[0]):
             v = candidates[j].clone()
-            ok, v = self._orthonormalize(self.b[: n_existing + added], v)
+            ok, v = yield from self._orthonormalize_steps(self.b[: n_existing + added], v)
             if ok:
                 self.b[n_existing + added].copy_(v)
                 added += 1
@@ -219,77 +256,69 @@ class DavidsonLiuSolver:
         torch = _torch()
         return torch.rand((k, self.size), generator=self._gen, dtype=torch.float64, device="cuda") * 2.0 - 1.0
 
-    def _call_sigma(self, lo, hi):
+    def _sigma_steps(self, lo, hi):
         if getattr(self._build_sigma, "device_rows", False):
             self._build_sigma(self.b[lo:hi], self.sigma[lo:hi])
         else:
             torch = _torch()
-            B = self.b[lo:hi].T.cpu().numpy().copy()
+            (B,) = yield [self.b[lo:hi]]
+            B = np.ascontiguousarray(B.T)
             S = np.zeros_like(B)
             self._build_sigma(B, S)
-            self.sigma[lo:hi].copy_(torch.as_tensor(S.T.copy()).to("cuda"))
+            self.sigma[lo:hi].copy_(torch.as_tensor(np.ascontiguousarray(S.T)).to("cuda"))
         self.sigma_builds += hi - lo
 
-    def _eigh(self, m):
+    def _eigh_dev(self, m):
+        """Enqueue the subspace matrix B S^T and its Jacobi eigendecomposition; returns (evals, evecs)."""
         torch = _torch()
-        G = self.gbuf[: m * m]
-        # subspace matrix B S^T, hermitized inside the eigensolver
-        check(lib().f2g_dav_dots(_ptr(self.b), m, self.b.stride(0), _ptr(self.sigma), m, self.sigma.stride(0),
-                                 self.size, _ptr(G), _ptr(self.scratch), stream_handle()))
-        ev = self.gbuf[m * m : m * m + m]
-        vec = self.gbuf[m * m + m : 2 * m * m + m]
+        G = self._dots_dev(self.b[:m], self.sigma[:m]).contiguous()
+        ev = torch.empty(m, dtype=torch.float64, device="cuda")
+        vec = torch.empty((m, m), dtype=torch.float64, device="cuda")
         check(lib().f2g_dav_eigh(m, _ptr(G), _ptr(ev), _ptr(vec), stream_handle()))
-        lam = ev.cpu().numpy().copy()
-        alpha = vec.cpu().numpy().reshape(m, m).copy()
-        if self.energy_shift is not None:
-            idx = np.argsort(np.abs(lam - self.energy_shift))
-            lam, alpha = lam[idx], alpha[:, idx]
-        return lam, alpha
+        return ev, vec
 
-    def _collapse(self, alpha):
+    def _collapse_steps(self, alpha):
         k = min(self.collapse_size, self.basis_size)
         m = self.basis_size
-        self.orthonormality_check(self.b[:m], f"Before collapse: Checking orthonormality of Bblk with size {m}")
+        yield from self._orthonormality_steps(self.b[:m], f"Before collapse: Checking orthonormality of Bblk with size {m}")
         self._lincomb(self.b[:m], alpha[:m, :k], self.tmp[:k], 0.0)
         self.b[:k].copy_(self.tmp[:k])
         self._lincomb(self.sigma[:m], alpha[:m, :k], self.tmp[:k], 0.0)
         self.sigma[:k].copy_(self.tmp[:k])
         self.basis_size = k
         self.sigma_size = k
-        self.orthonormality_check(self.b[:k], f"After collapse: Checking orthonormality of newB with size {k}")
+        yield from self._orthonormality_steps(self.b[:k], f"After collapse: Checking orthonormality of newB with size {k}")
 
     def _log(self, msg):
         if self.logger is not None and self.log_level > 0:
             self.logger(msg)
 
     # ---- solve (davidsonliu.py:184-387) ----
-    def solve(self):
+    def solve_steps(self):
+        """Step generator of solve(): yields lists of device tensors to read, returns (evals, evecs)."""
         if self._build_sigma is None:
             raise ValueError("Sigma builder function is not set.")
         if self.h_diag is None:
             raise ValueError("Hamiltonian diagonal is not set.")
         torch = _torch()
         if not self._executed:
-            if hasattr(self, "_guesses"):
-                G = self._guesses.clone()
-            else:
-                G = self._random_rows(self.nroot)
+            G = self._guesses.clone() if hasattr(self, "_guesses") else self._random_rows(self.nroot)
             self.do_project_out(G)
             k = 0
             for j in range(min(G.shape[0], self.max_subspace_size)):
-                ok, v = self._orthonormalize(self.b[:k], G[j].clone())
+                ok, v = yield from self._orthonormalize_steps(self.b[:k], G[j].clone())
                 if ok:
                     self.b[k].copy_(v)
                     k += 1
             while k < min(self.nroot, self.max_subspace_size):  # dependent guesses: fill at random
-                ok, v = self._orthonormalize(self.b[:k], self._random_rows(1)[0])
+                ok, v = yield from self._orthonormalize_steps(self.b[:k], self._random_rows(1)[0])
                 if ok:
                     self.b[k].copy_(v)
                     k += 1
             self.basis_size = k
             self.sigma_size = 0
             self.lam_old[:] = 0.0
-        self.orthonormality_check(self.b[: self.basis_size])
+        yield from self._orthonormality_steps(self.b[: self.basis_size])
         self.iter = 0
         self.converged = False
         self.history = []
@@ -297,24 +326,28 @@ class DavidsonLiuSolver:
         for self.iter in range(self.maxiter):
             t0 = time.perf_counter()
             if self.basis_size > self.sigma_size:
-                self._call_sigma(self.sigma_size, self.basis_size)
+                yield from self._sigma_steps(self.sigma_size, self.basis_size)
                 self.sigma_size = self.basis_size
             m = self.basis_size
             if hasattr(self, "_proj_out"):
                 self.do_project_out(self.sigma[:m])
-            lam, alpha = self._eigh(m)
+            ev, vec = self._eigh_dev(m)
+            lam, alpha = yield [ev, vec]
+            if self.energy_shift is not None:
+                idx = np.argsort(np.abs(lam - self.energy_shift))
+                lam, alpha = lam[idx], alpha[:, idx]
             self.lam[:m] = lam
             self.alpha[:m, :m] = alpha
             lamr = lam[:nroot].copy()
-            ar = np.ascontiguousarray(alpha[:, :nroot])
-            d_alpha = torch.as_tensor(ar).to("cuda")
+            d_alpha = torch.as_tensor(np.ascontiguousarray(alpha[:, :nroot])).to("cuda")
             d_lam = torch.as_tensor(lamr).to("cuda")
-            norms2 = self.nbuf[:nroot]
+            norms2 = torch.empty(nroot, dtype=torch.float64, device="cuda")
             check(lib().f2g_dav_residual(_ptr(self.b), _ptr(self.sigma), m, self.b.stride(0), _ptr(d_alpha),
                                          _ptr(d_lam), nroot, _ptr(self.h_diag), self.size,
                                          self.preconditioner_denom_threshold, _ptr(self.r), self.r.stride(0),
                                          _ptr(norms2), _ptr(self.scratch), stream_handle()))
-            rnorms = np.sqrt(np.maximum(norms2.cpu().numpy(), 0.0))
+            (n2,) = yield [norms2]
+            rnorms = np.sqrt(np.maximum(n2, 0.0))
             max_de = float(np.max(np.abs(lamr - self.lam_old[:nroot])))
             max_r = float(rnorms.max())
             self.history.append((self.iter, float(lamr.mean()), max_de, max_r, m, time.perf_counter() - t0))
@@ -331,27 +364,25 @@ class DavidsonLiuSolver:
                 break
             self.lam_old[:nroot] = lamr
             if self.basis_size + nroot > self.max_subspace_size:
-                self._collapse(alpha)
+                yield from self._collapse_steps(alpha)
             m = self.basis_size
             R0 = self.r[:nroot]
-            # R0 -= B (B^T R0)
-            d = self._dots(self.b[:m], R0)
+            d = self._dots_dev(self.b[:m], R0)  # R0 -= B (B^T R0), on the device
             self._lincomb(self.b[:m], -d, R0, 1.0)
             self.do_project_out(R0)
             to_add = min(nroot, self.max_subspace_size - self.basis_size)
             if to_add == 0:
                 self.converged = True
                 break
-            added = self.add_rows_and_orthonormalize(self.basis_size, R0[:to_add])
+            added = yield from self._add_rows_steps(self.basis_size, R0[:to_add])
             self.basis_size += added
             if added < to_add:
                 temp = self._random_rows(to_add - added)
                 self.do_project_out(temp)
-                added2 = self.add_rows_and_orthonormalize(self.basis_size, temp)
+                added2 = yield from self._add_rows_steps(self.basis_size, temp)
                 self.basis_size += added2
             self._log(f"iter {self.iter:4d} <E> {lamr.mean():20.12f} max(dE) {max_de:+.4e} max(r) {max_r:+.4e} "
                       f"basis {self.basis_size}")
-        # final eigenpairs
         m = self.basis_size
         lamr = self.lam[:nroot].copy()
         self._lincomb(self.b[:m], self.alpha[:m, :nroot], self.tmp[:nroot], 0.0)
@@ -361,3 +392,7 @@ class DavidsonLiuSolver:
         self._executed = True
         self.evecs_rows = self.b[:nroot]
         return lamr, self.b[:nroot].T
+
+    def solve(self):
+        """Run to convergence (or maxiter) on the current stream; returns (evals, evecs (size, nroot))."""
+        return drive(self.solve_steps())

@@ -1,0 +1,98 @@
+"""Continuous-batching CASCI solve server on one GPU.
+
+Requests (active space, multiplicity, roots, integrals) arrive over time. Each round of the step
+scheduler admits waiting requests in arrival order while the estimated HBM footprint of all
+solves in flight stays within the budget, so requests that arrive while others run join as soon
+as memory frees up, and their kernels overlap on the device with the others'. Latency is measured
+from a request's arrival to its result.
+"""
+
+from __future__ import annotations
+
+import time
+from collections import deque
+from dataclasses import dataclass
+from math import comb
+
+import numpy as np
+
+from .batch import StepScheduler, footprint_bytes, make_solver
+
+
+@dataclass
+class Request:
+    idx: int
+    arrival: float  # seconds after the start of the stream
+    norb: int
+    multiplicity: int
+    nroot: int
+    iseed: int
+
+    @property
+    def inst(self):
+        return dict(norb=self.norb, na=self.norb // 2, nb=self.norb // 2, multiplicity=self.multiplicity,
+                    nroot=self.nroot, iseed=self.iseed)
+
+
+def poisson_stream(n_requests=10000, rate=200.0, seed=5, sizes=(6, 8, 10, 12, 14, 16)):
+    """The serving workload: Poisson arrivals at `rate` per second; active spaces (n e, n o), Ms = 0,
+    drawn with weight 1/Ndet(n); multiplicity 1 or 3; 1-3 roots; per-request seeded integrals."""
+    rng = np.random.default_rng(seed)
+    w = np.array([1.0 / comb(n, n // 2) ** 2 for n in sizes])
+    w /= w.sum()
+    t = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    n = rng.choice(sizes, size=n_requests, p=w)
+    mult = rng.choice([1, 3], size=n_requests)
+    roots = rng.integers(1, 4, size=n_requests)
+    return [Request(i, float(t[i]), int(n[i]), int(mult[i]), int(roots[i]), 7_000_000 + i) for i in range(n_requests)]
+
+
+def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1e-10, max_inflight=256):
+    """Serve a request stream in real time; returns per-request latencies and summary stats."""
+    sched = StepScheduler(nstreams)
+    pending = deque(sorted(requests, key=lambda r: r.arrival))
+    waiting = deque()
+    used = [0]
+    lat = {}
+    energies = {}
+    t_start = time.perf_counter()
+    peak = [0, 0]
+
+    def admit(now, active):
+        rel = now - t_start
+        while pending and pending[0].arrival <= rel:
+            waiting.append(pending.popleft())
+        new = []
+        while waiting and len(active) + len(new) < max_inflight:
+            r = waiting[0]
+            fp = footprint_bytes(r.norb, r.norb // 2, r.norb // 2, r.nroot)
+            if used[0] + fp > hbm_budget and (active or new):
+                break
+            waiting.popleft()
+            used[0] += fp
+            new.append((r, make_solver(r.inst, precision, e_tol=e_tol).run_steps(), fp))
+        peak[0] = max(peak[0], len(active) + len(new))
+        peak[1] = max(peak[1], used[0])
+        if not new and not active and not waiting:
+            if not pending:
+                return None
+            # idle until the next arrival
+            time.sleep(max(0.0, pending[0].arrival - (time.perf_counter() - t_start)))
+        return new
+
+    def on_done(job):
+        r = job.key
+        used[0] -= job.footprint
+        lat[r.idx] = (job.t_done - t_start) - r.arrival
+        energies[r.idx] = [float(e) for e in job.result.evals]
+
+    sched.run(admit=admit, on_done=on_done)
+    wall = time.perf_counter() - t_start
+    L = np.array([lat[r.idx] for r in requests])
+    return {
+        "requests": len(requests), "precision": precision, "wall_s": wall,
+        "solves_per_s": len(requests) / wall, "p50_latency_s": float(np.percentile(L, 50)),
+        "p99_latency_s": float(np.percentile(L, 99)), "mean_latency_s": float(L.mean()),
+        "max_inflight": peak[0], "peak_footprint_gb": peak[1] / 2**30, "rounds": sched.rounds,
+        "sizes": {int(n): int(sum(1 for r in requests if r.norb == n)) for n in sorted({r.norb for r in requests})},
+    }, lat, energies

@@ -1,0 +1,46 @@
+"""Batched instances and the continuous-batching server: every result equals its solo solve."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batched_equals_loop(cuda):
+    from forte2_gb300.batch import batched_instances, solve_batched, solve_loop
+
+    inst = batched_instances(6, seed=11)
+    for x in inst:  # keep the test quick: the smaller spaces of the batched workload
+        x["norb"] = min(x["norb"], 8)
+        x["na"] = x["nb"] = x["norb"] // 2
+    loop, _ = solve_loop(inst)
+    batched, _, rounds = solve_batched(inst, nstreams=4)
+    assert rounds > 0
+    for i in range(len(inst)):
+        assert batched[i].converged and loop[i].converged
+        np.testing.assert_allclose(batched[i].evals, loop[i].evals, rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
+def test_serving_results_equal_solo(cuda, precision, tol):
+    from forte2_gb300.batch import make_solver
+    from forte2_gb300.serve import poisson_stream, serve
+
+    reqs = poisson_stream(40, rate=2000.0, seed=3, sizes=(6, 8, 10))
+    stats, lat, energies = serve(reqs, precision=precision, nstreams=8)
+    assert stats["requests"] == 40 and stats["max_inflight"] > 1
+    assert len(lat) == 40 and all(v >= 0 for v in lat.values())
+    for r in reqs[::5]:
+        solo = make_solver(r.inst, precision).run()
+        np.testing.assert_allclose(energies[r.idx], solo.evals, rtol=0, atol=tol)
+
+
+def test_serving_admission_respects_budget(cuda):
+    from forte2_gb300.batch import footprint_bytes
+    from forte2_gb300.serve import poisson_stream, serve
+
+    reqs = poisson_stream(12, rate=5000.0, seed=4, sizes=(6, 8))
+    one = max(footprint_bytes(r.norb, r.norb // 2, r.norb // 2, r.nroot) for r in reqs)
+    stats, lat, _ = serve(reqs, hbm_budget=2 * one, nstreams=4)
+    assert stats["peak_footprint_gb"] * 2**30 <= 2 * one + 1
+    assert len(lat) == 12
