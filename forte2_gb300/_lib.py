@@ -57,6 +57,17 @@ def _declare(L):
         "f2g_dav_lincomb": (i32, [P, i32, i64, P, i32, P, i64, d, i64, vp]),
         "f2g_dav_residual": (i32, [P, P, i32, i64, P, P, i32, P, i64, d, P, i64, P, P, vp]),
         "f2g_dav_eigh": (i32, [i32, P, P, P, vp]),
+        "f2g_dav_gs_append": (i32, [P, i64, i32, i32, P, i64, i32, i64, d, d, i32, C.c_uint64, P, vp]),
+        "f2g_dgraph_create": (i32, [vp, vp, i64, i32, i32, i32, i32, C.c_uint64, i32, P, P, P, P, P, i64, i64, i64,
+                                    P, pp]),
+        "f2g_dgraph_destroy": (i32, [vp]),
+        "f2g_dgraph_set_correction": (i32, [vp, P, P, i64, P, i32]),
+        "f2g_dgraph_reset": (i32, [vp, i32, i32, P, i32, d, d, i32, i32, d, vp]),
+        "f2g_dgraph_launch": (i32, [vp, vp]),
+        "f2g_dgraph_state": (i32, [vp, P, P]),
+        "f2g_dgraph_ritz": (i32, [vp, P, i64, vp]),
+        "f2g_dgraph_history": (i32, [vp, P, i32]),
+        "f2g_sigma_set_hamiltonian_async": (i32, [vp, d, P, P, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

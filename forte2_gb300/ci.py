@@ -50,6 +50,8 @@ class CASCISolver:
     mixed_r_tol: float = 1e-4
     mixed_max_outer: int = 6
     seed: int = 12345
+    # graph-captured Davidson iterations: None = automatic (small CSF spaces), True/False = force
+    use_graph: bool = None
 
     def __post_init__(self):
         self.executed = False
@@ -82,6 +84,15 @@ class CASCISolver:
         self.rebuild_guess = True
         self.eigensolver = None
 
+    def new_problem(self, E, H, V):
+        """Next solve of the same active space with other integrals, from fresh guesses. Keeps the
+        strings, spin adapter, sigma builder, eigensolver buffers and captured graphs (no
+        counterpart in the reference; a solver pool of the serving loop uses it)."""
+        self.set_ints(E, H, V)
+        self.rebuild_guess = True
+        if self.eigensolver is not None:
+            self.eigensolver.restart()
+
     def _make_sigma_closure(self):
         torch = _torch()
         sa, sb = self.spin_adapter, self.sigma_builder
@@ -100,6 +111,7 @@ class CASCISolver:
             sa.det_C_to_csf_C(sdet, S)
 
         sigma_builder.device_rows = True
+        sigma_builder.graph = (sb, sa, None)  # lets the eigensolver capture the same closure in a CUDA graph
         return sigma_builder
 
     def _build_guess(self, hdiag):
@@ -132,7 +144,13 @@ class CASCISolver:
         if not self.executed:
             self._startup()
         t0 = time.perf_counter()
-        self.sigma_builder = CISigmaBuilder(self.ci_strings, self.E, self.H, self.V, self.log_level)
+        if getattr(self, "sigma_builder", None) is None:
+            self.sigma_builder = CISigmaBuilder(self.ci_strings, self.E, self.H, self.V, self.log_level)
+        else:
+            # same strings: new integrals into the same builder, ordered on this stream (the first
+            # host read below, in the guess, synchronises the stream before the builder is read)
+            self.sigma_builder.update_integrals(self.E, self.H, self.V)
+            self.sigma_builder.set_precision("fp64")
         self.sigma_builder.set_memory(self.ci_params.ci_builder_memory)
         alg = self.ci_params.ci_algorithm.lower()
         if alg == "exact":
@@ -150,7 +168,8 @@ class CASCISolver:
             self.eigensolver = DavidsonLiuSolver(size=self.basis_size, nroot=self.nroot,
                                                  davidson_liu_params=self.davidson_liu_params,
                                                  energy_shift=self.ci_params.energy_shift,
-                                                 log_level=self.log_level, seed=self.seed)
+                                                 log_level=self.log_level, seed=self.seed,
+                                                 use_graph=self.use_graph)
         self.eigensolver.add_h_diag(hdiag)
         if self.rebuild_guess:
             self._build_guess(hdiag)
@@ -209,9 +228,13 @@ class CASCISolver:
         es.stall_window, es.stall_floor = 25, 1e-3
         ev, _ = yield from es.solve_steps()
         self.phases.append(("fp32", es.iter + 1, es.sigma_builds, [float(x) for x in ev]))
-        X = es.b[:k].clone()
-        S64 = torch.empty_like(X)
-        S32 = torch.empty_like(X)
+        # persistent buffers: a captured graph of the corrected phase keeps their addresses
+        if getattr(self, "_mixed_bufs", None) is None or self._mixed_bufs[0].shape != (k, es.size):
+            shape = (k, es.size)
+            self._mixed_bufs = tuple(torch.zeros(shape, dtype=torch.float64, device="cuda") for _ in range(4)) + (
+                torch.zeros((k, k), dtype=torch.float64, device="cuda"),)
+        X, S64, S32, D, Mb = self._mixed_bufs
+        X.copy_(es.b[:k])
         lam_prev = None
         converged = False
         w = np.asarray(ev, dtype=np.float64)
@@ -240,11 +263,11 @@ class CASCISolver:
                 converged = True
                 break
             lam_prev = w.copy()
-            D = S64 - S32
+            torch.sub(S64, S32, out=D)
             Mxd = es._dots_dev(X, D)
-            Mxd = 0.5 * (Mxd + Mxd.T)
+            Mb.copy_(0.5 * (Mxd + Mxd.T))
 
-            def corrected(B, S, X=X, D=D, Mxd=Mxd):
+            def corrected(B, S, X=X, D=D, Mxd=Mb):
                 # enqueue only: H' B = H32 B + D (X B) + X (D B) - X Mxd (X B)
                 plain(B, S)
                 A = es._dots_dev(X, B)  # (k, m): <x_i, b_l>
@@ -253,6 +276,7 @@ class CASCISolver:
                 es._lincomb(X, Bd - Mxd @ A, S, 1.0)
 
             corrected.device_rows = True
+            corrected.graph = (sb, self.spin_adapter, (X, D, Mb, k))
             es.add_sigma_builder(corrected)
             # warm start from X with its exact corrected sigma (S64): no FP32 rebuild of X
             es.b[:k].copy_(X)
@@ -264,7 +288,7 @@ class CASCISolver:
             b0 = es.sigma_builds
             ev, _ = yield from es.solve_steps()
             self.phases.append(("fp32-corrected", es.iter + 1, es.sigma_builds - b0, [float(x) for x in ev]))
-            X = es.b[:k].clone()
+            X.copy_(es.b[:k])
         es.add_sigma_builder(plain)
         es.e_tol, es.r_tol = e_tol, r_tol
         es.stall_window, es.stall_floor = 0, 0.0
@@ -272,7 +296,7 @@ class CASCISolver:
         es.b[:k].copy_(X)
         es.basis_size, es.sigma_size = k, 0
         es.converged = converged
-        return w[:k], X.T, converged
+        return w[:k], es.b[:k].T, converged
 
     def avg_build_time(self):
         return self.sigma_builder.avg_build_time()

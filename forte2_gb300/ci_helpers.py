@@ -285,6 +285,15 @@ class CISigmaBuilder:
     def set_log_level(self, level):
         self.log_level = int(level)
 
+    def update_integrals(self, E, H, V):
+        """Replace the integrals, ordered on the current CUDA stream (no counterpart in the reference,
+        whose builder takes its integrals once, ci_sigma_builder.cc:102-185). Nothing waits for the
+        rest of the device and the device buffers keep their addresses, so a pool of builders can
+        serve new requests of the same active space without new allocations or graph captures."""
+        H, V = self._validate(H, V)
+        self._E, self._H, self._V = float(E), H, V
+        check(lib().f2g_sigma_set_hamiltonian_async(self.h, self._E, H.ctypes.data, V.ctypes.data, stream_handle()))
+
     def set_memory(self, mb):
         check(lib().f2g_sigma_set_memory(self.h, int(mb)))
 

@@ -8,6 +8,7 @@
 
 #include "../../include/forte2_gb300.h"
 #include "csf.cuh"
+#include "dgraph.cuh"
 
 namespace f2g {
 void dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n, double* out,
@@ -370,6 +371,132 @@ int f2g_dav_residual(const double* B, const double* Sv, int m, int64_t ld, const
 
 int f2g_dav_eigh(int m, const double* G, double* evals, double* evecs, void* stream) {
     return guard([&] { dav_eigh(m, G, evals, evecs, S(stream)); });
+}
+
+int f2g_dav_gs_append(double* B, int64_t ld, int cap, int m0, const double* R, int64_t ldr, int ncand, int64_t n,
+                      double discard, double ortho, int min_total, uint64_t seed, int* added, void* stream) {
+    return guard([&] {
+        need(B, "B");
+        need(added, "added");
+        if (ncand > 0)
+            need(R, "R");
+        dav_gs_append(B, ld, cap, m0, R, ldr, ncand, n, discard, ortho, min_total, seed, added, S(stream));
+    });
+}
+
+int f2g_dgraph_create(void* sb, void* sa, int64_t n, int nroot, int maxm, int collapse_k, int maxiter_cap,
+                      uint64_t seed, int iters_per_launch, const double* thresholds, double* b, double* sigma,
+                      double* r, double* tmp, int64_t ld, int64_t ldr, int64_t ldt, const double* hdiag, void** out) {
+    return guard([&] {
+        need(sb, "sigma");
+        need(sa, "spin adapter");
+        need(thresholds, "thresholds");
+        need(out, "out");
+        need(b, "b");
+        need(sigma, "sigma rows");
+        need(r, "r");
+        need(tmp, "tmp");
+        need(hdiag, "hdiag");
+        if (ld < n || ldr < n || ldt < n)
+            throw Error(2, "dgraph: leading dimensions must be at least n");
+        DGParams P{};
+        P.n = n;
+        P.nroot = nroot;
+        P.maxm = maxm;
+        P.collapse_k = collapse_k;
+        P.maxiter_cap = maxiter_cap;
+        P.precond_thresh = thresholds[0];
+        P.discard = thresholds[1];
+        P.ortho = thresholds[2];
+        P.seed = seed;
+        auto g = std::make_unique<DavGraph>(static_cast<SigmaBuilder*>(sb), static_cast<SpinAdapter*>(sa), P,
+                                            iters_per_launch, b, sigma, r, tmp, ld, ldr, ldt, hdiag);
+        *out = g.release();
+    });
+}
+
+int f2g_dgraph_destroy(void* g) {
+    return guard([&] { delete static_cast<DavGraph*>(g); });
+}
+
+int f2g_dgraph_set_correction(void* g, const double* X, const double* D, int64_t ldx, const double* Mxd, int k) {
+    return guard([&] {
+        need(g, "dgraph");
+        if (k > 0) {
+            need(X, "X");
+            need(D, "D");
+            need(Mxd, "Mxd");
+        }
+        static_cast<DavGraph*>(g)->set_correction(X, D, ldx, Mxd, k);
+    });
+}
+
+int f2g_dgraph_reset(void* g, int m, int sigma_size, const double* lam_old, int nlam, double e_tol, double r_tol,
+                     int maxiter, int stall_window, double stall_floor, void* stream) {
+    return guard([&] {
+        need(g, "dgraph");
+        DGReset rs{};
+        rs.m = m;
+        rs.sigma_size = sigma_size;
+        rs.nlam = nlam;
+        rs.maxiter = maxiter;
+        rs.stall_window = stall_window;
+        rs.e_tol = e_tol;
+        rs.r_tol = r_tol;
+        rs.stall_floor = stall_floor;
+        if (nlam < 0 || nlam > 64)
+            throw Error(2, "dgraph: 0 to 64 previous roots");
+        if (nlam)
+            need(lam_old, "lam_old");
+        for (int i = 0; i < nlam; ++i)
+            rs.lam_old[i] = lam_old[i];
+        static_cast<DavGraph*>(g)->reset(rs, S(stream));
+    });
+}
+
+int f2g_dgraph_launch(void* g, void* stream) {
+    return guard([&] {
+        need(g, "dgraph");
+        static_cast<DavGraph*>(g)->launch(S(stream));
+    });
+}
+
+int f2g_dgraph_state(void* g, int32_t* host_ints, double* host_dbl) {
+    return guard([&] {
+        need(g, "dgraph");
+        need(host_ints, "ints");
+        need(host_dbl, "doubles");
+        const DGState& s = *static_cast<DavGraph*>(g)->host_state;
+        const int32_t iv[8] = {s.m, s.sigma_size, s.iter, s.status, s.collapse, s.added, s.m_eig, 0};
+        std::memcpy(host_ints, iv, sizeof(iv));
+        host_dbl[0] = s.max_de;
+        host_dbl[1] = s.max_r;
+        std::memcpy(host_dbl + 2, s.lam, sizeof(s.lam));
+        std::memcpy(host_dbl + 66, s.lam_old, sizeof(s.lam_old));
+    });
+}
+
+int f2g_dgraph_ritz(void* g, double* out, int64_t ldo, void* stream) {
+    return guard([&] {
+        need(g, "dgraph");
+        need(out, "out");
+        static_cast<DavGraph*>(g)->ritz(out, ldo, S(stream));
+    });
+}
+
+int f2g_dgraph_history(void* g, double* host_out, int count) {
+    return guard([&] {
+        need(g, "dgraph");
+        need(host_out, "out");
+        static_cast<DavGraph*>(g)->history(host_out, count);
+    });
+}
+
+int f2g_sigma_set_hamiltonian_async(void* sb, double E, const double* H, const double* V, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        static_cast<SigmaBuilder*>(sb)->set_hamiltonian_async(E, H, V, S(stream));
+    });
 }
 
 } // extern "C"

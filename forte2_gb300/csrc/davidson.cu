@@ -14,7 +14,7 @@
 #include <mutex>
 #include <string>
 
-#include "common.cuh"
+#include "davidson.cuh"
 
 namespace f2g {
 
@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(256) k_residual(const double* __restrict__ B, 
 
 // Cyclic Jacobi for a symmetric m x m matrix (m <= 64), one block. Output: eigenvalues ascending,
 // eigenvectors as columns of V (row-major V[i * m + j]).
-__global__ void k_jacobi(int m, const double* __restrict__ G, double* __restrict__ evals, double* __restrict__ V,
-                         int max_sweeps) {
+__device__ void jacobi_block(int m, const double* __restrict__ G, int ldg, double* __restrict__ evals,
+                             double* __restrict__ V, int ldv, int max_sweeps) {
     __shared__ double A[64][65];
     __shared__ double Q[64][65];
     __shared__ double cs[2];
@@ -149,7 +149,7 @@ __global__ void k_jacobi(int m, const double* __restrict__ G, double* __restrict
     // Hermitize on load: A = (G + G^T) / 2 (davidsonliu.py:258)
     for (int k = t; k < m * m; k += blockDim.x) {
         const int i = k / m, j = k % m;
-        A[i][j] = 0.5 * (G[i * m + j] + G[j * m + i]);
+        A[i][j] = 0.5 * (G[i * ldg + j] + G[j * ldg + i]);
         Q[i][j] = i == j ? 1.0 : 0.0;
     }
     __syncthreads();
@@ -244,8 +244,13 @@ __global__ void k_jacobi(int m, const double* __restrict__ G, double* __restrict
             evals[i] = w[i];
         for (int i = 0; i < m; ++i)
             for (int j = 0; j < m; ++j)
-                V[i * m + j] = Q[i][order[j]];
+                V[i * ldv + j] = Q[i][order[j]];
     }
+}
+
+__global__ void k_jacobi(int m, const double* __restrict__ G, double* __restrict__ evals, double* __restrict__ V,
+                         int max_sweeps) {
+    jacobi_block(m, G, m, evals, V, m, max_sweeps);
 }
 
 // ---- host wrappers ----------------------------------------------------------------------------
@@ -367,6 +372,591 @@ void dav_eigh(int m, const double* G, double* evals, double* evecs, cudaStream_t
         throw Error(2, "eigh: subspace larger than 64");
     k_jacobi<<<1, 128, 0, st>>>(m, G, evals, evecs, 100);
     F2G_LAUNCH("k_jacobi");
+}
+
+
+// ---- Gram-Schmidt with on-device acceptance ----------------------------------------------------
+// The acceptance rule is the reference's (davidsonliu.py:438-484): each candidate is cycled (at
+// most 10 times) through v -= sum_i <B_i,v> B_i, rejected when |v| < discard, v /= |v|, and
+// accepted once max_i |<B_i,v>| < ortho and |<v,v> - 1| < ortho. One CTA runs the whole sequence,
+// so the decisions never leave the device; it suits the short vectors (up to a few 10^4) for which
+// host round trips, not bandwidth, bound the iteration.
+constexpr int kGsChunk = 8;
+constexpr int kGsThreads = 1024;
+
+// out[j] = <B_{i0+j}, v> for j < cnt (cnt <= kGsChunk); whole-CTA reduction in a fixed order.
+__device__ void gs_block_dots(const double* B, int64_t ld, int i0, int cnt, const double* v, int64_t n,
+                              double (*red)[kGsChunk], double* out) {
+    double acc[kGsChunk];
+#pragma unroll
+    for (int j = 0; j < kGsChunk; ++j)
+        acc[j] = 0.0;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+        const double x = v[e];
+#pragma unroll
+        for (int j = 0; j < kGsChunk; ++j)
+            if (j < cnt)
+                acc[j] += B[(int64_t)(i0 + j) * ld + e] * x;
+    }
+#pragma unroll
+    for (int j = 0; j < kGsChunk; ++j)
+        for (int off = 16; off > 0; off >>= 1)
+            acc[j] += __shfl_down_sync(0xffffffffu, acc[j], off);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < kGsChunk; ++j)
+            red[warp][j] = acc[j];
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            s += red[w][threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+// Uniform deviate in [-1, 1) from a counter (SplitMix64 output function, Steele, Lea and Flood,
+// OOPSLA 2014), for the random vectors that replace rejected candidates.
+__device__ __forceinline__ double gs_uniform(uint64_t seed, uint64_t stream, uint64_t e) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (stream * 0x100000001B3ull + e + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * 0x1.0p-53 * 2.0 - 1.0;
+}
+
+struct GsShared {
+    double red[kGsThreads / 32][kGsChunk];
+    double dv[72];
+    double scal[2];
+};
+
+// Orthonormalise row s of B (already holding the candidate) against rows [0, s). Returns 1 if
+// accepted. Every thread returns the same value (decisions read shared values after a barrier).
+__device__ int gs_one(double* B, int64_t ld, int s, int64_t n, double discard, double ortho, GsShared& sh) {
+    double* v = B + (int64_t)s * ld;
+    for (int cycle = 0; cycle < 10; ++cycle) {
+        for (int i0 = 0; i0 < s; i0 += kGsChunk)
+            gs_block_dots(B, ld, i0, min(kGsChunk, s - i0), v, n, sh.red, sh.dv + i0);
+        if (s > 0) {
+            for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+                double x = v[e];
+                for (int i = 0; i < s; ++i)
+                    x -= sh.dv[i] * B[(int64_t)i * ld + e];
+                v[e] = x;
+            }
+            __syncthreads();
+        }
+        gs_block_dots(v, 0, 0, 1, v, n, sh.red, sh.scal);
+        const double nrm = sqrt(fmax(sh.scal[0], 0.0));
+        if (nrm < discard)
+            return 0;
+        const double inv = 1.0 / nrm;
+        for (int64_t e = threadIdx.x; e < n; e += blockDim.x)
+            v[e] *= inv;
+        __syncthreads();
+        for (int i0 = 0; i0 < s; i0 += kGsChunk)
+            gs_block_dots(B, ld, i0, min(kGsChunk, s - i0), v, n, sh.red, sh.dv + i0);
+        gs_block_dots(v, 0, 0, 1, v, n, sh.red, sh.scal + 1);
+        double mo = 0.0;
+        for (int i = 0; i < s; ++i)
+            mo = fmax(mo, fabs(sh.dv[i]));
+        if (mo < ortho && fabs(sh.scal[1] - 1.0) < ortho)
+            return 1;
+    }
+    return 0;
+}
+
+// Append candidates R_c (c < ncand) to B[0, m0), then random rows until m0 + added >= min_total
+// (at most 10 tries per missing row). Rows are written in place, so B needs cap >= m0 + ncand and
+// cap >= min_total rows (checked on the host).
+__global__ void __launch_bounds__(kGsThreads) k_gs_append(double* B, int64_t ld, int m0, const double* R,
+                                                          int64_t ldr, int ncand, int64_t n, double discard,
+                                                          double ortho, int min_total, uint64_t seed, int* added) {
+    __shared__ GsShared sh;
+    int nadd = 0;
+    for (int c = 0; c < ncand; ++c) {
+        double* v = B + (int64_t)(m0 + nadd) * ld;
+        const double* rc = R + (int64_t)c * ldr;
+        for (int64_t e = threadIdx.x; e < n; e += blockDim.x)
+            v[e] = rc[e];
+        __syncthreads();
+        nadd += gs_one(B, ld, m0 + nadd, n, discard, ortho, sh);
+    }
+    const int missing = min_total - m0 - nadd;
+    for (int t = 0; t < 10 * missing && m0 + nadd < min_total; ++t) {
+        double* v = B + (int64_t)(m0 + nadd) * ld;
+        for (int64_t e = threadIdx.x; e < n; e += blockDim.x)
+            v[e] = gs_uniform(seed, (uint64_t)t, (uint64_t)e);
+        __syncthreads();
+        nadd += gs_one(B, ld, m0 + nadd, n, discard, ortho, sh);
+    }
+    if (threadIdx.x == 0)
+        *added = nadd;
+}
+
+void dav_gs_append(double* B, int64_t ld, int cap, int m0, const double* R, int64_t ldr, int ncand, int64_t n,
+                   double discard, double ortho, int min_total, uint64_t seed, int* added, cudaStream_t st) {
+    if (m0 < 0 || ncand < 0 || n < 0)
+        throw Error(2, "gs_append: negative size");
+    if (cap > 64 || m0 + ncand > cap || min_total > cap)
+        throw Error(2, "gs_append: the basis holds at most min(64, cap) vectors");
+    k_gs_append<<<1, kGsThreads, 0, st>>>(B, ld, m0, R, ldr, ncand, n, discard, ortho, min_total, seed, added);
+    F2G_LAUNCH("k_gs_append");
+}
+
+// ---- device-driven iteration -------------------------------------------------------------------
+// Each kernel returns at once unless the solve is running, so a captured run of iterations stops
+// doing work as soon as one of them converges. Sizes that change during the solve (basis size,
+// collapse) come from the state; grids are sized for the largest case.
+
+__global__ void k_dg_reset(DGState* st, DGReset r) {
+    st->m = r.m;
+    st->sigma_size = r.sigma_size;
+    st->iter = 0;
+    st->status = kDGRunning;
+    st->collapse = 0;
+    st->added = 0;
+    st->m_eig = 0;
+    st->maxiter = r.maxiter;
+    st->stall_window = r.stall_window;
+    st->e_tol = r.e_tol;
+    st->r_tol = r.r_tol;
+    st->stall_floor = r.stall_floor;
+    st->max_de = st->max_r = 0.0;
+    for (int i = 0; i < 64; ++i) {
+        st->lam_old[i] = i < r.nlam ? r.lam_old[i] : 0.0;
+        st->lam[i] = 0.0;
+    }
+}
+
+void dg_reset(DGState* st, const DGReset& r, cudaStream_t s) {
+    k_dg_reset<<<1, 1, 0, s>>>(st, r);
+    F2G_LAUNCH("k_dg_reset");
+}
+
+__global__ void k_dg_stage(const DGState* st, const double* __restrict__ b, int64_t ld, int R, int64_t n,
+                           double* __restrict__ out) {
+    if (st->status != kDGRunning)
+        return;
+    const int lo = st->sigma_size, m = st->m;
+    const int64_t total = (int64_t)R * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(t / n);
+        const int64_t e = t - (int64_t)r * n;
+        out[t] = lo + r < m ? b[(int64_t)(lo + r) * ld + e] : 0.0;
+    }
+}
+
+static int dg_grid(int64_t work) { return (int)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 8)); }
+
+void dg_stage(const DGState* st, const double* b, int64_t ld, int R, int64_t n, double* out, cudaStream_t s) {
+    k_dg_stage<<<dg_grid((int64_t)R * n), 256, 0, s>>>(st, b, ld, R, n, out);
+    F2G_LAUNCH("k_dg_stage");
+}
+
+__global__ void k_dg_unstage(const DGState* st, const double* __restrict__ in, int R, int64_t n,
+                             double* __restrict__ sigma, int64_t ld) {
+    if (st->status != kDGRunning)
+        return;
+    const int lo = st->sigma_size, m = st->m;
+    const int64_t total = (int64_t)R * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(t / n);
+        const int64_t e = t - (int64_t)r * n;
+        if (lo + r < m)
+            sigma[(int64_t)(lo + r) * ld + e] = in[t];
+    }
+}
+
+void dg_unstage(const DGState* st, const double* in, int R, int64_t n, double* sigma, int64_t ld, cudaStream_t s) {
+    k_dg_unstage<<<dg_grid((int64_t)R * n), 256, 0, s>>>(st, in, R, n, sigma, ld);
+    F2G_LAUNCH("k_dg_unstage");
+}
+
+// One CTA per (i, j) pair of a grid of ni x nj; pairs outside the current sizes return.
+__global__ void __launch_bounds__(256) k_dg_dots(const DGState* st, int which, const double* __restrict__ A,
+                                                 int64_t lda, const double* __restrict__ B, int64_t ldb, int64_t n,
+                                                 int ni, int nj, double* __restrict__ out, int ldo) {
+    if (st->status != kDGRunning)
+        return;
+    if ((which == 1 || which == 2) && !st->collapse)
+        return;
+    const int i = blockIdx.x / nj, j = blockIdx.x % nj;
+    int li = ni, lj = nj;
+    if (which == 0 || which == 1)
+        li = lj = st->m;
+    else if (which == 3)
+        li = st->m;
+    if (i >= li || j >= lj)
+        return;
+    const double* a = A + (int64_t)i * lda;
+    const double* bb = B + (int64_t)j * ldb;
+    double acc = 0.0;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x)
+        acc += a[e] * bb[e];
+    __shared__ double red[8];
+    for (int off = 16; off > 0; off >>= 1)
+        acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            s += red[w];
+        out[i * ldo + j] = s;
+    }
+}
+
+void dg_dots(const DGState* st, int which, const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n,
+             int ni, int nj, double* out, int ldo, cudaStream_t s) {
+    if (ni <= 0 || nj <= 0 || ni > 64 || nj > 64)
+        throw Error(2, "dg_dots: 1 to 64 vectors per operand");
+    k_dg_dots<<<ni * nj, 256, 0, s>>>(st, which, A, lda, B, ldb, n, ni, nj, out, ldo);
+    F2G_LAUNCH("k_dg_dots");
+}
+
+__global__ void k_dg_eigh(DGState* st, const double* G, int ldg, double* evals, double* V, int ldv) {
+    if (st->status != kDGRunning)
+        return;
+    const int m = st->m;
+    jacobi_block(m, G, ldg, evals, V, ldv, 100);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->m_eig = m;
+        st->sigma_size = m;
+    }
+}
+
+void dg_eigh(DGState* st, const double* G, int ldg, double* evals, double* V, int ldv, cudaStream_t s) {
+    k_dg_eigh<<<1, 128, 0, s>>>(st, G, ldg, evals, V, ldv);
+    F2G_LAUNCH("k_dg_eigh");
+}
+
+// Residuals of the first nroot Ritz pairs, as k_residual, with m and alpha (columns of V) taken
+// from the device.
+__global__ void __launch_bounds__(256) k_dg_residual(const DGState* st, DGParams P, const double* __restrict__ B,
+                                                     const double* __restrict__ S, int64_t ld,
+                                                     const double* __restrict__ V, int ldv,
+                                                     const double* __restrict__ lam, const double* __restrict__ hdiag,
+                                                     double* __restrict__ R, int64_t ldr, double* __restrict__ partial) {
+    if (st->status != kDGRunning)
+        return;
+    const int m = st->m, nroot = P.nroot;
+    __shared__ double sa[64 * 16];
+    __shared__ double sl[16];
+    __shared__ double red[16][256];
+    for (int t = threadIdx.x; t < m * nroot; t += blockDim.x)
+        sa[t] = V[(t / nroot) * ldv + (t % nroot)];
+    for (int t = threadIdx.x; t < nroot; t += blockDim.x)
+        sl[t] = lam[t];
+    __syncthreads();
+    double nrm[16];
+    for (int r = 0; r < nroot; ++r)
+        nrm[r] = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x) {
+        const double hd = hdiag[e];
+        for (int r = 0; r < nroot; ++r) {
+            double ba = 0.0, sa_ = 0.0;
+            for (int i = 0; i < m; ++i) {
+                ba += B[i * ld + e] * sa[i * nroot + r];
+                sa_ += S[i * ld + e] * sa[i * nroot + r];
+            }
+            const double res = sa_ - ba * sl[r];
+            nrm[r] += res * res;
+            const double den = sl[r] - hd;
+            R[r * ldr + e] = fabs(den) > P.precond_thresh ? res / den : 0.0;
+        }
+    }
+    for (int r = 0; r < nroot; ++r)
+        red[r][threadIdx.x] = nrm[r];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int r = 0; r < nroot; ++r)
+                red[r][threadIdx.x] += red[r][threadIdx.x + w];
+        __syncthreads();
+    }
+    if ((int)threadIdx.x < nroot)
+        partial[(int64_t)blockIdx.x * nroot + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_dg_reduce(const DGState* st, int nblocks, int npair, const double* partial, double* out) {
+    if (st->status != kDGRunning)
+        return;
+    const int pr = threadIdx.x;
+    if (pr >= npair)
+        return;
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b)
+        s += partial[(int64_t)b * npair + pr];
+    out[pr] = s;
+}
+
+int dg_residual_blocks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 4)); }
+
+void dg_residual(const DGState* st, const DGParams& P, const double* B, const double* S, int64_t ld, const double* V,
+                 int ldv, const double* evals, const double* hdiag, double* R, int64_t ldr, double* norms2,
+                 double* partial, cudaStream_t s) {
+    if (P.nroot > 16 || P.maxm > 64)
+        throw Error(2, "dg_residual: at most 16 roots and 64 basis vectors");
+    const int blocks = dg_residual_blocks(P.n);
+    k_dg_residual<<<blocks, 256, 0, s>>>(st, P, B, S, ld, V, ldv, evals, hdiag, R, ldr, partial);
+    F2G_LAUNCH("k_dg_residual");
+    k_dg_reduce<<<1, 32, 0, s>>>(st, blocks, P.nroot, partial, norms2);
+    F2G_LAUNCH("k_dg_reduce");
+}
+
+// Convergence and control decisions of one iteration (davidsonliu.py:295-336), one thread.
+// hist holds 4 doubles per iteration: mean root energy, max |dE|, max |r|, basis size.
+__global__ void k_dg_check(DGState* st, DGParams P, const double* norms2, const double* evals, double* hist) {
+    if (st->status != kDGRunning)
+        return;
+    const int nroot = P.nroot, m = st->m, it = st->iter;
+    double max_de = 0.0, max_r = 0.0, mean = 0.0;
+    for (int r = 0; r < nroot; ++r) {
+        const double lam = evals[r];
+        st->lam[r] = lam;
+        mean += lam;
+        max_de = fmax(max_de, fabs(lam - st->lam_old[r]));
+        max_r = fmax(max_r, sqrt(fmax(norms2[r], 0.0)));
+    }
+    for (int r = nroot; r < m; ++r)
+        st->lam[r] = evals[r];
+    st->max_de = max_de;
+    st->max_r = max_r;
+    st->iter = it + 1;
+    hist[4 * it + 0] = mean / nroot;
+    hist[4 * it + 1] = max_de;
+    hist[4 * it + 2] = max_r;
+    hist[4 * it + 3] = m;
+    if ((max_de < st->e_tol && max_r < st->r_tol) || (int64_t)m == P.n) {
+        st->status = kDGConverged;
+        return;
+    }
+    const int w = st->stall_window;
+    if (w > 0 && it + 1 > w) {
+        double recent = hist[4 * (it - w + 1) + 2], before = hist[2];
+        for (int k = it - w + 1; k <= it; ++k)
+            recent = fmin(recent, hist[4 * k + 2]);
+        for (int k = 0; k <= it - w; ++k)
+            before = fmin(before, hist[4 * k + 2]);
+        if (recent > 0.5 * before && recent < st->stall_floor) {
+            st->status = kDGStalled;
+            return;
+        }
+    }
+    if (it >= st->maxiter - 1) {
+        st->status = kDGMaxIter;
+        return;
+    }
+    for (int r = 0; r < nroot; ++r)
+        st->lam_old[r] = evals[r];
+    st->collapse = m + nroot > P.maxm;
+}
+
+void dg_check(DGState* st, const DGParams& P, const double* norms2, const double* evals, double* hist, cudaStream_t s) {
+    k_dg_check<<<1, 1, 0, s>>>(st, P, norms2, evals, hist);
+    F2G_LAUNCH("k_dg_check");
+}
+
+// np.allclose(S, I, atol=1e-11) on the basis overlap (davidsonliu.py:391-411): |S_ij - d_ij| <=
+// 1e-11 + 1e-5 d_ij. After a passing post-collapse check the basis size becomes collapse_k.
+__global__ void k_dg_orthocheck(DGState* st, DGParams P, const double* G, int ldg, int after) {
+    if (st->status != kDGRunning || !st->collapse)
+        return;
+    const int m = after ? P.collapse_k : st->m;
+    __shared__ int bad;
+    if (threadIdx.x == 0)
+        bad = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+        const int i = t / m, j = t % m;
+        const double d = i == j ? 1.0 : 0.0;
+        if (!(fabs(G[i * ldg + j] - d) <= 1e-11 + 1e-5 * d))
+            bad = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (bad) {
+            st->status = after ? kDGNotOrthoAfter : kDGNotOrthoBefore;
+        } else if (after) {
+            st->m = P.collapse_k;
+            st->sigma_size = P.collapse_k;
+            st->collapse = 0;
+        }
+    }
+}
+
+void dg_orthocheck(DGState* st, const DGParams& P, const double* G, int ldg, int after, cudaStream_t s) {
+    k_dg_orthocheck<<<1, 256, 0, s>>>(st, P, G, ldg, after);
+    F2G_LAUNCH("k_dg_orthocheck");
+}
+
+// tmp[j] = sum_i V[i, j] b_i and tmp[k + j] = sum_i V[i, j] sigma_i for j < k = collapse_k
+// (davidsonliu.py:389-411), summed in the order of k_lincomb.
+__global__ void k_dg_collapse_lc(const DGState* st, DGParams P, const double* __restrict__ b,
+                                 const double* __restrict__ sigma, int64_t ld, const double* __restrict__ V, int ldv,
+                                 double* __restrict__ tmp, int64_t ldt) {
+    if (st->status != kDGRunning || !st->collapse)
+        return;
+    const int m = st->m, k = P.collapse_k;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x) {
+        for (int j = 0; j < k; ++j) {
+            double sb = 0.0, ss = 0.0;
+            for (int i = 0; i < m; ++i) {
+                const double c = V[i * ldv + j];
+                sb += c * b[i * ld + e];
+                ss += c * sigma[i * ld + e];
+            }
+            tmp[j * ldt + e] = sb;
+            tmp[(k + j) * ldt + e] = ss;
+        }
+    }
+}
+
+__global__ void k_dg_collapse_copy(const DGState* st, DGParams P, double* __restrict__ b, double* __restrict__ sigma,
+                                   int64_t ld, const double* __restrict__ tmp, int64_t ldt) {
+    if (st->status != kDGRunning || !st->collapse)
+        return;
+    const int k = P.collapse_k;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x)
+        for (int j = 0; j < k; ++j) {
+            b[j * ld + e] = tmp[j * ldt + e];
+            sigma[j * ld + e] = tmp[(k + j) * ldt + e];
+        }
+}
+
+void dg_collapse(const DGState* st, const DGParams& P, double* b, double* sigma, int64_t ld, const double* V, int ldv,
+                 double* tmp, int64_t ldt, cudaStream_t s) {
+    const int g = dg_grid(P.n);
+    k_dg_collapse_lc<<<g, 256, 0, s>>>(st, P, b, sigma, ld, V, ldv, tmp, ldt);
+    F2G_LAUNCH("k_dg_collapse_lc");
+    k_dg_collapse_copy<<<g, 256, 0, s>>>(st, P, b, sigma, ld, tmp, ldt);
+    F2G_LAUNCH("k_dg_collapse_copy");
+}
+
+// r_j -= sum_i D[i, j] b_i for i < m, j < nroot (projection of the new directions out of the basis).
+__global__ void k_dg_project(const DGState* st, DGParams P, const double* __restrict__ b, int64_t ld,
+                             const double* __restrict__ D, double* __restrict__ r, int64_t ldr) {
+    if (st->status != kDGRunning)
+        return;
+    const int m = st->m, nroot = P.nroot;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x)
+        for (int j = 0; j < nroot; ++j) {
+            double s = r[j * ldr + e];
+            for (int i = 0; i < m; ++i)
+                s += -D[i * nroot + j] * b[i * ld + e];
+            r[j * ldr + e] = s;
+        }
+}
+
+void dg_project(const DGState* st, const DGParams& P, const double* b, int64_t ld, const double* D, double* r,
+                int64_t ldr, cudaStream_t s) {
+    k_dg_project<<<dg_grid(P.n), 256, 0, s>>>(st, P, b, ld, D, r, ldr);
+    F2G_LAUNCH("k_dg_project");
+}
+
+// Append the preconditioned residuals to the basis (davidsonliu.py:338-366): to_add = min(nroot,
+// maxm - m) candidates; if some are rejected, as many random vectors are tried once each.
+__global__ void __launch_bounds__(kGsThreads) k_dg_gs(DGState* st, DGParams P, double* b, int64_t ld,
+                                                      const double* r, int64_t ldr) {
+    __shared__ GsShared sh;
+    __shared__ int go;
+    if (threadIdx.x == 0)
+        go = st->status == kDGRunning;
+    __syncthreads();
+    if (!go)
+        return;
+    const int m0 = st->m, it = st->iter;
+    const int to_add = min(P.nroot, P.maxm - m0);
+    if (to_add <= 0) {
+        if (threadIdx.x == 0)
+            st->status = kDGConverged;
+        return;
+    }
+    int nadd = 0;
+    for (int c = 0; c < to_add; ++c) {
+        double* v = b + (int64_t)(m0 + nadd) * ld;
+        const double* rc = r + (int64_t)c * ldr;
+        for (int64_t e = threadIdx.x; e < P.n; e += blockDim.x)
+            v[e] = rc[e];
+        __syncthreads();
+        nadd += gs_one(b, ld, m0 + nadd, P.n, P.discard, P.ortho, sh);
+    }
+    const int refill = to_add - nadd;
+    for (int t = 0; t < refill; ++t) {
+        double* v = b + (int64_t)(m0 + nadd) * ld;
+        for (int64_t e = threadIdx.x; e < P.n; e += blockDim.x)
+            v[e] = gs_uniform(P.seed, (uint64_t)it * 64 + t, (uint64_t)e);
+        __syncthreads();
+        nadd += gs_one(b, ld, m0 + nadd, P.n, P.discard, P.ortho, sh);
+    }
+    if (threadIdx.x == 0) {
+        st->m = m0 + nadd;
+        st->added = nadd;
+    }
+}
+
+void dg_gs(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr, cudaStream_t s) {
+    k_dg_gs<<<1, kGsThreads, 0, s>>>(st, P, b, ld, r, ldr);
+    F2G_LAUNCH("k_dg_gs");
+}
+
+// Defect correction of the mixed-precision operator on R staged rows: S_r += D A_r + X (Bd_r - Mxd A_r)
+// with A = X B^T, Bd = D B^T (k x R, from dg_dots) and the symmetric k x k matrix Mxd.
+__global__ void k_dg_correct(const DGState* st, const double* __restrict__ X, const double* __restrict__ D,
+                             int64_t ldx, const double* __restrict__ Mxd, const double* __restrict__ A,
+                             const double* __restrict__ Bd, int k, int R, int64_t n, double* __restrict__ S) {
+    if (st->status != kDGRunning)
+        return;
+    __shared__ double c1[16 * 16], c2[16 * 16];
+    for (int t = threadIdx.x; t < k * R; t += blockDim.x) {
+        const int i = t / R, r = t % R;
+        double s = Bd[t];
+        for (int l = 0; l < k; ++l)
+            s -= Mxd[i * k + l] * A[l * R + r];
+        c1[t] = A[t];
+        c2[t] = s;
+    }
+    __syncthreads();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        for (int r = 0; r < R; ++r) {
+            double s = S[r * n + e];
+            for (int i = 0; i < k; ++i)
+                s += D[i * ldx + e] * c1[i * R + r] + X[i * ldx + e] * c2[i * R + r];
+            S[r * n + e] = s;
+        }
+}
+
+void dg_correct(const DGState* st, const double* X, const double* D, int64_t ldx, const double* Mxd, const double* A,
+                const double* Bd, int k, int R, int64_t n, double* S, cudaStream_t s) {
+    if (k > 16 || R > 16)
+        throw Error(2, "dg_correct: at most 16 corrected vectors and 16 staged rows");
+    k_dg_correct<<<dg_grid(n), 256, 0, s>>>(st, X, D, ldx, Mxd, A, Bd, k, R, n, S);
+    F2G_LAUNCH("k_dg_correct");
+}
+
+// Final Ritz vectors out_j = sum_{i < m} V[i, j] b_i, j < nroot (davidsonliu.py:380-387).
+__global__ void k_dg_ritz(const DGState* st, DGParams P, const double* __restrict__ b, int64_t ld,
+                          const double* __restrict__ V, int ldv, double* __restrict__ out, int64_t ldo) {
+    const int m = st->m;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x)
+        for (int j = 0; j < P.nroot; ++j) {
+            double s = 0.0;
+            for (int i = 0; i < m; ++i)
+                s += V[i * ldv + j] * b[i * ld + e];
+            out[j * ldo + e] = s;
+        }
+}
+
+void dg_ritz(const DGState* st, const DGParams& P, const double* b, int64_t ld, const double* V, int ldv, double* out,
+             int64_t ldo, cudaStream_t s) {
+    k_dg_ritz<<<dg_grid(P.n), 256, 0, s>>>(st, P, b, ld, V, ldv, out, ldo);
+    F2G_LAUNCH("k_dg_ritz");
 }
 
 } // namespace f2g

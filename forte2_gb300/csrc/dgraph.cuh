@@ -1,0 +1,195 @@
+// Graph-captured Davidson-Liu iterations (forte2/helpers/davidsonliu.py:184-387 with the CSF sigma
+// closure of forte2/ci/ci.py:221-235).
+//
+// One solve's iteration is captured once into a CUDA graph: stage the new basis rows, CSF -> det,
+// sigma, det -> CSF (plus the defect correction in the mixed-precision phase), the subspace matrix
+// and its Jacobi eigendecomposition, residuals, the convergence decision, collapse, projection and
+// Gram-Schmidt. Every size and decision lives in a DGState on the device, so K iterations replay
+// with no host involvement; the graph ends by copying the state to pinned host memory, which the
+// host reads after its next synchronisation. Kernels return at once when the state says the solve
+// has stopped, so a launch that converges early costs only empty launches for the rest.
+//
+// The captured addresses (basis, sigma and residual rows, the diagonal, the sigma builder's and the
+// spin adapter's tables) must stay valid while the graph exists; reusing one graph for a new solve
+// of the same shape only needs new integrals (SigmaBuilder::set_hamiltonian_async), a new
+// diagonal and guess written to the same buffers, and dg_reset.
+#pragma once
+
+#include <cstring>
+#include <string>
+
+#include "csf.cuh"
+#include "davidson.cuh"
+
+namespace f2g {
+
+struct DavGraph {
+    SigmaBuilder* sb;
+    SpinAdapter* sa;
+    DGParams P;
+    int R;     // staged rows per iteration
+    int iters; // iterations per launch
+    double *b, *sigma, *r, *tmp;
+    int64_t ld, ldr, ldt;
+    const double* hdiag;
+
+    DevBuf<DGState> st;
+    DevBuf<double> G, G2, evals, V, norms2, partial, Dp, hist, stage_c, stage_s, det_in, det_out, cA, cB;
+    DGState* host_state = nullptr;
+
+    const double *X = nullptr, *D = nullptr, *Mxd = nullptr;
+    int64_t ldx = 0;
+    int kc = 0;
+
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+
+    DavGraph(SigmaBuilder* sb_, SpinAdapter* sa_, const DGParams& p, int iters_, double* b_, double* sigma_, double* r_,
+             double* tmp_, int64_t ld_, int64_t ldr_, int64_t ldt_, const double* hdiag_)
+        : sb(sb_), sa(sa_), P(p), iters(iters_), b(b_), sigma(sigma_), r(r_), tmp(tmp_), ld(ld_), ldr(ldr_), ldt(ldt_),
+          hdiag(hdiag_) {
+        if (P.nroot < 1 || P.nroot > 16)
+            throw Error(2, "dgraph: 1 to 16 roots");
+        if (P.maxm < P.nroot || P.maxm > 64)
+            throw Error(2, "dgraph: basis size must be in [nroot, 64]");
+        if (P.collapse_k < 1 || P.collapse_k > P.maxm)
+            throw Error(2, "dgraph: collapse size must be in [1, maxm]");
+        if (P.n != sa->ncsf)
+            throw Error(2, "dgraph: vector length differs from the spin adapter's CSF count");
+        if (P.maxiter_cap < 1 || iters < 1)
+            throw Error(2, "dgraph: maxiter and iterations per launch must be positive");
+        R = P.nroot;
+        const int64_t n = P.n, nd = sa->s->ndet;
+        st.reserve(1);
+        G.reserve(64 * 64);
+        G2.reserve(64 * 64);
+        evals.reserve(64);
+        V.reserve(64 * 64);
+        norms2.reserve(16);
+        partial.reserve((size_t)dg_residual_blocks(n) * 16);
+        Dp.reserve(64 * 16);
+        hist.reserve((size_t)4 * P.maxiter_cap);
+        stage_c.reserve((size_t)R * n);
+        stage_s.reserve((size_t)R * n);
+        det_in.reserve((size_t)R * nd);
+        det_out.reserve((size_t)R * nd);
+        F2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&host_state), sizeof(DGState)));
+        std::memset(host_state, 0, sizeof(DGState));
+        F2G_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    }
+
+    ~DavGraph() {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (cap)
+            cudaStreamDestroy(cap);
+        if (host_state)
+            cudaFreeHost(host_state);
+    }
+
+    void set_correction(const double* X_, const double* D_, int64_t ldx_, const double* Mxd_, int k) {
+        if (k < 0 || k > 16)
+            throw Error(2, "dgraph: at most 16 corrected vectors");
+        X = X_;
+        D = D_;
+        ldx = ldx_;
+        Mxd = Mxd_;
+        kc = k;
+        if (k) {
+            cA.reserve((size_t)k * R);
+            cB.reserve((size_t)k * R);
+        }
+        drop();
+    }
+
+    void drop() {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        exec = nullptr;
+    }
+
+    void iteration(cudaStream_t s) {
+        const int64_t n = P.n, nd = sa->s->ndet;
+        const int mm = P.maxm;
+        DGState* S = st.get();
+        dg_stage(S, b, ld, R, n, stage_c.get(), s);
+        for (int i = 0; i < R; ++i) {
+            sa->csf_to_det(stage_c.get() + i * n, det_in.get() + i * nd, s);
+            sb->apply_untimed(det_in.get() + i * nd, det_out.get() + i * nd, s);
+            sa->det_to_csf(det_out.get() + i * nd, stage_s.get() + i * n, s);
+        }
+        if (kc) {
+            dg_dots(S, 4, X, ldx, stage_c.get(), n, n, kc, R, cA.get(), R, s);
+            dg_dots(S, 4, D, ldx, stage_c.get(), n, n, kc, R, cB.get(), R, s);
+            dg_correct(S, X, D, ldx, Mxd, cA.get(), cB.get(), kc, R, n, stage_s.get(), s);
+        }
+        dg_unstage(S, stage_s.get(), R, n, sigma, ld, s);
+        dg_dots(S, 0, b, ld, sigma, ld, n, mm, mm, G.get(), mm, s);
+        dg_eigh(S, G.get(), mm, evals.get(), V.get(), mm, s);
+        dg_residual(S, P, b, sigma, ld, V.get(), mm, evals.get(), hdiag, r, ldr, norms2.get(), partial.get(), s);
+        dg_check(S, P, norms2.get(), evals.get(), hist.get(), s);
+        dg_dots(S, 1, b, ld, b, ld, n, mm, mm, G2.get(), mm, s);
+        dg_orthocheck(S, P, G2.get(), mm, 0, s);
+        dg_collapse(S, P, b, sigma, ld, V.get(), mm, tmp, ldt, s);
+        dg_dots(S, 2, b, ld, b, ld, n, P.collapse_k, P.collapse_k, G2.get(), mm, s);
+        dg_orthocheck(S, P, G2.get(), mm, 1, s);
+        dg_dots(S, 3, b, ld, r, ldr, n, mm, P.nroot, Dp.get(), P.nroot, s);
+        dg_project(S, P, b, ld, Dp.get(), r, ldr, s);
+        dg_gs(S, P, b, ld, r, ldr, s);
+    }
+
+    void capture() {
+        drop();
+        sb->prepare_untimed();
+        sb->flush_timers();
+        F2G_CUDA(cudaStreamSynchronize(cap));
+        F2G_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        cudaGraph_t g = nullptr;
+        try {
+            for (int i = 0; i < iters; ++i)
+                iteration(cap);
+            F2G_CUDA(cudaMemcpyAsync(host_state, st.get(), sizeof(DGState), cudaMemcpyDeviceToHost, cap));
+        } catch (...) {
+            cudaStreamEndCapture(cap, &g);
+            if (g)
+                cudaGraphDestroy(g);
+            cudaGetLastError();
+            throw;
+        }
+        F2G_CUDA(cudaStreamEndCapture(cap, &g));
+        const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            exec = nullptr;
+            throw Error(3, std::string("dgraph: graph instantiation failed: ") + cudaGetErrorString(e));
+        }
+    }
+
+    void reset(const DGReset& rs, cudaStream_t s) {
+        if (rs.m < 0 || rs.m > P.maxm || rs.sigma_size < 0 || rs.sigma_size > rs.m || rs.nlam < 0 || rs.nlam > 64)
+            throw Error(2, "dgraph: reset sizes out of range");
+        if (rs.m - rs.sigma_size > R)
+            throw Error(2, "dgraph: at most nroot basis rows may lack sigma when the iterations start");
+        if (rs.maxiter < 1 || rs.maxiter > P.maxiter_cap)
+            throw Error(2, "dgraph: maxiter must be in [1, the limit given at creation]");
+        host_state->status = kDGRunning;
+        dg_reset(st.get(), rs, s);
+    }
+
+    void launch(cudaStream_t s) {
+        if (!exec)
+            capture();
+        F2G_CUDA(cudaGraphLaunch(exec, s));
+    }
+
+    void ritz(double* out, int64_t ldo, cudaStream_t s) { dg_ritz(st.get(), P, b, ld, V.get(), P.maxm, out, ldo, s); }
+
+    void history(double* host_out, int count) {
+        if (count < 0 || count > P.maxiter_cap)
+            throw Error(2, "dgraph: history count out of range");
+        if (count)
+            F2G_CUDA(cudaMemcpy(host_out, hist.get(), (size_t)4 * count * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+};
+
+} // namespace f2g

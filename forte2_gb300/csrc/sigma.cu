@@ -414,6 +414,70 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
         ensure_fp32();
 }
 
+// Same result as set_hamiltonian, ordered on stream st: the host arrays are copied into the
+// builder's own host vectors first, so the caller may reuse them at once. The FP32 copies are
+// refreshed too, so a later switch to FP32 needs no synchronisation. Buffers keep their addresses
+// when the orbital count is unchanged, which keeps captured graphs valid.
+void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const double* V_, cudaStream_t st) {
+    E = E_;
+    H.assign(H_, H_ + (size_t)n * n);
+    V.assign(V_, V_ + (size_t)n * n * n * n);
+    dH.reserve(std::max<size_t>(1, H.size()));
+    dV.reserve(std::max<size_t>(1, V.size()));
+    fV.reserve(std::max<size_t>(1, V.size()));
+    if (!H.empty())
+        F2G_CUDA(cudaMemcpyAsync(dH.get(), H.data(), H.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (!V.empty()) {
+        F2G_CUDA(cudaMemcpyAsync(dV.get(), V.data(), V.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        k_convert<double, float><<<64, 256, 0, st>>>((int64_t)V.size(), dV.get(), fV.get());
+        F2G_LAUNCH("k_convert V");
+    }
+    build_string_hamiltonian(0, ha, true, st);
+    build_string_hamiltonian(1, hb, false, st);
+    for (StringHamiltonian* sh : {&ha, &hb}) {
+        const int s_ = sh == &ha ? 0 : 1;
+        const size_t total = (size_t)s->spin(s_).N0 * sh->nnz;
+        if (total == 0)
+            continue;
+        sh->valf.reserve(total);
+        k_convert<double, float><<<1024, 256, 0, st>>>((int64_t)total, sh->val.get(), sh->valf.get());
+        F2G_LAUNCH("k_convert string Hamiltonian");
+    }
+    fp32_ready = true;
+}
+
+void SigmaBuilder::prepare_untimed() {
+    const int64_t nd = s->ndet;
+    if (nd == 0)
+        return;
+    Ct.reserve(nd);
+    Tt.reserve(nd);
+    if (precision == kFP32) {
+        ensure_fp32();
+        fC.reserve(nd);
+        fS.reserve(nd);
+        fCt.reserve(nd);
+        fTt.reserve(nd);
+    }
+}
+
+void SigmaBuilder::apply_untimed(const double* C, double* sigma, cudaStream_t st) {
+    const int64_t nd = s->ndet;
+    if (nd == 0)
+        return;
+    if (precision == kFP64) {
+        run<double>(C, sigma, st, 7, false);
+    } else {
+        float* c = fC.reserve(nd);
+        float* sg = fS.reserve(nd);
+        k_convert<double, float><<<1024, 256, 0, st>>>(nd, C, c);
+        F2G_LAUNCH("k_convert C");
+        run<float>(c, sg, st, 7, false);
+        k_convert<float, double><<<1024, 256, 0, st>>>(nd, sg, sigma);
+        F2G_LAUNCH("k_convert sigma");
+    }
+}
+
 // The reference's K-block memory contract (ci_sigma_builder_knowles_handy.cc:15-32): every term
 // needs at least one K-block column of nrows doubles in each of its two buffers. The device path
 // keeps the same validation and error text; its own scratch is two determinant vectors.

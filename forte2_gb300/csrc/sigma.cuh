@@ -51,6 +51,12 @@ struct SigmaBuilder {
     bool fp32_ready = false;
     void check_memory() const;
     void hamiltonian(const double* C, double* sigma, cudaStream_t st);
+    // Stream-ordered variants for solves that share the device with others: no device-wide
+    // synchronisation, no timers, no allocation (prepare_untimed() allocates the scratch first),
+    // so the calls can be captured into a CUDA graph.
+    void set_hamiltonian_async(double E, const double* H, const double* V, cudaStream_t st);
+    void prepare_untimed();
+    void apply_untimed(const double* C, double* sigma, cudaStream_t st);
     // one HZ term into sigma (overwrites): 0 H0, 1 H1a, 2 H1b, 3 aabb, 4 aaaa(+H1a? no), 5 bbbb
     void term(int which, const double* C, double* sigma, cudaStream_t st);
     void det_energies(double* out, cudaStream_t st);

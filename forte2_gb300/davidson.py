@@ -74,6 +74,11 @@ class DavidsonLiuSolver:
     # the FP32 rounding level.
     stall_window: int = 0
     stall_floor: float = 0.0  # the stall rule applies only once the residual is below this
+    # Graph-captured iterations (f2g_dgraph_*): None = whenever the sigma builder supports it and
+    # size <= graph_max_size; True/False force it on/off.
+    use_graph: bool = None
+    graph_max_size: int = 1 << 15
+    iters_per_launch: int = 8
 
     def __post_init__(self):
         p = self.davidson_liu_params
@@ -118,6 +123,9 @@ class DavidsonLiuSolver:
         self.converged = False
         self.sigma_builds = 0
         self.history = []
+        self._graphs = {}
+        self._tmp2 = None
+        self.used_graph = False
 
     # ---- configuration (davidsonliu.py:116-182) ----
     def add_sigma_builder(self, sigma_builder):
@@ -130,7 +138,10 @@ class DavidsonLiuSolver:
         t = h_diag.to(torch.float64).reshape(-1)
         if t.shape != (self.size,):
             raise ValueError("h_diag must be shape (size,)")
-        self.h_diag = t.to("cuda").contiguous().clone()
+        if self.h_diag is None:
+            self.h_diag = t.to("cuda").contiguous().clone()
+        else:  # same buffer: captured graphs keep its address
+            self.h_diag.copy_(t)
 
     def add_guesses(self, guesses):
         torch = _torch()
@@ -289,6 +300,134 @@ class DavidsonLiuSolver:
         self.sigma_size = k
         yield from self._orthonormality_steps(self.b[:k], f"After collapse: Checking orthonormality of newB with size {k}")
 
+    def restart(self):
+        """Forget the previous solution (the next solve starts from the guesses) but keep the
+        buffers and captured graphs, for a new problem of the same size."""
+        self._executed = False
+        self.basis_size = self.sigma_size = 0
+        self.lam_old[:] = 0.0
+        if hasattr(self, "_guesses"):
+            del self._guesses
+
+    def __del__(self):
+        try:
+            for h in getattr(self, "_graphs", {}).values():
+                lib().f2g_dgraph_destroy(h)
+        except Exception:
+            pass
+        self._graphs = {}
+
+    # ---- graph-captured iterations ----
+    def _graph_spec(self):
+        """(sigma builder, spin adapter, correction) when the graph path applies, else None."""
+        spec = getattr(self._build_sigma, "graph", None)
+        if spec is None or self.use_graph is False:
+            return None
+        if self.energy_shift is not None or hasattr(self, "_proj_out"):
+            return None
+        if self.use_graph is None and self.size > self.graph_max_size:
+            return None
+        return spec
+
+    def _graph_for(self, spec):
+        import ctypes as C
+
+        torch = _torch()
+        sb, sa, corr = spec
+        key = (sb.h.value, sa.h.value, sb.get_precision(),
+               None if corr is None else tuple(t.data_ptr() for t in corr[:3]) + (corr[3],))
+        g = self._graphs.get(key)
+        if g is not None and g[1] >= self.maxiter:
+            return g[0]
+        if g is not None:
+            lib().f2g_dgraph_destroy(g[0])
+        if self._tmp2 is None:
+            self._tmp2 = torch.zeros((2 * self.collapse_size, self.size), dtype=torch.float64, device="cuda")
+        thr = np.array([self.preconditioner_denom_threshold, self.schmidt_discard_threshold,
+                        self.schmidt_orthogonality_threshold], dtype=np.float64)
+        h = C.c_void_p()
+        check(lib().f2g_dgraph_create(sb.h, sa.h, self.size, self.nroot, self.max_subspace_size, self.collapse_size,
+                                      self.maxiter, int(self.seed), int(self.iters_per_launch), thr.ctypes.data,
+                                      _ptr(self.b), _ptr(self.sigma), _ptr(self.r), _ptr(self._tmp2), self.b.stride(0),
+                                      self.r.stride(0), self._tmp2.stride(0), _ptr(self.h_diag), C.byref(h)))
+        if corr is not None:
+            X, D, M, k = corr
+            check(lib().f2g_dgraph_set_correction(h, _ptr(X), _ptr(D), X.stride(0), _ptr(M), int(k)))
+        self._graphs[key] = (h, self.maxiter)
+        return h
+
+    def _solve_graph_steps(self, spec):
+        """solve_steps with the iterations replayed from a captured graph: one host read per
+        iters_per_launch iterations instead of several per iteration."""
+        torch = _torch()
+        L = lib()
+        nroot, maxm = self.nroot, self.max_subspace_size
+        self.used_graph = True
+        if not self._executed:
+            G = self._guesses if hasattr(self, "_guesses") else self._random_rows(nroot)
+            ncand = min(G.shape[0], maxm)
+            added = torch.zeros(1, dtype=torch.int32, device="cuda")
+            check(L.f2g_dav_gs_append(_ptr(self.b), self.b.stride(0), maxm, 0, _ptr(G), G.stride(0), ncand, self.size,
+                                      self.schmidt_discard_threshold, self.schmidt_orthogonality_threshold,
+                                      min(nroot, maxm), int(self.seed), _ptr(added), stream_handle()))
+            (a,) = yield [added]
+            self.basis_size = int(a[0])
+            self.sigma_size = 0
+            self.lam_old[:] = 0.0
+        m = self.basis_size
+        if m == 0:
+            raise RuntimeError("Davidson-Liu solver: no basis vector survived orthonormalisation.")
+        S = self._dots_dev(self.b[:m], self.b[:m])
+        if m > self.sigma_size:
+            yield from self._sigma_steps(self.sigma_size, m)
+        self.sigma_size = m
+        g = self._graph_for(spec)
+        lam_old = np.ascontiguousarray(self.lam_old[:nroot])
+        check(L.f2g_dgraph_reset(g, m, m, lam_old.ctypes.data, nroot, float(self.e_tol), float(self.r_tol),
+                                 int(self.maxiter), int(self.stall_window), float(self.stall_floor), stream_handle()))
+        check(L.f2g_dgraph_launch(g, stream_handle()))
+        (S,) = yield [S]
+        if not np.allclose(S, np.eye(S.shape[0]), atol=1e-11):
+            raise ValueError("Orthonormality check failed." +
+                             f" Largest deviation from orthonormality: {np.max(np.abs(S - np.eye(S.shape[0])))}")
+        ints = np.zeros(8, dtype=np.int32)
+        dbl = np.zeros(130, dtype=np.float64)
+        while True:
+            check(L.f2g_dgraph_state(g, ints.ctypes.data, dbl.ctypes.data))
+            if ints[3] != 0:
+                break
+            check(L.f2g_dgraph_launch(g, stream_handle()))
+            yield []
+        m, iters, status = int(ints[0]), int(ints[2]), int(ints[3])
+        if status == 4:
+            raise ValueError(f"Before collapse: Checking orthonormality of Bblk with size {m}")
+        if status == 5:
+            raise ValueError(f"After collapse: Checking orthonormality of newB with size {self.collapse_size}")
+        self.iter = iters - 1
+        self.converged = status == 1
+        self.sigma_builds += nroot * iters
+        lamr = dbl[2 : 2 + nroot].copy()
+        self.lam[:nroot] = lamr
+        self.lam_old[:nroot] = dbl[66 : 66 + nroot]
+        self.graph_status = status
+        self._graph_last = (g, iters)
+        check(L.f2g_dgraph_ritz(g, _ptr(self.tmp), self.tmp.stride(0), stream_handle()))
+        self.b[:nroot].copy_(self.tmp[:nroot])
+        self.basis_size = nroot
+        self.sigma_size = 0
+        self._executed = True
+        self.evecs_rows = self.b[:nroot]
+        return lamr, self.b[:nroot].T
+
+    def graph_history(self):
+        """Per-iteration (iteration, mean root energy, max |dE|, max |r|, basis size) of the last
+        graph-captured solve (a blocking read)."""
+        g, iters = self._graph_last
+        h = np.zeros(4 * iters, dtype=np.float64)
+        check(lib().f2g_dgraph_history(g, h.ctypes.data, iters))
+        h = h.reshape(iters, 4)
+        return [(i, h[i, 0], h[i, 1], h[i, 2], int(h[i, 3])) for i in range(iters)]
+
     def _log(self, msg):
         if self.logger is not None and self.log_level > 0:
             self.logger(msg)
@@ -300,6 +439,10 @@ class DavidsonLiuSolver:
             raise ValueError("Sigma builder function is not set.")
         if self.h_diag is None:
             raise ValueError("Hamiltonian diagonal is not set.")
+        spec = self._graph_spec()
+        if spec is not None:
+            return (yield from self._solve_graph_steps(spec))
+        self.used_graph = False
         torch = _torch()
         if not self._executed:
             G = self._guesses.clone() if hasattr(self, "_guesses") else self._random_rows(self.nroot)

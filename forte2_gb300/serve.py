@@ -17,6 +17,7 @@ from math import comb
 import numpy as np
 
 from .batch import StepScheduler, footprint_bytes, make_solver
+from .synthetic import make_integrals
 
 
 @dataclass
@@ -47,16 +48,67 @@ def poisson_stream(n_requests=10000, rate=200.0, seed=5, sizes=(6, 8, 10, 12, 14
     return [Request(i, float(t[i]), int(n[i]), int(mult[i]), int(roots[i]), 7_000_000 + i) for i in range(n_requests)]
 
 
-def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1e-10, max_inflight=256):
+class SolverPool:
+    """Idle solvers by shape (orbitals, multiplicity, roots, precision). A request of a shape seen
+    before takes an idle solver and only uploads its integrals: strings, spin adapter, sigma-builder
+    buffers, eigensolver buffers and captured iteration graphs are all reused. Idle solvers keep
+    their device memory, so they count against the HBM budget and the least recently used ones are
+    dropped when an admission needs the room."""
+
+    def __init__(self, precision, e_tol):
+        self.precision, self.e_tol = precision, e_tol
+        self.idle = {}  # key -> list of (solver, footprint), most recent last
+        self.order = deque()  # keys of idle solvers, least recent first
+        self.idle_bytes = 0
+        self.created = 0
+        self.reused = 0
+
+    @staticmethod
+    def key(r):
+        return (r.norb, r.multiplicity, r.nroot)
+
+    def take(self, r):
+        lst = self.idle.get(self.key(r))
+        if lst:
+            solver, fp = lst.pop()
+            self.order.remove(self.key(r))
+            self.idle_bytes -= fp
+            ints = make_integrals(r.norb, r.iseed)
+            solver.new_problem(ints.E, ints.H, ints.V)
+            self.reused += 1
+            return solver
+        self.created += 1
+        return make_solver(r.inst, self.precision, e_tol=self.e_tol)
+
+    def has_idle(self, r):
+        return bool(self.idle.get(self.key(r)))
+
+    def give(self, r, solver, fp):
+        self.idle.setdefault(self.key(r), []).append((solver, fp))
+        self.order.append(self.key(r))
+        self.idle_bytes += fp
+
+    def evict_one(self):
+        if not self.order:
+            return False
+        k = self.order.popleft()
+        _, fp = self.idle[k].pop(0)
+        self.idle_bytes -= fp
+        return True
+
+
+def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1e-10, max_inflight=256,
+          pool=True):
     """Serve a request stream in real time; returns per-request latencies and summary stats."""
     sched = StepScheduler(nstreams)
     pending = deque(sorted(requests, key=lambda r: r.arrival))
     waiting = deque()
-    used = [0]
+    used = [0]  # footprint of the solves in flight
     lat = {}
     energies = {}
     t_start = time.perf_counter()
     peak = [0, 0]
+    sp = SolverPool(precision, e_tol)
 
     def admit(now, active):
         rel = now - t_start
@@ -66,13 +118,18 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
         while waiting and len(active) + len(new) < max_inflight:
             r = waiting[0]
             fp = footprint_bytes(r.norb, r.norb // 2, r.norb // 2, r.nroot)
-            if used[0] + fp > hbm_budget and (active or new):
+            reuse = pool and sp.has_idle(r)
+            extra = 0 if reuse else fp
+            while used[0] + sp.idle_bytes + extra > hbm_budget and sp.evict_one():
+                pass
+            if used[0] + sp.idle_bytes + extra > hbm_budget and (active or new):
                 break
             waiting.popleft()
+            solver = sp.take(r) if pool else make_solver(r.inst, precision, e_tol=e_tol)
             used[0] += fp
-            new.append((r, make_solver(r.inst, precision, e_tol=e_tol).run_steps(), fp))
+            new.append(((r, solver), solver.run_steps(), fp))
         peak[0] = max(peak[0], len(active) + len(new))
-        peak[1] = max(peak[1], used[0])
+        peak[1] = max(peak[1], used[0] + sp.idle_bytes)
         if not new and not active and not waiting:
             if not pending:
                 return None
@@ -81,10 +138,12 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
         return new
 
     def on_done(job):
-        r = job.key
+        r, solver = job.key
         used[0] -= job.footprint
         lat[r.idx] = (job.t_done - t_start) - r.arrival
         energies[r.idx] = [float(e) for e in job.result.evals]
+        if pool:
+            sp.give(r, solver, job.footprint)
 
     sched.run(admit=admit, on_done=on_done)
     wall = time.perf_counter() - t_start
@@ -94,5 +153,6 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
         "solves_per_s": len(requests) / wall, "p50_latency_s": float(np.percentile(L, 50)),
         "p99_latency_s": float(np.percentile(L, 99)), "mean_latency_s": float(L.mean()),
         "max_inflight": peak[0], "peak_footprint_gb": peak[1] / 2**30, "rounds": sched.rounds,
+        "solvers_created": sp.created, "solvers_reused": sp.reused,
         "sizes": {int(n): int(sum(1 for r in requests if r.norb == n)) for n in sorted({r.norb for r in requests})},
     }, lat, energies

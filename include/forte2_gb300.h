@@ -124,6 +124,54 @@ int f2g_dav_residual(const double* dev_B, const double* dev_S, int m, int64_t ld
                      double* dev_R, int64_t ldr, double* dev_norms2, double* dev_scratch, void* stream);
 /* Symmetric eigensolver for m <= 64: eigenvalues ascending, eigenvectors as columns (row-major). */
 int f2g_dav_eigh(int m, const double* dev_G, double* dev_evals, double* dev_evecs, void* stream);
+/* Gram-Schmidt with the reference's acceptance rule (davidsonliu.py:438-484) decided on the device:
+ * appends the ncand rows of R, in order, to the orthonormal rows B[0, m0), then random rows until
+ * m0 + added >= min_total (at most 10 tries per missing row); *dev_added receives the count. One
+ * thread block does the work, so it suits vectors up to a few 10^4 elements. Needs
+ * m0 + ncand <= cap, min_total <= cap, cap <= 64 (B has cap rows of leading dimension ld). */
+int f2g_dav_gs_append(double* dev_B, int64_t ld, int cap, int m0, const double* dev_R, int64_t ldr, int ncand,
+                      int64_t n, double discard, double ortho, int min_total, uint64_t seed, int* dev_added,
+                      void* stream);
+
+/* ---- graph-captured Davidson-Liu iterations ----------------------------------------------------
+ * Replaces the host loop of DavidsonLiuSolver.solve (forte2/helpers/davidsonliu.py:184-387) driving
+ * the CSF sigma closure of _CISingleStateSolver (forte2/ci/ci.py:221-235); no C++ counterpart in the
+ * reference. One iteration (sigma of the new basis rows, subspace matrix, Jacobi, residuals,
+ * convergence and stall tests, collapse with its orthonormality checks, projection, Gram-Schmidt)
+ * is captured once into a CUDA graph of iters_per_launch iterations that reads every size and
+ * decision from a device state, and ends by copying that state to pinned host memory.
+ * Caller-owned device buffers: b, sigma (maxm rows, leading dimension ld), r (nroot rows, ldr),
+ * tmp (2 * collapse_k rows, ldt), hdiag (n); they must outlive the handle. thresholds =
+ * {preconditioner denominator, Gram-Schmidt discard, orthogonality} (1e-8, 1e-8, 1e-12 in the
+ * reference). The sigma builder's precision at the first launch is the one captured. */
+int f2g_dgraph_create(void* sigma, void* spin_adapter, int64_t n, int nroot, int maxm, int collapse_k,
+                      int maxiter_cap, uint64_t seed, int iters_per_launch, const double* host_thresholds,
+                      double* dev_b, double* dev_sigma, double* dev_r, double* dev_tmp, int64_t ld, int64_t ldr,
+                      int64_t ldt, const double* dev_hdiag, void** out);
+int f2g_dgraph_destroy(void* dgraph);
+/* Mixed-precision phase: sigma of each new row gains D (X b) + X (D b) - X Mxd (X b) (k <= 16 rows
+ * X, D of leading dimension ldx, symmetric k x k Mxd, all device). k = 0 removes it. */
+int f2g_dgraph_set_correction(void* dgraph, const double* dev_X, const double* dev_D, int64_t ldx,
+                              const double* dev_Mxd, int k);
+/* Start a solve: basis rows [0, m) orthonormal in b, sigma current for [0, sigma_size), at most
+ * nroot rows without sigma; lam_old = previous roots (nlam of them, zeros otherwise). */
+int f2g_dgraph_reset(void* dgraph, int m, int sigma_size, const double* host_lam_old, int nlam, double e_tol,
+                     double r_tol, int maxiter, int stall_window, double stall_floor, void* stream);
+/* Enqueue iters_per_launch iterations on stream (the first launch captures the graph). */
+int f2g_dgraph_launch(void* dgraph, void* stream);
+/* The state copied by the last completed launch (synchronise the stream first):
+ * ints = {m, sigma_size, iterations, status, collapse, added, m_eig, 0}; status 0 running,
+ * 1 converged, 2 iteration limit, 3 stalled, 4/5 basis not orthonormal before/after a collapse;
+ * doubles = {max |dE|, max |r|, the 64 subspace eigenvalues, the 64 previous roots}. */
+int f2g_dgraph_state(void* dgraph, int32_t* host_ints8, double* host_doubles130);
+/* Ritz vectors of the first nroot roots into rows of out (davidsonliu.py:380-387). */
+int f2g_dgraph_ritz(void* dgraph, double* dev_out, int64_t ldo, void* stream);
+/* Per-iteration {mean root energy, max |dE|, max |r|, basis size} of the current solve (blocking). */
+int f2g_dgraph_history(void* dgraph, double* host_out, int count);
+/* set_hamiltonian ordered on a stream, with no device-wide synchronisation; buffers keep their
+ * addresses for the same orbital count, so graphs captured on this builder stay valid. */
+int f2g_sigma_set_hamiltonian_async(void* sigma, double E, const double* host_H, const double* host_V,
+                                    void* stream);
 
 #ifdef __cplusplus
 }

@@ -194,28 +194,31 @@ def test_dl_shift(cuda):
 @pytest.mark.parametrize("key", ["2_2_4_m1_r2_it100", "3_3_6_m1_r3_it100", "3_3_6_m3_r2_it100",
                                  "4_3_7_m2_r2_it100", "4_4_8_m1_r4_it100", "4_4_8_m3_r3_it100",
                                  "5_5_10_m1_r4_it1000"])
-def test_casci_energies_match_reference(cuda, golden_davidson, key):
+@pytest.mark.parametrize("graph", [False, True])
+def test_casci_energies_match_reference(cuda, golden_davidson, key, graph):
     from forte2_gb300.ci import CASCISolver
     from forte2_gb300.params import DavidsonLiuParams
 
     g = golden_davidson[key]
     ints = make_integrals(g["norb"], g["iseed"])
     sol = CASCISolver(norb=g["norb"], na=g["na"], nb=g["nb"], multiplicity=g["multiplicity"], nroot=g["nroot"],
-                      E=ints.E, H=ints.H, V=ints.V,
+                      E=ints.E, H=ints.H, V=ints.V, use_graph=graph,
                       davidson_liu_params=DavidsonLiuParams(e_tol=g["e_tol"], maxiter=1000)).run()
     assert sol.converged
+    assert sol.eigensolver.used_graph == graph
     assert sol.spin_adapter.ncsf == g["ncsf"]
     np.testing.assert_allclose(np.sort(sol.evals), np.sort(g["evals"]), rtol=0, atol=1e-10)
 
 
-def test_casci_mixed_precision_within_1e8(cuda, golden_davidson):
+@pytest.mark.parametrize("graph", [False, True])
+def test_casci_mixed_precision_within_1e8(cuda, golden_davidson, graph):
     from forte2_gb300.ci import CASCISolver
     from forte2_gb300.params import CIParams, DavidsonLiuParams
 
     g = golden_davidson["5_5_10_m1_r4_it1000"]
     ints = make_integrals(g["norb"], g["iseed"])
     sol = CASCISolver(norb=10, na=5, nb=5, multiplicity=1, nroot=4, E=ints.E, H=ints.H, V=ints.V,
-                      ci_params=CIParams(precision="mixed"),
+                      ci_params=CIParams(precision="mixed"), use_graph=graph,
                       davidson_liu_params=DavidsonLiuParams(e_tol=1e-10, maxiter=1000)).run()
     assert sol.converged
     assert sol.phases[0][0] == "fp32"
