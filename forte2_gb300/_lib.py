@@ -38,6 +38,7 @@ def _declare(L):
         "f2g_sigma_get_algorithm": (i32, [vp, C.c_char_p, i32]),
         "f2g_sigma_set_memory": (i32, [vp, i32]),
         "f2g_sigma_set_precision": (i32, [vp, i32]),
+        "f2g_sigma_set_max_blocks": (i32, [vp, i32]),
         "f2g_sigma_apply": (i32, [vp, P, P, i32, vp]),
         "f2g_sigma_apply_host": (i32, [vp, P, P, i32]),
         "f2g_sigma_term": (i32, [vp, i32, P, P, vp]),
@@ -50,6 +51,7 @@ def _declare(L):
         "f2g_det_to_csf": (i32, [vp, P, P, i32, vp]),
         "f2g_hdiag_csf": (i32, [vp, vp, P, vp]),
         "f2g_csf_matrix": (i32, [vp, vp, P, i32, P]),
+        "f2g_csf_matrix_dev": (i32, [vp, vp, P, i32, P, vp]),
         "f2g_spin_adapter_dump": (i32, [vp, P, P, P, P]),
         "f2g_dav_scratch_size": (i64, [i64]),
         "f2g_dav_dots": (i32, [P, i32, i64, P, i32, i64, i64, P, P, vp]),
@@ -62,7 +64,7 @@ def _declare(L):
                                     P, pp]),
         "f2g_dgraph_destroy": (i32, [vp]),
         "f2g_dgraph_set_correction": (i32, [vp, P, P, i64, P, i32]),
-        "f2g_dgraph_reset": (i32, [vp, i32, i32, P, i32, d, d, i32, i32, d, vp]),
+        "f2g_dgraph_reset": (i32, [vp, i32, i32, P, P, i32, P, i32, d, d, i32, i32, d, vp]),
         "f2g_dgraph_launch": (i32, [vp, vp]),
         "f2g_dgraph_state": (i32, [vp, P, P]),
         "f2g_dgraph_ritz": (i32, [vp, P, i64, vp]),
@@ -99,8 +101,21 @@ def check(rc: int):
     raise RuntimeError(msg)
 
 
-def stream_handle(stream=None):
-    import torch
+_raw_stream = None
 
-    s = stream if stream is not None else torch.cuda.current_stream()
-    return C.c_void_p(s.cuda_stream)
+
+def stream_handle(stream=None):
+    """cudaStream_t of `stream`, default the current stream of the current device."""
+    global _raw_stream
+    if stream is not None:
+        return C.c_void_p(stream.cuda_stream)
+    if _raw_stream is None:
+        import torch
+
+        get_raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+        get_dev = getattr(torch._C, "_cuda_getDevice", None)
+        if get_raw is not None and get_dev is not None:
+            _raw_stream = lambda: get_raw(get_dev())  # noqa: E731
+        else:
+            _raw_stream = lambda: torch.cuda.current_stream().cuda_stream  # noqa: E731
+    return C.c_void_p(_raw_stream())

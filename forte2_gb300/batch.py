@@ -1,18 +1,22 @@
 """Many CASCI solves in flight on one GPU: batched instances and a continuous-batching server.
 
-Every solve is a step generator (``CASCISolver.run_steps``): it enqueues device work on its
-CUDA stream and yields the small device tensors it must read next. ``StepScheduler`` resumes
-every runnable job once per round (each on its own stream from a pool, so their kernels overlap
-on the device), then synchronises the device once, copies all requested values to the host in one
-transfer, and hands them back. New jobs can be admitted between rounds (``admit`` callback): the
-serving loop admits arriving requests while their estimated HBM footprint fits the budget.
+Every solve is a step generator (``CASCISolver.run_steps``): it enqueues device work on its CUDA
+stream and yields the small device tensors it must read next (nothing, when its iterations run
+from a captured graph that leaves its state in pinned host memory). ``StepScheduler`` gives each
+job in flight a stream of its own, records an event after each step, and resumes a job as soon as
+its event has completed, so a job never waits for another job's work: a slow solve (a large
+active space) does not hold back the small ones. New jobs can be admitted whenever the
+scheduler polls (``admit`` callback): the serving loop admits arriving requests while their
+estimated HBM footprint fits the budget.
+
+Streams of different jobs share the device's hardware queues (CUDA_DEVICE_MAX_CONNECTIONS, 8 by
+default); an application with many jobs in flight should raise it (up to 32) before CUDA starts.
 """
 
 from __future__ import annotations
 
-import heapq
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from math import comb
 
 import numpy as np
@@ -33,6 +37,7 @@ class Job:
     key: object
     gen: object
     stream: object
+    event: object = None  # recorded after each step; completed = the step's device work is done
     request: list = None
     result: object = None
     t_admit: float = 0.0
@@ -42,18 +47,26 @@ class Job:
 
 
 class StepScheduler:
-    """Round-robin driver of step generators with one device synchronisation per round."""
+    """Event-driven driver of step generators, one CUDA stream per job in flight."""
 
-    def __init__(self, nstreams: int = 16):
+    def __init__(self, nstreams: int = 16, poll_sleep: float = 2e-5):
         torch = _torch()
-        self.streams = [torch.cuda.Stream() for _ in range(nstreams)]
-        self._next_stream = 0
-        self.rounds = 0
+        # free streams by priority class: 0 normal, 1 high (lower CUDA priority value); more are
+        # made on demand
+        self._free = {0: [torch.cuda.Stream() for _ in range(nstreams)], 1: []}
+        self.max_streams = nstreams
+        self.rounds = 0  # resumptions of jobs after a completed step
+        self.polls = 0
+        self.poll_sleep = poll_sleep
+        self.host_s = {"start": 0.0, "resume": 0.0, "admit": 0.0}  # host time by activity
 
-    def _stream(self):
-        s = self.streams[self._next_stream % len(self.streams)]
-        self._next_stream += 1
-        return s
+    def _stream(self, high=False):
+        torch = _torch()
+        free = self._free[1 if high else 0]
+        if free:
+            return free.pop()
+        self.max_streams += 1
+        return torch.cuda.Stream(priority=-1) if high else torch.cuda.Stream()
 
     def _resume(self, job, values):
         torch = _torch()
@@ -61,33 +74,61 @@ class StepScheduler:
             try:
                 job.request = job.gen.send(values) if values is not None else next(job.gen)
                 job.steps += 1
+                if job.event is None:
+                    job.event = torch.cuda.Event()
+                job.event.record(job.stream)
                 return False
             except StopIteration as e:
+                # no host wait: the work the job enqueued last (its final vectors) is ordered by
+                # the event; a consumer on another stream waits for it (CASCISolver does)
                 job.result = e.value
+                if job.event is None:
+                    job.event = torch.cuda.Event()
+                job.event.record(job.stream)
+                if isinstance(job.result, CASCISolver):
+                    job.result._ready_event = job.event
                 job.t_done = time.perf_counter()
+                self._free[1 if job.stream.priority < 0 else 0].append(job.stream)
                 return True
 
+    @staticmethod
+    def _read(job):
+        if not job.request:
+            return []
+        torch = _torch()
+        with torch.cuda.stream(job.stream):
+            return [t.cpu().numpy() for t in job.request]
+
     def run(self, jobs=(), admit=None, on_done=None, idle_wait=None):
-        """Run jobs (iterable of (key, generator)) plus whatever ``admit(now, active)`` returns each
-        round, until nothing is active and ``admit`` reports no more work (returns None)."""
+        """Run jobs (iterable of (key, generator)) plus whatever ``admit(now, active)`` returns
+        ((key, generator, footprint[, high]) tuples), until nothing is active and ``admit`` reports
+        no more work (returns None). Jobs admitted with high=True run on high-priority streams, so
+        the block scheduler serves their small kernels before waiting blocks of long kernels."""
         torch = _torch()
         active = []
         done = []
 
-        def start(key, gen, footprint=0):
-            job = Job(key, gen, self._stream(), t_admit=time.perf_counter(), footprint=footprint)
+        def finish(job):
+            done.append(job)
+            if on_done:
+                on_done(job)
+
+        def start(key, gen, footprint=0, high=False):
+            t0 = time.perf_counter()
+            job = Job(key, gen, self._stream(high), t_admit=t0, footprint=footprint)
             if self._resume(job, None):
-                done.append(job)
-                if on_done:
-                    on_done(job)
+                finish(job)
             else:
                 active.append(job)
+            self.host_s["start"] += time.perf_counter() - t0
 
         for key, gen in jobs:
             start(key, gen)
         while True:
             if admit is not None:
-                new = admit(time.perf_counter(), active)
+                t0 = time.perf_counter()
+                new = admit(t0, active)
+                self.host_s["admit"] += time.perf_counter() - t0
                 if new is None and not active:
                     break
                 for item in new or ():
@@ -98,32 +139,25 @@ class StepScheduler:
                 if idle_wait:
                     idle_wait()
                 continue
-            self.rounds += 1
-            # one synchronisation and one D2H transfer for every value requested this round
-            # (the jobs' streams are synchronised before the gather, which runs on this thread's
-            # current stream and must see every job's results)
-            reqs = [t for job in active for t in job.request]
-            torch.cuda.synchronize()
-            if reqs:
-                flat = torch.cat([t.reshape(-1) for t in reqs]) if len(reqs) > 1 else reqs[0].reshape(-1)
-                host = flat.cpu().numpy()
-            else:
-                host = np.zeros(0)
-            pos = 0
+            self.polls += 1
             still = []
+            progressed = False
             for job in active:
-                vals = []
-                for t in job.request:
-                    n = t.numel()
-                    vals.append(host[pos : pos + n].reshape(t.shape))
-                    pos += n
-                if self._resume(job, vals):
-                    done.append(job)
-                    if on_done:
-                        on_done(job)
+                if not job.event.query():
+                    still.append(job)
+                    continue
+                progressed = True
+                self.rounds += 1
+                t0 = time.perf_counter()
+                fin = self._resume(job, self._read(job))
+                self.host_s["resume"] += time.perf_counter() - t0
+                if fin:
+                    finish(job)
                 else:
                     still.append(job)
             active = still
+            if not progressed and self.poll_sleep:
+                time.sleep(self.poll_sleep)
         torch.cuda.synchronize()
         return done
 

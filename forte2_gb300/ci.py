@@ -52,8 +52,11 @@ class CASCISolver:
     seed: int = 12345
     # graph-captured Davidson iterations: None = automatic (small CSF spaces), True/False = force
     use_graph: bool = None
+    # cap on the opposite-spin kernel's thread blocks (0 = none); see CISigmaBuilder.set_max_blocks
+    sigma_max_blocks: int = 0
 
     def __post_init__(self):
+        self._ready_event = None
         self.executed = False
         self.rebuild_guess = True
         self.eigensolver = None
@@ -123,7 +126,23 @@ class CASCISolver:
             key = (hdiag - self.ci_params.energy_shift).abs()
         else:
             key = hdiag
-        idx = torch.sort(key, stable=True).indices[:nguess_dets].cpu().numpy()
+        idx_dev = torch.sort(key, stable=True).indices[:nguess_dets].contiguous()
+        if nguess_dets <= 64:
+            # all on the device (no host wait): guess matrix, Jacobi, scatter into CSF rows
+            from ._lib import check, lib, stream_handle
+
+            m = nguess_dets
+            Hg = torch.empty((m, m), dtype=torch.float64, device="cuda")
+            check(lib().f2g_csf_matrix_dev(self.sigma_builder.h, self.spin_adapter.h, idx_dev.data_ptr(), m,
+                                           Hg.data_ptr(), stream_handle()))
+            ev = torch.empty(m, dtype=torch.float64, device="cuda")
+            V = torch.empty((m, m), dtype=torch.float64, device="cuda")
+            check(lib().f2g_dav_eigh(m, Hg.data_ptr(), ev.data_ptr(), V.data_ptr(), stream_handle()))
+            rows = torch.zeros((nguess, self.basis_size), dtype=torch.float64, device="cuda")
+            rows[:, idx_dev] = V[:, :nguess].T
+            self.eigensolver.add_guess_rows(rows)
+            return
+        idx = idx_dev.cpu().numpy()
         Hg = self.sigma_builder.csf_matrix(self.spin_adapter, idx)
         _, vecs = np.linalg.eigh(Hg)
         guess = torch.zeros((self.basis_size, nguess), dtype=torch.float64, device="cuda")
@@ -141,6 +160,10 @@ class CASCISolver:
         """Step generator of run() (see forte2_gb300.davidson.drive and forte2_gb300.batch)."""
         torch = _torch()
         t_all = time.perf_counter()
+        ready = getattr(self, "_ready_event", None)
+        if ready is not None:  # the previous solve of this object ran on another stream
+            torch.cuda.current_stream().wait_event(ready)
+            self._ready_event = None
         if not self.executed:
             self._startup()
         t0 = time.perf_counter()
@@ -152,6 +175,7 @@ class CASCISolver:
             self.sigma_builder.update_integrals(self.E, self.H, self.V)
             self.sigma_builder.set_precision("fp64")
         self.sigma_builder.set_memory(self.ci_params.ci_builder_memory)
+        self.sigma_builder.set_max_blocks(self.sigma_max_blocks)
         alg = self.ci_params.ci_algorithm.lower()
         if alg == "exact":
             return self._exact()
@@ -215,8 +239,11 @@ class CASCISolver:
         corrected operator H' = H32 + D X^T + X D^T - X (X^T D) X^T with D = S64 - S32, which
         acts exactly as FP64 H on span(X) (its sigma for X is S64 itself) and as FP32 H elsewhere.
         The error of X then shrinks by about |H64 - H32| / gap per outer step, so a solve needs a
-        few FP64 builds per root instead of FP64 Davidson iterations. Returns (evals, evecs
-        (size, nroot), converged) with the energies from the final FP64 Rayleigh-Ritz step.
+        few FP64 builds per root instead of FP64 Davidson iterations. When an outer step no
+        longer halves the FP64 residual (the FP32 sigma noise floor, about 1e-6 for |H| ~ 20) or
+        the outer steps run out, FP64 Davidson iterations warm-started from X finish the solve
+        under the caller's tolerances. Returns (evals, evecs (size, nroot), converged) with the
+        energies from the final FP64 Rayleigh-Ritz step.
         """
         torch = _torch()
         es, sb = self.eigensolver, self.sigma_builder
@@ -236,6 +263,7 @@ class CASCISolver:
         X, S64, S32, D, Mb = self._mixed_bufs
         X.copy_(es.b[:k])
         lam_prev = None
+        rn_prev = None
         converged = False
         w = np.asarray(ev, dtype=np.float64)
         for outer in range(self.mixed_max_outer):
@@ -262,6 +290,13 @@ class CASCISolver:
             if rn.max() < r_tol and de < e_tol:
                 converged = True
                 break
+            if (rn_prev is not None and rn.max() > 0.5 * rn_prev) or outer == self.mixed_max_outer - 1:
+                # the corrected FP32 iterations no longer reduce the FP64 residual (their sigma
+                # noise floor): finish with FP64 Davidson iterations from X, whose FP64 sigma S64
+                # is already known, under the caller's tolerances
+                w, converged = yield from self._fp64_polish_steps(X, S64, w, plain, e_tol, r_tol)
+                break
+            rn_prev = float(rn.max())
             lam_prev = w.copy()
             torch.sub(S64, S32, out=D)
             Mxd = es._dots_dev(X, D)
@@ -297,6 +332,25 @@ class CASCISolver:
         es.basis_size, es.sigma_size = k, 0
         es.converged = converged
         return w[:k], es.b[:k].T, converged
+
+    def _fp64_polish_steps(self, X, S64, w, plain, e_tol, r_tol):
+        """FP64 Davidson iterations warm-started from the rows X with their FP64 sigma S64; X is
+        overwritten with the converged Ritz vectors. Returns (energies, converged)."""
+        es, sb = self.eigensolver, self.sigma_builder
+        k = self.nroot
+        sb.set_precision("fp64")
+        es.add_sigma_builder(plain)
+        es.b[:k].copy_(X)
+        es.sigma[:k].copy_(S64)
+        es.basis_size = es.sigma_size = k
+        es.lam_old[:k] = w[:k]
+        es.e_tol, es.r_tol = e_tol, r_tol
+        es.stall_window, es.stall_floor = 0, 0.0
+        b0 = es.sigma_builds
+        ev, _ = yield from es.solve_steps()
+        self.phases.append(("fp64-polish", es.iter + 1, es.sigma_builds - b0, [float(x) for x in ev]))
+        X.copy_(es.b[:k])
+        return np.asarray(ev, dtype=np.float64), es.converged
 
     def avg_build_time(self):
         return self.sigma_builder.avg_build_time()

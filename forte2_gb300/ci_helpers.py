@@ -297,6 +297,11 @@ class CISigmaBuilder:
     def set_memory(self, mb):
         check(lib().f2g_sigma_set_memory(self.h, int(mb)))
 
+    def set_max_blocks(self, n):
+        """Cap the opposite-spin kernel at n thread blocks (one per SM; 0 = no cap), leaving the
+        other SMs to concurrent solves. Same sigma. No counterpart in the reference."""
+        check(lib().f2g_sigma_set_max_blocks(self.h, int(n)))
+
     def set_algorithm(self, algorithm):
         check(lib().f2g_sigma_set_algorithm(self.h, algorithm.encode()))
 

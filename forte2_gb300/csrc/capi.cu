@@ -1,6 +1,7 @@
 // C-ABI entry points (include/forte2_gb300.h). Every call catches exceptions and maps them to
 // status codes with a thread-local message; nothing here allocates on behalf of the caller's
 // vectors (C, sigma, CSF vectors are caller-owned device or host buffers).
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -201,6 +202,15 @@ int f2g_sigma_set_memory(void* sb, int mb) {
     });
 }
 
+int f2g_sigma_set_max_blocks(void* sb, int max_blocks) {
+    return guard([&] {
+        need(sb, "sigma");
+        if (max_blocks < 0)
+            throw Error(2, "max_blocks must be >= 0");
+        static_cast<SigmaBuilder*>(sb)->max_ctas = max_blocks;
+    });
+}
+
 int f2g_sigma_set_precision(void* sb, int precision) {
     return guard([&] {
         need(sb, "sigma");
@@ -226,8 +236,7 @@ int f2g_sigma_apply(void* sb, const double* C, double* sigma, int nvec, void* st
         const int64_t nd = b->s->ndet;
         if (nd && (!C || !sigma))
             throw Error(2, "NULL vector");
-        for (int v = 0; v < nvec; ++v)
-            b->hamiltonian(C + v * nd, sigma + v * nd, S(stream));
+        b->hamiltonian(C, sigma, S(stream), nvec);
     });
 }
 
@@ -297,8 +306,8 @@ int f2g_csf_to_det(void* h, const double* csf, double* det, int nvec, void* stre
     return guard([&] {
         need(h, "spin adapter");
         auto* a = static_cast<SpinAdapter*>(h);
-        for (int v = 0; v < nvec; ++v)
-            a->csf_to_det(csf + v * a->ncsf, det + v * a->s->ndet, S(stream));
+        for (int v0 = 0; v0 < nvec; v0 += 65535)
+            a->csf_to_det(csf + v0 * a->ncsf, det + v0 * a->s->ndet, S(stream), std::min(65535, nvec - v0));
     });
 }
 
@@ -306,8 +315,8 @@ int f2g_det_to_csf(void* h, const double* det, double* csf, int nvec, void* stre
     return guard([&] {
         need(h, "spin adapter");
         auto* a = static_cast<SpinAdapter*>(h);
-        for (int v = 0; v < nvec; ++v)
-            a->det_to_csf(det + v * a->s->ndet, csf + v * a->ncsf, S(stream));
+        for (int v0 = 0; v0 < nvec; v0 += 65535)
+            a->det_to_csf(det + v0 * a->s->ndet, csf + v0 * a->ncsf, S(stream), std::min(65535, nvec - v0));
     });
 }
 
@@ -317,11 +326,9 @@ int f2g_hdiag_csf(void* sb, void* h, double* out, void* stream) {
         need(h, "spin adapter");
         auto* b = static_cast<SigmaBuilder*>(sb);
         auto* a = static_cast<SpinAdapter*>(h);
-        DevBuf<double> e;
-        e.reserve(std::max<int64_t>(1, b->s->ndet));
-        b->det_energies(e.get(), S(stream));
-        a->hdiag(e.get(), out, S(stream));
-        F2G_CUDA(cudaStreamSynchronize(S(stream)));
+        double* e = b->eDet.reserve(std::max<int64_t>(1, b->s->ndet));
+        b->det_energies(e, S(stream));
+        a->hdiag(e, out, S(stream));
     });
 }
 
@@ -334,6 +341,20 @@ int f2g_csf_matrix(void* sb, void* h, const int64_t* idx, int m, double* out) {
             if (idx[i] < 0 || idx[i] >= a->ncsf)
                 throw Error(2, "CSF index out of range");
         a->csf_matrix(*static_cast<SigmaBuilder*>(sb), idx, m, out);
+    });
+}
+
+int f2g_csf_matrix_dev(void* sb, void* h, const int64_t* idx, int m, double* out, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        need(h, "spin adapter");
+        if (m < 0)
+            throw Error(2, "csf_matrix: negative size");
+        if (m > 0) {
+            need(idx, "idx");
+            need(out, "out");
+        }
+        static_cast<SpinAdapter*>(h)->csf_matrix_dev(*static_cast<SigmaBuilder*>(sb), idx, m, out, S(stream));
     });
 }
 
@@ -431,13 +452,19 @@ int f2g_dgraph_set_correction(void* g, const double* X, const double* D, int64_t
     });
 }
 
-int f2g_dgraph_reset(void* g, int m, int sigma_size, const double* lam_old, int nlam, double e_tol, double r_tol,
-                     int maxiter, int stall_window, double stall_floor, void* stream) {
+int f2g_dgraph_reset(void* g, int m, int sigma_size, const int32_t* dev_m, const double* dev_S, int ldS,
+                     const double* lam_old, int nlam, double e_tol, double r_tol, int maxiter, int stall_window,
+                     double stall_floor, void* stream) {
     return guard([&] {
         need(g, "dgraph");
         DGReset rs{};
         rs.m = m;
         rs.sigma_size = sigma_size;
+        rs.dev_m = dev_m;
+        rs.S = dev_S;
+        rs.ldS = ldS;
+        if (dev_S && ldS < m)
+            throw Error(2, "dgraph: ldS must be at least m");
         rs.nlam = nlam;
         rs.maxiter = maxiter;
         rs.stall_window = stall_window;
@@ -473,6 +500,7 @@ int f2g_dgraph_state(void* g, int32_t* host_ints, double* host_dbl) {
         host_dbl[1] = s.max_r;
         std::memcpy(host_dbl + 2, s.lam, sizeof(s.lam));
         std::memcpy(host_dbl + 66, s.lam_old, sizeof(s.lam_old));
+        host_dbl[130] = s.ortho_dev;
     });
 }
 

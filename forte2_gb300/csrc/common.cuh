@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -148,6 +149,23 @@ template <typename T> struct DevBuf {
         F2G_CUDA(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)));
         n = count;
         return p;
+    }
+    T* get() const { return p; }
+};
+
+// Scratch of one set-up step: allocated and released in stream order on `st` (cudaMallocAsync /
+// cudaFreeAsync), so that releasing it does not wait for work on other streams.
+template <typename T> struct TmpBuf {
+    T* p = nullptr;
+    cudaStream_t st = nullptr;
+    TmpBuf(size_t count, cudaStream_t s) : st(s) {
+        F2G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), std::max<size_t>(count, 1) * sizeof(T), st));
+    }
+    TmpBuf(const TmpBuf&) = delete;
+    TmpBuf& operator=(const TmpBuf&) = delete;
+    ~TmpBuf() {
+        if (p)
+            cudaFreeAsync(p, st);
     }
     T* get() const { return p; }
 };

@@ -238,10 +238,14 @@ struct CsfView {
     const int* ndetN;
 };
 
-__global__ void k_csf_to_det(int64_t nslot, CsfView v, const double* __restrict__ csf, double* __restrict__ det) {
+// Vector blockIdx.y of a batch: csf + y * ncsf_stride, det + y * ndet_stride.
+__global__ void k_csf_to_det(int64_t nslot, CsfView v, const double* __restrict__ csf, double* __restrict__ det,
+                             int64_t ncsf_stride, int64_t ndet_stride) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= nslot)
         return;
+    csf += blockIdx.y * ncsf_stride;
+    det += blockIdx.y * ndet_stride;
     const int64_t c = find_bucket(v.conf_slot, v.nconf, t);
     const int N = popc64(v.conf_s[c]);
     const int nd = v.ndetN[N], nc = v.ncsfN[N];
@@ -256,10 +260,13 @@ __global__ void k_csf_to_det(int64_t nslot, CsfView v, const double* __restrict_
 }
 
 template <bool SQUARE>
-__global__ void k_det_to_csf(int64_t ncsf, CsfView v, const double* __restrict__ det, double* __restrict__ csf) {
+__global__ void k_det_to_csf(int64_t ncsf, CsfView v, const double* __restrict__ det, double* __restrict__ csf,
+                             int64_t ndet_stride, int64_t ncsf_stride) {
     const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (u >= ncsf)
         return;
+    det += blockIdx.y * ndet_stride;
+    csf += blockIdx.y * ncsf_stride;
     const int64_t c = find_bucket(v.conf_csf, v.nconf, u);
     const int N = popc64(v.conf_s[c]);
     const int nd = v.ndetN[N];
@@ -409,8 +416,7 @@ __global__ void k_csf_matrix(int m, const int64_t* idx, CsfView v, int64_t N0b, 
 template <typename T> static void exclusive_scan(const T* in, T* out, int64_t n, cudaStream_t st) {
     size_t bytes = 0;
     F2G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, st));
-    DevBuf<unsigned char> tmp;
-    tmp.reserve(std::max<size_t>(bytes, 1));
+    TmpBuf<unsigned char> tmp(bytes, st);
     F2G_CUDA(cub::DeviceScan::ExclusiveSum(tmp.get(), bytes, in, out, n, st));
     F2G_CUDA(cudaStreamSynchronize(st));
 }
@@ -469,19 +475,16 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
         total += (int64_t)(host_binom(n, nd) * host_binom(n - nd, ns));
     }
     base[n + 1] = total;
-    DevBuf<int64_t> dbase;
-    dbase.reserve(n + 2);
-    F2G_CUDA(cudaMemcpy(dbase.get(), base.data(), (n + 2) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    TmpBuf<int64_t> dbase(n + 2, st);
+    F2G_CUDA(cudaMemcpyAsync(dbase.get(), base.data(), (n + 2) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
     ConfSpace cs{n, nel, dbase.get(), s->binom.get()};
 
     const int64_t NA = s->a.N0, NB = s->b.N0, nd_ = NA * NB;
     if (nd_ > 0x7fffffffLL)
         throw Error(1, "CISpinAdapter: more than 2^31 determinants");
-    DevBuf<uint32_t> first, flag, cidx;
-    first.reserve(std::max<int64_t>(1, total));
+    TmpBuf<uint32_t> first(std::max<int64_t>(1, total), st), flag(std::max<int64_t>(1, nd_), st),
+        cidx(std::max<int64_t>(1, nd_), st);
     F2G_CUDA(cudaMemsetAsync(first.get(), 0xff, std::max<int64_t>(1, total) * sizeof(uint32_t), st));
-    flag.reserve(std::max<int64_t>(1, nd_));
-    cidx.reserve(std::max<int64_t>(1, nd_));
     const int T = 256;
     if (nd_ > 0) {
         k_conf_first<<<ceil_div(nd_, T), T, 0, st>>>(NA, NB, s->a.str.get(), s->b.str.get(), twoS, cs, first.get());
@@ -491,17 +494,16 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
         F2G_LAUNCH("k_conf_flag");
         exclusive_scan<uint32_t>(flag.get(), cidx.get(), nd_, st);
         uint32_t last_flag = 0, last_idx = 0;
-        F2G_CUDA(cudaMemcpy(&last_flag, flag.get() + nd_ - 1, 4, cudaMemcpyDeviceToHost));
-        F2G_CUDA(cudaMemcpy(&last_idx, cidx.get() + nd_ - 1, 4, cudaMemcpyDeviceToHost));
+        F2G_CUDA(cudaMemcpyAsync(&last_flag, flag.get() + nd_ - 1, 4, cudaMemcpyDeviceToHost, st));
+        F2G_CUDA(cudaMemcpyAsync(&last_idx, cidx.get() + nd_ - 1, 4, cudaMemcpyDeviceToHost, st));
+        F2G_CUDA(cudaStreamSynchronize(st));
         nconf = (int64_t)last_idx + last_flag;
     }
     conf_d.reserve(std::max<int64_t>(1, nconf));
     conf_s.reserve(std::max<int64_t>(1, nconf));
     conf_csf.reserve(nconf + 1);
     conf_slot.reserve(nconf + 1);
-    DevBuf<int64_t> cnc, cns;
-    cnc.reserve(nconf + 1);
-    cns.reserve(nconf + 1);
+    TmpBuf<int64_t> cnc(nconf + 1, st), cns(nconf + 1, st);
     F2G_CUDA(cudaMemsetAsync(cnc.get(), 0, (nconf + 1) * sizeof(int64_t), st));
     F2G_CUDA(cudaMemsetAsync(cns.get(), 0, (nconf + 1) * sizeof(int64_t), st));
     if (nconf > 0) {
@@ -512,8 +514,9 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
     }
     exclusive_scan<int64_t>(cnc.get(), conf_csf.get(), nconf + 1, st);
     exclusive_scan<int64_t>(cns.get(), conf_slot.get(), nconf + 1, st);
-    F2G_CUDA(cudaMemcpy(&ncsf, conf_csf.get() + nconf, 8, cudaMemcpyDeviceToHost));
-    F2G_CUDA(cudaMemcpy(&nslot, conf_slot.get() + nconf, 8, cudaMemcpyDeviceToHost));
+    F2G_CUDA(cudaMemcpyAsync(&ncsf, conf_csf.get() + nconf, 8, cudaMemcpyDeviceToHost, st));
+    F2G_CUDA(cudaMemcpyAsync(&nslot, conf_slot.get() + nconf, 8, cudaMemcpyDeviceToHost, st));
+    F2G_CUDA(cudaStreamSynchronize(st));
     covers_all_dets = nslot == nd_;
     perm.reserve(std::max<int64_t>(1, nslot));
     if (nslot > 0) {
@@ -522,19 +525,19 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
         F2G_LAUNCH("k_conf_perm");
     }
     // coupling count (non-zero overlaps), as the reference logs it
-    DevBuf<unsigned long long> hist;
-    hist.reserve(65);
+    TmpBuf<unsigned long long> hist(65, st);
     F2G_CUDA(cudaMemsetAsync(hist.get(), 0, 65 * 8, st));
     if (nconf > 0) {
         k_hist<<<ceil_div(nconf, T), T, 0, st>>>(nconf, conf_s.get(), hist.get());
         F2G_LAUNCH("k_hist");
     }
     std::vector<unsigned long long> h(65);
-    F2G_CUDA(cudaMemcpy(h.data(), hist.get(), 65 * 8, cudaMemcpyDeviceToHost));
+    F2G_CUDA(cudaMemcpyAsync(h.data(), hist.get(), 65 * 8, cudaMemcpyDeviceToHost, st));
+    F2G_CUDA(cudaStreamSynchronize(st));
     ncoupling = 0;
     for (int N = 0; N <= n; ++N)
         ncoupling += (int64_t)h[N] * nnzN[N];
-    F2G_CUDA(cudaDeviceSynchronize());
+    F2G_CUDA(cudaStreamSynchronize(st));
 }
 
 static CsfView view_of(const SpinAdapter& a) {
@@ -542,41 +545,56 @@ static CsfView view_of(const SpinAdapter& a) {
                    a.O.get(), a.dOff.get(), a.dNcsf.get(), a.dNdet.get()};
 }
 
-void SpinAdapter::csf_to_det(const double* csf, double* det, cudaStream_t st) const {
+void SpinAdapter::csf_to_det(const double* csf, double* det, cudaStream_t st, int nvec) const {
+    if (nvec <= 0)
+        return;
+    if (nvec > 65535)
+        throw Error(2, "csf_to_det: at most 65535 vectors per call");
     if (!covers_all_dets)
-        F2G_CUDA(cudaMemsetAsync(det, 0, s->ndet * sizeof(double), st));
+        F2G_CUDA(cudaMemsetAsync(det, 0, (size_t)nvec * s->ndet * sizeof(double), st));
     if (nslot == 0)
         return;
-    k_csf_to_det<<<ceil_div(nslot, 256), 256, 0, st>>>(nslot, view_of(*this), csf, det);
+    k_csf_to_det<<<dim3((unsigned)ceil_div(nslot, 256), (unsigned)nvec), 256, 0, st>>>(nslot, view_of(*this), csf, det,
+                                                                                       ncsf, s->ndet);
     F2G_LAUNCH("k_csf_to_det");
 }
 
-void SpinAdapter::det_to_csf(const double* det, double* csf, cudaStream_t st) const {
-    if (ncsf == 0)
+void SpinAdapter::det_to_csf(const double* det, double* csf, cudaStream_t st, int nvec) const {
+    if (ncsf == 0 || nvec <= 0)
         return;
-    k_det_to_csf<false><<<ceil_div(ncsf, 256), 256, 0, st>>>(ncsf, view_of(*this), det, csf);
+    if (nvec > 65535)
+        throw Error(2, "det_to_csf: at most 65535 vectors per call");
+    k_det_to_csf<false><<<dim3((unsigned)ceil_div(ncsf, 256), (unsigned)nvec), 256, 0, st>>>(ncsf, view_of(*this), det,
+                                                                                             csf, s->ndet, ncsf);
     F2G_LAUNCH("k_det_to_csf");
 }
 
 void SpinAdapter::hdiag(const double* det_energy, double* out, cudaStream_t st) const {
     if (ncsf == 0)
         return;
-    k_det_to_csf<true><<<ceil_div(ncsf, 256), 256, 0, st>>>(ncsf, view_of(*this), det_energy, out);
+    k_det_to_csf<true><<<ceil_div(ncsf, 256), 256, 0, st>>>(ncsf, view_of(*this), det_energy, out, 0, 0);
     F2G_LAUNCH("k_hdiag");
 }
 
 void SpinAdapter::csf_matrix(const SigmaBuilder& sb, const int64_t* idx, int m, double* out_host) const {
     if (m <= 0)
         return;
-    DevBuf<int64_t> didx;
-    DevBuf<double> dout;
-    didx.reserve(m);
-    dout.reserve((size_t)m * m);
-    F2G_CUDA(cudaMemcpy(didx.get(), idx, m * sizeof(int64_t), cudaMemcpyHostToDevice));
-    k_csf_matrix<<<dim3(m, m), 256>>>(m, didx.get(), view_of(*this), s->b.N0, s->a.str.get(), s->b.str.get(), norb,
-                                      sb.E, sb.dH.get(), sb.dV.get(), dout.get());
+    int64_t* didx = mat_idx.reserve(m);
+    double* dout = mat_out.reserve((size_t)m * m);
+    F2G_CUDA(cudaMemcpy(didx, idx, m * sizeof(int64_t), cudaMemcpyHostToDevice));
+    csf_matrix_dev(sb, didx, m, dout, 0);
+    F2G_CUDA(cudaMemcpy(out_host, dout, (size_t)m * m * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
+void SpinAdapter::csf_matrix_dev(const SigmaBuilder& sb, const int64_t* idx, int m, double* out,
+                                 cudaStream_t st) const {
+    if (m <= 0)
+        return;
+    if (m > 65535)
+        throw Error(2, "csf_matrix: at most 65535 CSFs per call");
+    k_csf_matrix<<<dim3(m, m), 256, 0, st>>>(m, idx, view_of(*this), s->b.N0, s->a.str.get(), s->b.str.get(), norb,
+                                             sb.E, sb.dH.get(), sb.dV.get(), out);
     F2G_LAUNCH("k_csf_matrix");
-    F2G_CUDA(cudaMemcpy(out_host, dout.get(), (size_t)m * m * sizeof(double), cudaMemcpyDeviceToHost));
 }
 
 void SpinAdapter::dump(int64_t* bounds, int64_t* det_idx, double* coeff, int64_t* ranges) const {

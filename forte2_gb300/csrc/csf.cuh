@@ -23,11 +23,16 @@ struct SpinAdapter {
     DevBuf<uint32_t> perm;                 // [nslot] determinant address | negative sign << 31
 
     SpinAdapter(const CIStrings* s, int twoS, int twoMs);
-    void csf_to_det(const double* csf, double* det, cudaStream_t st) const;
-    void det_to_csf(const double* det, double* csf, cudaStream_t st) const;
+    // nvec vectors back to back (strides ncsf and ndet), one launch
+    void csf_to_det(const double* csf, double* det, cudaStream_t st, int nvec = 1) const;
+    void det_to_csf(const double* det, double* csf, cudaStream_t st, int nvec = 1) const;
     void hdiag(const double* det_energy, double* out, cudaStream_t st) const;
     // dense <I|H|J> over CSFs idx[0..m) (slater_rules_csf, ci_sigma_builder.cc:278-297)
     void csf_matrix(const SigmaBuilder& sb, const int64_t* idx, int m, double* out_host) const;
+    // the same with device indices and output, ordered on st
+    void csf_matrix_dev(const SigmaBuilder& sb, const int64_t* idx, int m, double* out, cudaStream_t st) const;
+    mutable DevBuf<int64_t> mat_idx; // staging of csf_matrix (kept: no allocation per call)
+    mutable DevBuf<double> mat_out;
     void dump(int64_t* bounds, int64_t* det_idx, double* coeff, int64_t* ranges) const;
 };
 

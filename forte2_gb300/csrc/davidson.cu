@@ -136,121 +136,131 @@ __global__ void __launch_bounds__(256) k_residual(const double* __restrict__ B, 
         partial[(int64_t)blockIdx.x * nroot + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// Cyclic Jacobi for a symmetric m x m matrix (m <= 64), one block. Output: eigenvalues ascending,
-// eigenvectors as columns of V (row-major V[i * m + j]).
+// Jacobi eigensolver for a symmetric m x m matrix (m <= 64), one block of at least 32 threads.
+// Output: eigenvalues ascending, eigenvectors as columns of V (row-major V[i * ldv + j]).
+// Parallel cyclic ordering (Brent and Luk, 1985; round-robin tournament): each sweep has
+// m' - 1 steps (m' = m rounded up to even) and each step rotates m'/2 disjoint pairs at once, so
+// the rotations of a step commute and are applied as one row pass and one column pass. Each
+// rotation zeroes A[p][q] with t = sgn(tau) / (|tau| + sqrt(1 + tau^2)), tau = (A_qq - A_pp) /
+// (2 A_pq), c = 1 / sqrt(1 + t^2), s = t c. Sweeps stop when the off-diagonal squared norm is at
+// most 1e-32 of the total.
+template <int MAXM>
 __device__ void jacobi_block(int m, const double* __restrict__ G, int ldg, double* __restrict__ evals,
                              double* __restrict__ V, int ldv, int max_sweeps) {
-    __shared__ double A[64][65];
-    __shared__ double Q[64][65];
-    __shared__ double cs[2];
-    __shared__ double off_red[128];
-    __shared__ int stop;
-    const int t = threadIdx.x;
+    __shared__ double A[MAXM][MAXM + 1];
+    __shared__ double Q[MAXM][MAXM + 1];
+    __shared__ double rc[MAXM / 2], rs[MAXM / 2];
+    __shared__ int rp[MAXM / 2], rq[MAXM / 2];
+    __shared__ double red[2][32];
+    __shared__ int order[MAXM];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int M = m + (m & 1), npair = M / 2;
     // Hermitize on load: A = (G + G^T) / 2 (davidsonliu.py:258)
-    for (int k = t; k < m * m; k += blockDim.x) {
+    for (int k = t; k < m * m; k += nt) {
         const int i = k / m, j = k % m;
         A[i][j] = 0.5 * (G[i * ldg + j] + G[j * ldg + i]);
         Q[i][j] = i == j ? 1.0 : 0.0;
     }
     __syncthreads();
-    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    for (int sweep = 0; sweep < max_sweeps && m > 1; ++sweep) {
         double off = 0.0, tot = 0.0;
-        for (int k = t; k < m * m; k += blockDim.x) {
+        for (int k = t; k < m * m; k += nt) {
             const int i = k / m, j = k % m;
             const double a2 = A[i][j] * A[i][j];
             tot += a2;
             if (i != j)
                 off += a2;
         }
-        off_red[t] = off;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if (t < w)
-                off_red[t] += off_red[t + w];
-            __syncthreads();
+        for (int o = 16; o > 0; o >>= 1) {
+            off += __shfl_down_sync(0xffffffffu, off, o);
+            tot += __shfl_down_sync(0xffffffffu, tot, o);
         }
-        const double offsum = off_red[0];
-        __syncthreads();
-        off_red[t] = tot;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if (t < w)
-                off_red[t] += off_red[t + w];
-            __syncthreads();
+        if ((t & 31) == 0) {
+            red[0][t >> 5] = off;
+            red[1][t >> 5] = tot;
         }
-        if (t == 0)
-            stop = (offsum <= 1e-32 * off_red[0]) || offsum == 0.0;
         __syncthreads();
-        if (stop)
+        double offsum = 0.0, totsum = 0.0;
+        for (int w = 0; w < (nt + 31) / 32; ++w) {
+            offsum += red[0][w];
+            totsum += red[1][w];
+        }
+        __syncthreads();
+        if (offsum <= 1e-32 * totsum || offsum == 0.0)
             break;
-        for (int p = 0; p < m - 1; ++p) {
-            for (int q = p + 1; q < m; ++q) {
-                if (t == 0) {
+        for (int step = 0; step < M - 1; ++step) {
+            if (t < npair) {
+                // players 0..M-1: 0 stays, 1..M-1 rotate; pair t is (r(t), r(M-1-t))
+                const int a_ = t == 0 ? 0 : (t - 1 + step) % (M - 1) + 1;
+                const int b_ = (M - 1 - t - 1 + step) % (M - 1) + 1;
+                const int p = min(a_, b_), q = max(a_, b_);
+                double c = 1.0, sn = 0.0;
+                if (q < m) {
                     const double apq = A[p][q];
-                    double c = 1.0, s = 0.0;
                     if (apq != 0.0) {
                         const double tau = (A[q][q] - A[p][p]) / (2.0 * apq);
                         const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
                         c = 1.0 / sqrt(1.0 + tt * tt);
-                        s = tt * c;
-                    }
-                    cs[0] = c;
-                    cs[1] = s;
-                }
-                __syncthreads();
-                const double c = cs[0], s = cs[1];
-                if (s != 0.0) {
-                    if (t < m) {
-                        const double akp = A[t][p], akq = A[t][q];
-                        A[t][p] = c * akp - s * akq;
-                        A[t][q] = s * akp + c * akq;
-                        const double vkp = Q[t][p], vkq = Q[t][q];
-                        Q[t][p] = c * vkp - s * vkq;
-                        Q[t][q] = s * vkp + c * vkq;
-                    }
-                    __syncthreads();
-                    if (t < m) {
-                        const double apk = A[p][t], aqk = A[q][t];
-                        A[p][t] = c * apk - s * aqk;
-                        A[q][t] = s * apk + c * aqk;
+                        sn = tt * c;
                     }
                 }
-                __syncthreads();
+                rp[t] = p;
+                rq[t] = q < m ? q : -1;
+                rc[t] = c;
+                rs[t] = sn;
             }
+            __syncthreads();
+            // columns: A <- A J, Q <- Q J
+            for (int k = t; k < npair * m; k += nt) {
+                const int pr = k / m, i = k % m, q = rq[pr];
+                if (q < 0 || rs[pr] == 0.0)
+                    continue;
+                const int p = rp[pr];
+                const double c = rc[pr], sn = rs[pr];
+                const double aip = A[i][p], aiq = A[i][q];
+                A[i][p] = c * aip - sn * aiq;
+                A[i][q] = sn * aip + c * aiq;
+                const double vip = Q[i][p], viq = Q[i][q];
+                Q[i][p] = c * vip - sn * viq;
+                Q[i][q] = sn * vip + c * viq;
+            }
+            __syncthreads();
+            // rows: A <- J^T A
+            for (int k = t; k < npair * m; k += nt) {
+                const int pr = k / m, j = k % m, q = rq[pr];
+                if (q < 0 || rs[pr] == 0.0)
+                    continue;
+                const int p = rp[pr];
+                const double c = rc[pr], sn = rs[pr];
+                const double apj = A[p][j], aqj = A[q][j];
+                A[p][j] = c * apj - sn * aqj;
+                A[q][j] = sn * apj + c * aqj;
+            }
+            __syncthreads();
         }
     }
+    // ascending order by rank (ties by index), then gather
+    for (int i = t; i < m; i += nt) {
+        const double w = A[i][i];
+        int r = 0;
+        for (int j = 0; j < m; ++j) {
+            const double x = A[j][j];
+            r += (x < w) || (x == w && j < i);
+        }
+        order[r] = i;
+    }
     __syncthreads();
-    if (t == 0) {
-        // selection sort of eigenpairs, ascending
-        int order[64];
-        double w[64];
-        for (int i = 0; i < m; ++i) {
-            order[i] = i;
-            w[i] = A[i][i];
-        }
-        for (int i = 0; i < m; ++i) {
-            int b = i;
-            for (int j = i + 1; j < m; ++j)
-                if (w[j] < w[b])
-                    b = j;
-            const double tw = w[i];
-            w[i] = w[b];
-            w[b] = tw;
-            const int to = order[i];
-            order[i] = order[b];
-            order[b] = to;
-        }
-        for (int i = 0; i < m; ++i)
-            evals[i] = w[i];
-        for (int i = 0; i < m; ++i)
-            for (int j = 0; j < m; ++j)
-                V[i * ldv + j] = Q[i][order[j]];
+    for (int i = t; i < m; i += nt)
+        evals[i] = A[order[i]][order[i]];
+    for (int k = t; k < m * m; k += nt) {
+        const int i = k / m, j = k % m;
+        V[i * ldv + j] = Q[i][order[j]];
     }
 }
 
 __global__ void k_jacobi(int m, const double* __restrict__ G, double* __restrict__ evals, double* __restrict__ V,
                          int max_sweeps) {
-    jacobi_block(m, G, m, evals, V, m, max_sweeps);
+    jacobi_block<64>(m, G, m, evals, V, m, max_sweeps);
 }
 
 // ---- host wrappers ----------------------------------------------------------------------------
@@ -497,13 +507,20 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_append(double* B, int64_t ld,
         *added = nadd;
 }
 
+// Threads of the one-block Gram-Schmidt: about 8 elements per thread, 64 to 1024 (whole warps),
+// so that short vectors do not pay for barriers across idle warps.
+static int gs_threads(int64_t n) {
+    const int64_t t = ((n / 8 + 31) / 32) * 32;
+    return (int)std::max<int64_t>(64, std::min<int64_t>(kGsThreads, t));
+}
+
 void dav_gs_append(double* B, int64_t ld, int cap, int m0, const double* R, int64_t ldr, int ncand, int64_t n,
                    double discard, double ortho, int min_total, uint64_t seed, int* added, cudaStream_t st) {
     if (m0 < 0 || ncand < 0 || n < 0)
         throw Error(2, "gs_append: negative size");
     if (cap > 64 || m0 + ncand > cap || min_total > cap)
         throw Error(2, "gs_append: the basis holds at most min(64, cap) vectors");
-    k_gs_append<<<1, kGsThreads, 0, st>>>(B, ld, m0, R, ldr, ncand, n, discard, ortho, min_total, seed, added);
+    k_gs_append<<<1, gs_threads(n), 0, st>>>(B, ld, m0, R, ldr, ncand, n, discard, ortho, min_total, seed, added);
     F2G_LAUNCH("k_gs_append");
 }
 
@@ -513,8 +530,11 @@ void dav_gs_append(double* B, int64_t ld, int cap, int m0, const double* R, int6
 // collapse) come from the state; grids are sized for the largest case.
 
 __global__ void k_dg_reset(DGState* st, DGReset r) {
-    st->m = r.m;
-    st->sigma_size = r.sigma_size;
+    int m = r.m;
+    if (r.dev_m)
+        m = max(0, min(r.m, *r.dev_m));
+    st->m = m;
+    st->sigma_size = r.sigma_size < 0 ? m : min(r.sigma_size, m);
     st->iter = 0;
     st->status = kDGRunning;
     st->collapse = 0;
@@ -526,10 +546,30 @@ __global__ void k_dg_reset(DGState* st, DGReset r) {
     st->r_tol = r.r_tol;
     st->stall_floor = r.stall_floor;
     st->max_de = st->max_r = 0.0;
+    st->ortho_dev = 0.0;
     for (int i = 0; i < 64; ++i) {
         st->lam_old[i] = i < r.nlam ? r.lam_old[i] : 0.0;
         st->lam[i] = 0.0;
     }
+    if (r.S) {
+        // np.allclose(S, I, atol=1e-11) of the starting basis (the check at the start of the
+        // reference's solve); the deviation reported is max |S - I|
+        bool ok = true;
+        double dev = 0.0;
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j) {
+                const double d = i == j ? 1.0 : 0.0;
+                const double x = fabs(r.S[i * r.ldS + j] - d);
+                dev = fmax(dev, x);
+                if (!(x <= 1e-11 + 1e-5 * d))
+                    ok = false;
+            }
+        st->ortho_dev = dev;
+        if (!ok)
+            st->status = kDGNotOrthoStart;
+    }
+    if (m == 0)
+        st->status = kDGNotOrthoStart;
 }
 
 void dg_reset(DGState* st, const DGReset& r, cudaStream_t s) {
@@ -557,10 +597,11 @@ void dg_stage(const DGState* st, const double* b, int64_t ld, int R, int64_t n, 
     F2G_LAUNCH("k_dg_stage");
 }
 
-__global__ void k_dg_unstage(const DGState* st, const double* __restrict__ in, int R, int64_t n,
-                             double* __restrict__ sigma, int64_t ld) {
-    if (st->status != kDGRunning)
-        return;
+// Bodies shared by the one-kernel-per-step iteration and the fused one-block iteration. Loops are
+// grid-stride, so a body called from a one-block kernel covers everything with that block.
+
+__device__ void dg_unstage_body(const DGState* st, const double* __restrict__ in, int R, int64_t n,
+                                double* __restrict__ sigma, int64_t ld) {
     const int lo = st->sigma_size, m = st->m;
     const int64_t total = (int64_t)R * n;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -569,6 +610,13 @@ __global__ void k_dg_unstage(const DGState* st, const double* __restrict__ in, i
         if (lo + r < m)
             sigma[(int64_t)(lo + r) * ld + e] = in[t];
     }
+}
+
+__global__ void k_dg_unstage(const DGState* st, const double* __restrict__ in, int R, int64_t n,
+                             double* __restrict__ sigma, int64_t ld) {
+    if (st->status != kDGRunning)
+        return;
+    dg_unstage_body(st, in, R, n, sigma, ld);
 }
 
 void dg_unstage(const DGState* st, const double* in, int R, int64_t n, double* sigma, int64_t ld, cudaStream_t s) {
@@ -619,11 +667,29 @@ void dg_dots(const DGState* st, int which, const double* A, int64_t lda, const d
     F2G_LAUNCH("k_dg_dots");
 }
 
+// out[i * ldo + j] = <A_i, B_j> for i < ni, j < nj inside one block: one warp per pair.
+__device__ void warp_pair_dots(const double* __restrict__ A, int64_t lda, const double* __restrict__ B,
+                               int64_t ldb, int64_t n, int ni, int nj, double* __restrict__ out, int ldo) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int p = warp; p < ni * nj; p += nw) {
+        const int i = p / nj, j = p % nj;
+        const double* a = A + (int64_t)i * lda;
+        const double* bb = B + (int64_t)j * ldb;
+        double acc = 0.0;
+        for (int64_t e = lane; e < n; e += 32)
+            acc += a[e] * bb[e];
+        for (int off = 16; off > 0; off >>= 1)
+            acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (lane == 0)
+            out[i * ldo + j] = acc;
+    }
+}
+
 __global__ void k_dg_eigh(DGState* st, const double* G, int ldg, double* evals, double* V, int ldv) {
     if (st->status != kDGRunning)
         return;
     const int m = st->m;
-    jacobi_block(m, G, ldg, evals, V, ldv, 100);
+    jacobi_block<64>(m, G, ldg, evals, V, ldv, 100);
     __syncthreads();
     if (threadIdx.x == 0) {
         st->m_eig = m;
@@ -637,18 +703,15 @@ void dg_eigh(DGState* st, const double* G, int ldg, double* evals, double* V, in
 }
 
 // Residuals of the first nroot Ritz pairs, as k_residual, with m and alpha (columns of V) taken
-// from the device.
-__global__ void __launch_bounds__(256) k_dg_residual(const DGState* st, DGParams P, const double* __restrict__ B,
-                                                     const double* __restrict__ S, int64_t ld,
-                                                     const double* __restrict__ V, int ldv,
-                                                     const double* __restrict__ lam, const double* __restrict__ hdiag,
-                                                     double* __restrict__ R, int64_t ldr, double* __restrict__ partial) {
-    if (st->status != kDGRunning)
-        return;
+// from the device; per-block partial squared norms (the total when the grid is one block).
+__device__ void dg_residual_body(const DGState* st, const DGParams& P, const double* __restrict__ B,
+                                 const double* __restrict__ S, int64_t ld, const double* __restrict__ V, int ldv,
+                                 const double* __restrict__ lam, const double* __restrict__ hdiag,
+                                 double* __restrict__ R, int64_t ldr, double* __restrict__ partial) {
     const int m = st->m, nroot = P.nroot;
     __shared__ double sa[64 * 16];
     __shared__ double sl[16];
-    __shared__ double red[16][256];
+    __shared__ double red[32][16];
     for (int t = threadIdx.x; t < m * nroot; t += blockDim.x)
         sa[t] = V[(t / nroot) * ldv + (t % nroot)];
     for (int t = threadIdx.x; t < nroot; t += blockDim.x)
@@ -671,17 +734,32 @@ __global__ void __launch_bounds__(256) k_dg_residual(const DGState* st, DGParams
             R[r * ldr + e] = fabs(den) > P.precond_thresh ? res / den : 0.0;
         }
     }
-    for (int r = 0; r < nroot; ++r)
-        red[r][threadIdx.x] = nrm[r];
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w)
-            for (int r = 0; r < nroot; ++r)
-                red[r][threadIdx.x] += red[r][threadIdx.x + w];
-        __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = 0; r < nroot; ++r) {
+        double v = nrm[r];
+        for (int off = 16; off > 0; off >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0)
+            red[warp][r] = v;
     }
-    if ((int)threadIdx.x < nroot)
-        partial[(int64_t)blockIdx.x * nroot + threadIdx.x] = red[threadIdx.x][0];
+    __syncthreads();
+    if ((int)threadIdx.x < nroot) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            v += red[w][threadIdx.x];
+        partial[(int64_t)blockIdx.x * nroot + threadIdx.x] = v;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_dg_residual(const DGState* st, DGParams P, const double* __restrict__ B,
+                                                     const double* __restrict__ S, int64_t ld,
+                                                     const double* __restrict__ V, int ldv,
+                                                     const double* __restrict__ lam, const double* __restrict__ hdiag,
+                                                     double* __restrict__ R, int64_t ldr, double* __restrict__ partial) {
+    if (st->status != kDGRunning)
+        return;
+    dg_residual_body(st, P, B, S, ld, V, ldv, lam, hdiag, R, ldr, partial);
 }
 
 __global__ void k_dg_reduce(const DGState* st, int nblocks, int npair, const double* partial, double* out) {
@@ -712,9 +790,8 @@ void dg_residual(const DGState* st, const DGParams& P, const double* B, const do
 
 // Convergence and control decisions of one iteration (davidsonliu.py:295-336), one thread.
 // hist holds 4 doubles per iteration: mean root energy, max |dE|, max |r|, basis size.
-__global__ void k_dg_check(DGState* st, DGParams P, const double* norms2, const double* evals, double* hist) {
-    if (st->status != kDGRunning)
-        return;
+__device__ void dg_check_body(DGState* st, const DGParams& P, const double* norms2, const double* evals,
+                              double* hist) {
     const int nroot = P.nroot, m = st->m, it = st->iter;
     double max_de = 0.0, max_r = 0.0, mean = 0.0;
     for (int r = 0; r < nroot; ++r) {
@@ -758,6 +835,12 @@ __global__ void k_dg_check(DGState* st, DGParams P, const double* norms2, const 
     st->collapse = m + nroot > P.maxm;
 }
 
+__global__ void k_dg_check(DGState* st, DGParams P, const double* norms2, const double* evals, double* hist) {
+    if (st->status != kDGRunning)
+        return;
+    dg_check_body(st, P, norms2, evals, hist);
+}
+
 void dg_check(DGState* st, const DGParams& P, const double* norms2, const double* evals, double* hist, cudaStream_t s) {
     k_dg_check<<<1, 1, 0, s>>>(st, P, norms2, evals, hist);
     F2G_LAUNCH("k_dg_check");
@@ -765,9 +848,8 @@ void dg_check(DGState* st, const DGParams& P, const double* norms2, const double
 
 // np.allclose(S, I, atol=1e-11) on the basis overlap (davidsonliu.py:391-411): |S_ij - d_ij| <=
 // 1e-11 + 1e-5 d_ij. After a passing post-collapse check the basis size becomes collapse_k.
-__global__ void k_dg_orthocheck(DGState* st, DGParams P, const double* G, int ldg, int after) {
-    if (st->status != kDGRunning || !st->collapse)
-        return;
+// Block-level; ends with a barrier.
+__device__ void dg_orthocheck_body(DGState* st, const DGParams& P, const double* G, int ldg, int after) {
     const int m = after ? P.collapse_k : st->m;
     __shared__ int bad;
     if (threadIdx.x == 0)
@@ -789,6 +871,13 @@ __global__ void k_dg_orthocheck(DGState* st, DGParams P, const double* G, int ld
             st->collapse = 0;
         }
     }
+    __syncthreads();
+}
+
+__global__ void k_dg_orthocheck(DGState* st, DGParams P, const double* G, int ldg, int after) {
+    if (st->status != kDGRunning || !st->collapse)
+        return;
+    dg_orthocheck_body(st, P, G, ldg, after);
 }
 
 void dg_orthocheck(DGState* st, const DGParams& P, const double* G, int ldg, int after, cudaStream_t s) {
@@ -798,11 +887,9 @@ void dg_orthocheck(DGState* st, const DGParams& P, const double* G, int ldg, int
 
 // tmp[j] = sum_i V[i, j] b_i and tmp[k + j] = sum_i V[i, j] sigma_i for j < k = collapse_k
 // (davidsonliu.py:389-411), summed in the order of k_lincomb.
-__global__ void k_dg_collapse_lc(const DGState* st, DGParams P, const double* __restrict__ b,
-                                 const double* __restrict__ sigma, int64_t ld, const double* __restrict__ V, int ldv,
-                                 double* __restrict__ tmp, int64_t ldt) {
-    if (st->status != kDGRunning || !st->collapse)
-        return;
+__device__ void dg_collapse_lc_body(const DGState* st, const DGParams& P, const double* __restrict__ b,
+                                    const double* __restrict__ sigma, int64_t ld, const double* __restrict__ V,
+                                    int ldv, double* __restrict__ tmp, int64_t ldt) {
     const int m = st->m, k = P.collapse_k;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x) {
         for (int j = 0; j < k; ++j) {
@@ -818,16 +905,29 @@ __global__ void k_dg_collapse_lc(const DGState* st, DGParams P, const double* __
     }
 }
 
-__global__ void k_dg_collapse_copy(const DGState* st, DGParams P, double* __restrict__ b, double* __restrict__ sigma,
-                                   int64_t ld, const double* __restrict__ tmp, int64_t ldt) {
-    if (st->status != kDGRunning || !st->collapse)
-        return;
+__device__ void dg_collapse_copy_body(const DGParams& P, double* __restrict__ b, double* __restrict__ sigma,
+                                      int64_t ld, const double* __restrict__ tmp, int64_t ldt) {
     const int k = P.collapse_k;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x)
         for (int j = 0; j < k; ++j) {
             b[j * ld + e] = tmp[j * ldt + e];
             sigma[j * ld + e] = tmp[(k + j) * ldt + e];
         }
+}
+
+__global__ void k_dg_collapse_lc(const DGState* st, DGParams P, const double* __restrict__ b,
+                                 const double* __restrict__ sigma, int64_t ld, const double* __restrict__ V, int ldv,
+                                 double* __restrict__ tmp, int64_t ldt) {
+    if (st->status != kDGRunning || !st->collapse)
+        return;
+    dg_collapse_lc_body(st, P, b, sigma, ld, V, ldv, tmp, ldt);
+}
+
+__global__ void k_dg_collapse_copy(const DGState* st, DGParams P, double* __restrict__ b, double* __restrict__ sigma,
+                                   int64_t ld, const double* __restrict__ tmp, int64_t ldt) {
+    if (st->status != kDGRunning || !st->collapse)
+        return;
+    dg_collapse_copy_body(P, b, sigma, ld, tmp, ldt);
 }
 
 void dg_collapse(const DGState* st, const DGParams& P, double* b, double* sigma, int64_t ld, const double* V, int ldv,
@@ -840,10 +940,8 @@ void dg_collapse(const DGState* st, const DGParams& P, double* b, double* sigma,
 }
 
 // r_j -= sum_i D[i, j] b_i for i < m, j < nroot (projection of the new directions out of the basis).
-__global__ void k_dg_project(const DGState* st, DGParams P, const double* __restrict__ b, int64_t ld,
-                             const double* __restrict__ D, double* __restrict__ r, int64_t ldr) {
-    if (st->status != kDGRunning)
-        return;
+__device__ void dg_project_body(const DGState* st, const DGParams& P, const double* __restrict__ b, int64_t ld,
+                                const double* __restrict__ D, double* __restrict__ r, int64_t ldr) {
     const int m = st->m, nroot = P.nroot;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x)
         for (int j = 0; j < nroot; ++j) {
@@ -854,6 +952,13 @@ __global__ void k_dg_project(const DGState* st, DGParams P, const double* __rest
         }
 }
 
+__global__ void k_dg_project(const DGState* st, DGParams P, const double* __restrict__ b, int64_t ld,
+                             const double* __restrict__ D, double* __restrict__ r, int64_t ldr) {
+    if (st->status != kDGRunning)
+        return;
+    dg_project_body(st, P, b, ld, D, r, ldr);
+}
+
 void dg_project(const DGState* st, const DGParams& P, const double* b, int64_t ld, const double* D, double* r,
                 int64_t ldr, cudaStream_t s) {
     k_dg_project<<<dg_grid(P.n), 256, 0, s>>>(st, P, b, ld, D, r, ldr);
@@ -862,15 +967,9 @@ void dg_project(const DGState* st, const DGParams& P, const double* b, int64_t l
 
 // Append the preconditioned residuals to the basis (davidsonliu.py:338-366): to_add = min(nroot,
 // maxm - m) candidates; if some are rejected, as many random vectors are tried once each.
-__global__ void __launch_bounds__(kGsThreads) k_dg_gs(DGState* st, DGParams P, double* b, int64_t ld,
-                                                      const double* r, int64_t ldr) {
-    __shared__ GsShared sh;
-    __shared__ int go;
-    if (threadIdx.x == 0)
-        go = st->status == kDGRunning;
-    __syncthreads();
-    if (!go)
-        return;
+// Block-level (one block).
+__device__ void dg_gs_body(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr,
+                           GsShared& sh) {
     const int m0 = st->m, it = st->iter;
     const int to_add = min(P.nroot, P.maxm - m0);
     if (to_add <= 0) {
@@ -901,9 +1000,99 @@ __global__ void __launch_bounds__(kGsThreads) k_dg_gs(DGState* st, DGParams P, d
     }
 }
 
+__global__ void __launch_bounds__(kGsThreads) k_dg_gs(DGState* st, DGParams P, double* b, int64_t ld,
+                                                      const double* r, int64_t ldr) {
+    __shared__ GsShared sh;
+    __shared__ int go;
+    if (threadIdx.x == 0)
+        go = st->status == kDGRunning;
+    __syncthreads();
+    if (!go)
+        return;
+    dg_gs_body(st, P, b, ld, r, ldr, sh);
+}
+
 void dg_gs(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr, cudaStream_t s) {
-    k_dg_gs<<<1, kGsThreads, 0, s>>>(st, P, b, ld, r, ldr);
+    k_dg_gs<<<1, gs_threads(P.n), 0, s>>>(st, P, b, ld, r, ldr);
     F2G_LAUNCH("k_dg_gs");
+}
+
+// Everything of one iteration after the sigma build, in one block: for short vectors the
+// iteration is bound by the launches of the separate steps, not by their work. Same steps and
+// decisions as the separate kernels (unstage, subspace matrix, Jacobi, residuals, convergence,
+// collapse with its checks, projection, Gram-Schmidt); dot products are one warp per pair.
+template <int MAXM>
+__global__ void __launch_bounds__(256) k_dg_small_iter(DGState* st, DGParams P, const double* __restrict__ stage_s,
+                                                       int R, double* b, double* sigma, int64_t ld, double* r,
+                                                       int64_t ldr, const double* __restrict__ hdiag, double* G,
+                                                       double* evals, double* V, double* Dp, double* tmp, int64_t ldt,
+                                                       double* hist, double* norms2) {
+    __shared__ GsShared gsh;
+    __shared__ int flag;
+    if (threadIdx.x == 0)
+        flag = st->status == kDGRunning;
+    __syncthreads();
+    if (!flag)
+        return;
+    dg_unstage_body(st, stage_s, R, P.n, sigma, ld);
+    __syncthreads();
+    const int m = st->m;
+    warp_pair_dots(b, ld, sigma, ld, P.n, m, m, G, P.maxm);
+    __syncthreads();
+    jacobi_block<MAXM>(m, G, P.maxm, evals, V, P.maxm, 100);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->m_eig = m;
+        st->sigma_size = m;
+    }
+    dg_residual_body(st, P, b, sigma, ld, V, P.maxm, evals, hdiag, r, ldr, norms2);
+    if (threadIdx.x == 0) {
+        dg_check_body(st, P, norms2, evals, hist);
+        flag = st->status != kDGRunning ? 0 : (st->collapse ? 2 : 1);
+    }
+    __syncthreads();
+    if (flag == 0)
+        return;
+    if (flag == 2) {
+        warp_pair_dots(b, ld, b, ld, P.n, m, m, G, P.maxm);
+        __syncthreads();
+        dg_orthocheck_body(st, P, G, P.maxm, 0);
+        if (st->status != kDGRunning)
+            return;
+        dg_collapse_lc_body(st, P, b, sigma, ld, V, P.maxm, tmp, ldt);
+        __syncthreads();
+        dg_collapse_copy_body(P, b, sigma, ld, tmp, ldt);
+        __syncthreads();
+        warp_pair_dots(b, ld, b, ld, P.n, P.collapse_k, P.collapse_k, G, P.maxm);
+        __syncthreads();
+        dg_orthocheck_body(st, P, G, P.maxm, 1);
+        if (st->status != kDGRunning)
+            return;
+    }
+    const int m2 = st->m;
+    warp_pair_dots(b, ld, r, ldr, P.n, m2, P.nroot, Dp, P.nroot);
+    __syncthreads();
+    dg_project_body(st, P, b, ld, Dp, r, ldr);
+    __syncthreads();
+    dg_gs_body(st, P, b, ld, r, ldr, gsh);
+}
+
+bool dg_small_ok(const DGParams& P) { return P.n <= kDGSmallN && P.maxm <= 32 && P.nroot <= 16; }
+
+void dg_small_iter(DGState* st, const DGParams& P, const double* stage_s, int R, double* b, double* sigma, int64_t ld,
+                   double* r, int64_t ldr, const double* hdiag, double* G, double* evals, double* V, double* Dp,
+                   double* tmp, int64_t ldt, double* hist, double* norms2, cudaStream_t s) {
+    if (!dg_small_ok(P))
+        throw Error(2, "dg_small_iter: vectors too long or basis too large for the one-block iteration");
+    // one warp for the shortest vectors: its barriers are nearly free, and the work is small
+    const int threads = P.n <= 1024 ? 32 : P.n <= 2048 ? 64 : 128;
+    if (P.maxm <= 16)
+        k_dg_small_iter<16><<<1, threads, 0, s>>>(st, P, stage_s, R, b, sigma, ld, r, ldr, hdiag, G, evals, V, Dp,
+                                                 tmp, ldt, hist, norms2);
+    else
+        k_dg_small_iter<32><<<1, threads, 0, s>>>(st, P, stage_s, R, b, sigma, ld, r, ldr, hdiag, G, evals, V, Dp,
+                                                 tmp, ldt, hist, norms2);
+    F2G_LAUNCH("k_dg_small_iter");
 }
 
 // Defect correction of the mixed-precision operator on R staged rows: S_r += D A_r + X (Bd_r - Mxd A_r)

@@ -32,6 +32,7 @@ struct DGState {
     int32_t pad;
     double e_tol, r_tol, stall_floor;
     double max_de, max_r;
+    double ortho_dev;   // largest |S - I| of the starting basis (checked at reset when S is given)
     double lam[64];     // eigenvalues of the last subspace eigenproblem (first nroot are the roots)
     double lam_old[64]; // roots of the previous iteration
 };
@@ -43,6 +44,7 @@ enum DGStatus : int32_t {
     kDGStalled = 3,      // stall rule fired (residual stopped decreasing below the floor)
     kDGNotOrthoBefore = 4, // basis failed the orthonormality check before a collapse
     kDGNotOrthoAfter = 5,  // collapsed basis failed the orthonormality check
+    kDGNotOrthoStart = 6,  // starting basis failed the orthonormality check
 };
 
 // Fixed for the lifetime of a captured graph.
@@ -56,6 +58,9 @@ struct DGParams {
 // Start of a solve: sizes, previous roots and this solve's tolerances.
 struct DGReset {
     int32_t m, sigma_size, nlam, maxiter, stall_window, pad;
+    const int32_t* dev_m; // if set: basis size read on the device (m is an upper bound); sigma_size < 0 = m
+    const double* S;      // if set: overlap of the starting basis (leading dimension ldS) to check
+    int32_t ldS, pad2;
     double e_tol, r_tol, stall_floor;
     double lam_old[64];
 };
@@ -81,6 +86,12 @@ void dg_project(const DGState* st, const DGParams& P, const double* b, int64_t l
 void dg_gs(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr, cudaStream_t s);
 void dg_correct(const DGState* st, const double* X, const double* D, int64_t ldx, const double* Mxd, const double* A,
                 const double* Bd, int k, int R, int64_t n, double* S, cudaStream_t s);
+// One-block iteration after the sigma build, for vectors up to kDGSmallN and bases up to 32.
+constexpr int64_t kDGSmallN = 4096;
+bool dg_small_ok(const DGParams& P);
+void dg_small_iter(DGState* st, const DGParams& P, const double* stage_s, int R, double* b, double* sigma, int64_t ld,
+                   double* r, int64_t ldr, const double* hdiag, double* G, double* evals, double* V, double* Dp,
+                   double* tmp, int64_t ldt, double* hist, double* norms2, cudaStream_t s);
 void dg_ritz(const DGState* st, const DGParams& P, const double* b, int64_t ld, const double* V, int ldv, double* out,
              int64_t ldo, cudaStream_t s);
 

@@ -16,12 +16,55 @@
 #pragma once
 
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include "csf.cuh"
 #include "davidson.cuh"
 
 namespace f2g {
+
+// Pinned host slots for the state copies of all graphs, carved from 64-slot chunks: page-locked
+// allocation synchronises the device, so it happens once per 64 graphs, not per graph.
+class PinnedStateSlots {
+  public:
+    static PinnedStateSlots& get() {
+        static PinnedStateSlots inst;
+        return inst;
+    }
+    DGState* take() {
+        std::lock_guard<std::mutex> lock(mu_);
+        if (free_.empty()) {
+            DGState* chunk = nullptr;
+            F2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&chunk), 64 * sizeof(DGState)));
+            for (int i = 63; i >= 0; --i)
+                free_.push_back(chunk + i);
+        }
+        DGState* p = free_.back();
+        free_.pop_back();
+        std::memset(p, 0, sizeof(DGState));
+        return p;
+    }
+    void give(DGState* p) {
+        std::lock_guard<std::mutex> lock(mu_);
+        free_.push_back(p);
+    }
+
+  private:
+    std::mutex mu_;
+    std::vector<DGState*> free_; // chunks stay allocated until the process exits
+};
+
+// One stream for all captures (a capture only records work), created once; captures are serialised.
+inline cudaStream_t capture_stream(std::unique_lock<std::mutex>& lock) {
+    static std::mutex mu;
+    static cudaStream_t st = nullptr;
+    lock = std::unique_lock<std::mutex>(mu);
+    if (!st)
+        F2G_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    return st;
+}
 
 struct DavGraph {
     SigmaBuilder* sb;
@@ -41,8 +84,8 @@ struct DavGraph {
     int64_t ldx = 0;
     int kc = 0;
 
-    cudaStream_t cap = nullptr;
     cudaGraphExec_t exec = nullptr;
+    std::shared_ptr<int> users; // the sigma builder's count of graphs using its graph scratch
 
     DavGraph(SigmaBuilder* sb_, SpinAdapter* sa_, const DGParams& p, int iters_, double* b_, double* sigma_, double* r_,
              double* tmp_, int64_t ld_, int64_t ldr_, int64_t ldt_, const double* hdiag_)
@@ -73,18 +116,16 @@ struct DavGraph {
         stage_s.reserve((size_t)R * n);
         det_in.reserve((size_t)R * nd);
         det_out.reserve((size_t)R * nd);
-        F2G_CUDA(cudaMallocHost(reinterpret_cast<void**>(&host_state), sizeof(DGState)));
-        std::memset(host_state, 0, sizeof(DGState));
-        F2G_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        host_state = PinnedStateSlots::get().take();
     }
 
     ~DavGraph() {
+        if (users)
+            --*users;
         if (exec)
             cudaGraphExecDestroy(exec);
-        if (cap)
-            cudaStreamDestroy(cap);
         if (host_state)
-            cudaFreeHost(host_state);
+            PinnedStateSlots::get().give(host_state);
     }
 
     void set_correction(const double* X_, const double* D_, int64_t ldx_, const double* Mxd_, int k) {
@@ -113,15 +154,18 @@ struct DavGraph {
         const int mm = P.maxm;
         DGState* S = st.get();
         dg_stage(S, b, ld, R, n, stage_c.get(), s);
-        for (int i = 0; i < R; ++i) {
-            sa->csf_to_det(stage_c.get() + i * n, det_in.get() + i * nd, s);
-            sb->apply_untimed(det_in.get() + i * nd, det_out.get() + i * nd, s);
-            sa->det_to_csf(det_out.get() + i * nd, stage_s.get() + i * n, s);
-        }
+        sa->csf_to_det(stage_c.get(), det_in.get(), s, R);
+        sb->apply_untimed(det_in.get(), det_out.get(), s, R);
+        sa->det_to_csf(det_out.get(), stage_s.get(), s, R);
         if (kc) {
             dg_dots(S, 4, X, ldx, stage_c.get(), n, n, kc, R, cA.get(), R, s);
             dg_dots(S, 4, D, ldx, stage_c.get(), n, n, kc, R, cB.get(), R, s);
             dg_correct(S, X, D, ldx, Mxd, cA.get(), cB.get(), kc, R, n, stage_s.get(), s);
+        }
+        if (dg_small_ok(P)) {
+            dg_small_iter(S, P, stage_s.get(), R, b, sigma, ld, r, ldr, hdiag, G.get(), evals.get(), V.get(), Dp.get(),
+                          tmp, ldt, hist.get(), norms2.get(), s);
+            return;
         }
         dg_unstage(S, stage_s.get(), R, n, sigma, ld, s);
         dg_dots(S, 0, b, ld, sigma, ld, n, mm, mm, G.get(), mm, s);
@@ -140,9 +184,12 @@ struct DavGraph {
 
     void capture() {
         drop();
-        sb->prepare_untimed();
+        sb->prepare_untimed(R);
+        if (sb->precision == kFP32)
+            sb->ensure_fp32();
         sb->flush_timers();
-        F2G_CUDA(cudaStreamSynchronize(cap));
+        std::unique_lock<std::mutex> lock;
+        cudaStream_t cap = capture_stream(lock);
         F2G_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
         cudaGraph_t g = nullptr;
         try {
@@ -163,12 +210,18 @@ struct DavGraph {
             exec = nullptr;
             throw Error(3, std::string("dgraph: graph instantiation failed: ") + cudaGetErrorString(e));
         }
+        if (!users) {
+            users = sb->graph_users;
+            ++*users;
+        }
     }
 
     void reset(const DGReset& rs, cudaStream_t s) {
-        if (rs.m < 0 || rs.m > P.maxm || rs.sigma_size < 0 || rs.sigma_size > rs.m || rs.nlam < 0 || rs.nlam > 64)
+        if (rs.m < 0 || rs.m > P.maxm || rs.sigma_size > rs.m || rs.nlam < 0 || rs.nlam > 64)
             throw Error(2, "dgraph: reset sizes out of range");
-        if (rs.m - rs.sigma_size > R)
+        if (rs.sigma_size < 0 && !rs.dev_m)
+            throw Error(2, "dgraph: sigma_size < 0 needs a device basis size");
+        if (rs.sigma_size >= 0 && rs.m - rs.sigma_size > R)
             throw Error(2, "dgraph: at most nroot basis rows may lack sigma when the iterations start");
         if (rs.maxiter < 1 || rs.maxiter > P.maxiter_cap)
             throw Error(2, "dgraph: maxiter must be in [1, the limit given at creation]");

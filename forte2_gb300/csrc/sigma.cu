@@ -141,8 +141,10 @@ __global__ void k_build_ss(int n, int k, int64_t N0, int nnz, const uint64_t* st
 // grid (rows, column tiles of blockDim * VEC); the row's (col, val) list is staged in shared memory.
 template <typename T, int VEC>
 __global__ void __launch_bounds__(128) k_spmm_rows(int64_t nrows, int ncols, int nnz, const int32_t* col,
-                                                   const T* val, const T* X, T* Y, int accumulate) {
+                                                   const T* val, const T* X, T* Y, int accumulate, int64_t vstride) {
     extern __shared__ unsigned char smem_raw[];
+    X += blockIdx.z * vstride; // vector blockIdx.z of a batch
+    Y += blockIdx.z * vstride;
     T* sval = reinterpret_cast<T*>(smem_raw);
     int32_t* scol = reinterpret_cast<int32_t*>(sval + nnz);
     const int64_t J = blockIdx.x;
@@ -180,6 +182,8 @@ __global__ void __launch_bounds__(128) k_spmm_rows(int64_t nrows, int ncols, int
 template <typename T>
 __global__ void k_transpose(int64_t rows, int64_t cols, const T* __restrict__ in, T* __restrict__ out) {
     __shared__ T tile[32][33];
+    in += blockIdx.z * rows * cols; // vector blockIdx.z of a batch
+    out += blockIdx.z * rows * cols;
     const int64_t bx = (int64_t)blockIdx.x * 32, by = (int64_t)blockIdx.y * 32;
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
         const int64_t r = by + j, c = bx + threadIdx.x;
@@ -209,15 +213,19 @@ __global__ void k_scale(int64_t n, double a, const double* in, double* out) {
 // SMROW: sigma(Ja,:) lives in shared memory; otherwise updates go to global memory atomically.
 template <typename T, int MB, bool SMROW>
 __global__ void __launch_bounds__(512, 1)
-    k_opposite(int n, int na, int N0b, int64_t N1b, int ma, int mb, const uint32_t* __restrict__ down_a,
+    k_opposite(int64_t N0a, int n, int na, int N0b, int64_t N1b, int ma, int mb, const uint32_t* __restrict__ down_a,
                const uint32_t* __restrict__ up_a, const uint32_t* __restrict__ up_b, const T* __restrict__ V,
                const T* __restrict__ C, T* sig) {
     extern __shared__ unsigned char smem_raw[];
     T* vs = reinterpret_cast<T*>(smem_raw);                 // [n][ma][n]: V[p, r, q_i, s]
     T* row = vs + (size_t)n * ma * n;                       // [N0b] (SMROW)
     uint32_t* ua = reinterpret_cast<uint32_t*>(row + (SMROW ? N0b : 0)); // [ma]
-    const int64_t Ja = blockIdx.x;
+    C += blockIdx.y * N0a * N0b; // vector blockIdx.y of a batch
+    sig += blockIdx.y * N0a * N0b;
+    // grid-stride over the output alpha strings: a grid smaller than N0a leaves SMs free for other work
+    for (int64_t Ja = blockIdx.x; Ja < N0a; Ja += gridDim.x) {
     T* srow = sig + Ja * (int64_t)N0b;
+    __syncthreads(); // the previous row is written back
     if (SMROW) {
         for (int c = threadIdx.x; c < N0b; c += blockDim.x)
             row[c] = srow[c];
@@ -295,6 +303,7 @@ __global__ void __launch_bounds__(512, 1)
         __syncthreads();
         for (int c = threadIdx.x; c < N0b; c += blockDim.x)
             srow[c] = row[c];
+    }
     }
 }
 
@@ -387,7 +396,7 @@ void SigmaBuilder::ensure_fp32() {
         k_convert<double, float><<<1024, 256>>>((int64_t)total, sh->val.get(), sh->valf.get());
         F2G_LAUNCH("k_convert string Hamiltonian");
     }
-    F2G_CUDA(cudaDeviceSynchronize());
+    F2G_CUDA(cudaStreamSynchronize(0)); // the conversions ran on the legacy stream: wait for them alone
     fp32_ready = true;
 }
 
@@ -408,7 +417,7 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
     }
     build_string_hamiltonian(0, ha, true, 0);
     build_string_hamiltonian(1, hb, false, 0);
-    F2G_CUDA(cudaDeviceSynchronize());
+    F2G_CUDA(cudaStreamSynchronize(0)); // set-up ran on the legacy stream: wait for it alone
     fp32_ready = false;
     if (precision == kFP32)
         ensure_fp32();
@@ -446,36 +455,33 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
     fp32_ready = true;
 }
 
-void SigmaBuilder::prepare_untimed() {
-    const int64_t nd = s->ndet;
-    if (nd == 0)
+// Reserves the graph scratch for nvec vectors in both precisions. Captured graphs hold its
+// addresses, so once graph_users > 0 it may not grow (a larger request is an error).
+void SigmaBuilder::prepare_untimed(int nvec) {
+    nvec = std::max(1, nvec);
+    if (nvec <= untimed_nvec)
         return;
-    Ct.reserve(nd);
-    Tt.reserve(nd);
-    if (precision == kFP32) {
-        ensure_fp32();
-        fC.reserve(nd);
-        fS.reserve(nd);
-        fCt.reserve(nd);
-        fTt.reserve(nd);
-    }
+    if (*graph_users > 0)
+        throw Error(2, "sigma builder: captured graphs use its graph scratch for " + std::to_string(untimed_nvec) +
+                           " vectors; a graph of " + std::to_string(nvec) + " vectors needs a new builder");
+    const size_t tot = (size_t)nvec * std::max<int64_t>(1, s->ndet);
+    gCt.reserve(tot);
+    gTt.reserve(tot);
+    gfC.reserve(tot);
+    gfS.reserve(tot);
+    gfCt.reserve(tot);
+    gfTt.reserve(tot);
+    untimed_nvec = nvec;
 }
 
-void SigmaBuilder::apply_untimed(const double* C, double* sigma, cudaStream_t st) {
-    const int64_t nd = s->ndet;
-    if (nd == 0)
+void SigmaBuilder::apply_untimed(const double* C, double* sigma, cudaStream_t st, int nvec) {
+    if (s->ndet == 0 || nvec <= 0)
         return;
-    if (precision == kFP64) {
-        run<double>(C, sigma, st, 7, false);
-    } else {
-        float* c = fC.reserve(nd);
-        float* sg = fS.reserve(nd);
-        k_convert<double, float><<<1024, 256, 0, st>>>(nd, C, c);
-        F2G_LAUNCH("k_convert C");
-        run<float>(c, sg, st, 7, false);
-        k_convert<float, double><<<1024, 256, 0, st>>>(nd, sg, sigma);
-        F2G_LAUNCH("k_convert sigma");
-    }
+    if (nvec > untimed_nvec)
+        throw Error(2, "apply_untimed: more vectors than prepared");
+    if (precision == kFP32 && !fp32_ready)
+        throw Error(1, "apply_untimed: FP32 Hamiltonian copies are not ready");
+    apply_batch(C, sigma, st, nvec, false, true);
 }
 
 // The reference's K-block memory contract (ci_sigma_builder_knowles_handy.cc:15-32): every term
@@ -515,50 +521,60 @@ template <typename T> static int64_t opposite_smem(int n, int ma, int N0b, bool 
     return (int64_t)n * ma * n * sizeof(T) + (smrow ? (int64_t)N0b * sizeof(T) : 0) + (int64_t)ma * 4 + 16;
 }
 
+// All launchers take nvec vectors stored back to back (stride = the determinant count) and cover
+// them in one launch.
+// max_ctas > 0 caps the grid (one CTA per SM at 512 threads): the kernel then loops over the alpha
+// strings and leaves the other SMs to concurrent work.
+static thread_local int g_opposite_max_ctas = 0;
+
 template <typename T, int MB, bool SMROW>
-static void launch_opposite_mb(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st) {
+static void launch_opposite_mb(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st, int nvec) {
     const int n = s->norb, ma = s->a.m1, mb = s->b.m1;
     const int64_t smem = opposite_smem<T>(n, ma, (int)s->b.N0, SMROW);
     auto kern = k_opposite<T, MB, SMROW>;
     F2G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<(unsigned)s->a.N0, 512, smem, st>>>(n, s->na, (int)s->b.N0, s->b.N1, ma, mb, s->a.down1.get(),
-                                               s->a.up1.get(), s->b.up1.get(), V, C, sig);
+    int64_t gx = s->a.N0;
+    if (g_opposite_max_ctas > 0)
+        gx = std::min<int64_t>(gx, g_opposite_max_ctas);
+    kern<<<dim3((unsigned)gx, (unsigned)nvec), 512, smem, st>>>(s->a.N0, n, s->na, (int)s->b.N0, s->b.N1, ma, mb,
+                                                               s->a.down1.get(), s->a.up1.get(), s->b.up1.get(), V,
+                                                               C, sig);
     F2G_LAUNCH("k_opposite");
 }
 
 template <typename T, bool SMROW>
-static void launch_opposite_r(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st) {
+static void launch_opposite_r(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st, int nvec) {
     const int mb = s->b.m1;
     if (mb <= 4)
-        launch_opposite_mb<T, 4, SMROW>(s, V, C, sig, st);
+        launch_opposite_mb<T, 4, SMROW>(s, V, C, sig, st, nvec);
     else if (mb <= 8)
-        launch_opposite_mb<T, 8, SMROW>(s, V, C, sig, st);
+        launch_opposite_mb<T, 8, SMROW>(s, V, C, sig, st, nvec);
     else if (mb <= 9)
-        launch_opposite_mb<T, 9, SMROW>(s, V, C, sig, st);
+        launch_opposite_mb<T, 9, SMROW>(s, V, C, sig, st, nvec);
     else if (mb <= 12)
-        launch_opposite_mb<T, 12, SMROW>(s, V, C, sig, st);
+        launch_opposite_mb<T, 12, SMROW>(s, V, C, sig, st, nvec);
     else if (mb <= 16)
-        launch_opposite_mb<T, 16, SMROW>(s, V, C, sig, st);
+        launch_opposite_mb<T, 16, SMROW>(s, V, C, sig, st, nvec);
     else if (mb <= 24)
-        launch_opposite_mb<T, 24, SMROW>(s, V, C, sig, st);
+        launch_opposite_mb<T, 24, SMROW>(s, V, C, sig, st, nvec);
     else
         throw Error(1, "opposite-spin kernel supports at most 24 beta holes per 1-hole string");
 }
 
 template <typename T>
-static void launch_opposite(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st) {
+static void launch_opposite(const CIStrings* s, const T* V, const T* C, T* sig, cudaStream_t st, int nvec = 1) {
     if (s->na < 1 || s->nb < 1 || s->a.N0 == 0 || s->b.N1 == 0)
         return;
     const bool smrow = opposite_smem<T>(s->norb, s->a.m1, (int)s->b.N0, true) <= 200 * 1024;
     if (smrow)
-        launch_opposite_r<T, true>(s, V, C, sig, st);
+        launch_opposite_r<T, true>(s, V, C, sig, st, nvec);
     else
-        launch_opposite_r<T, false>(s, V, C, sig, st);
+        launch_opposite_r<T, false>(s, V, C, sig, st, nvec);
 }
 
 template <typename T>
 static void launch_spmm(const StringHamiltonian& sh, const T* val, int64_t nrows, int ncols, const T* X, T* Y,
-                        bool accumulate, cudaStream_t st) {
+                        bool accumulate, cudaStream_t st, int nvec = 1) {
     if (nrows == 0 || ncols == 0 || sh.nnz == 0)
         return;
     constexpr int VEC = sizeof(T) == 8 ? 4 : 8;
@@ -566,59 +582,58 @@ static void launch_spmm(const StringHamiltonian& sh, const T* val, int64_t nrows
     const size_t smem = (size_t)sh.nnz * (sizeof(T) + sizeof(int32_t));
     if (smem > 48 * 1024)
         F2G_CUDA(cudaFuncSetAttribute(k_spmm_rows<T, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((unsigned)nrows, (unsigned)ceil_div(ncols, tile));
-    k_spmm_rows<T, VEC><<<grid, 128, smem, st>>>(nrows, ncols, sh.nnz, sh.col.get(), val, X, Y, accumulate ? 1 : 0);
+    dim3 grid((unsigned)nrows, (unsigned)ceil_div(ncols, tile), (unsigned)nvec);
+    k_spmm_rows<T, VEC><<<grid, 128, smem, st>>>(nrows, ncols, sh.nnz, sh.col.get(), val, X, Y, accumulate ? 1 : 0,
+                                                 nrows * (int64_t)ncols);
     F2G_LAUNCH("k_spmm_rows");
 }
 
 template <typename T>
-static void launch_transpose(int64_t rows, int64_t cols, const T* in, T* out, cudaStream_t st) {
+static void launch_transpose(int64_t rows, int64_t cols, const T* in, T* out, cudaStream_t st, int nvec = 1) {
     if (rows == 0 || cols == 0)
         return;
-    dim3 grid((unsigned)ceil_div(cols, 32), (unsigned)ceil_div(rows, 32));
+    dim3 grid((unsigned)ceil_div(cols, 32), (unsigned)ceil_div(rows, 32), (unsigned)nvec);
     k_transpose<T><<<grid, dim3(32, 8), 0, st>>>(rows, cols, in, out);
     F2G_LAUNCH("k_transpose");
 }
 
 // mask bits: 1 alpha same-spin (+H0 +H1a), 2 beta same-spin (+H1b), 4 opposite spin
-template <typename T> void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed) {
+// Ct_, Tt_: transposition scratch of nvec * ndet elements.
+template <typename T>
+void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_) {
     const int64_t NA = s->a.N0, NB = s->b.N0, nd = NA * NB;
+    g_opposite_max_ctas = max_ctas;
     const T* valb = nullptr;
     const T* vala = nullptr;
     const T* Vt = nullptr;
-    T *Ct_, *Tt_;
     if constexpr (sizeof(T) == 8) {
         vala = ha.val.get();
         valb = hb.val.get();
         Vt = dV.get();
-        Ct_ = Ct.reserve(nd);
-        Tt_ = Tt.reserve(nd);
     } else {
         vala = ha.valf.get();
         valb = hb.valf.get();
         Vt = fV.get();
-        Ct_ = fCt.reserve(nd);
-        Tt_ = fTt.reserve(nd);
     }
     if (timed)
         F2G_CUDA(cudaEventRecord(ev[0], st));
     // beta same spin: sigma = (Hbb C^T)^T
     if ((mask & 2) && s->nb >= 1) {
-        launch_transpose<T>(NA, NB, C, Ct_, st);
-        launch_spmm<T>(hb, valb, NB, (int)NA, Ct_, Tt_, false, st);
-        launch_transpose<T>(NB, NA, Tt_, sig, st);
+        launch_transpose<T>(NA, NB, C, Ct_, st, nvec);
+        launch_spmm<T>(hb, valb, NB, (int)NA, Ct_, Tt_, false, st, nvec);
+        launch_transpose<T>(NB, NA, Tt_, sig, st, nvec);
     } else {
-        F2G_CUDA(cudaMemsetAsync(sig, 0, nd * sizeof(T), st));
+        F2G_CUDA(cudaMemsetAsync(sig, 0, (size_t)nvec * nd * sizeof(T), st));
     }
     if (timed)
         F2G_CUDA(cudaEventRecord(ev[1], st));
     // alpha same spin + H0
     if (mask & 1)
-        launch_spmm<T>(ha, vala, NA, (int)NB, C, sig, true, st);
+        launch_spmm<T>(ha, vala, NA, (int)NB, C, sig, true, st, nvec);
     if (timed)
         F2G_CUDA(cudaEventRecord(ev[2], st));
     if (mask & 4)
-        launch_opposite<T>(s, Vt, C, sig, st);
+        launch_opposite<T>(s, Vt, C, sig, st, nvec);
     if (timed)
         F2G_CUDA(cudaEventRecord(ev[3], st));
 }
@@ -635,7 +650,7 @@ void SigmaBuilder::flush_timers() {
     t_acc[1] += ab * 1e-3;
     t_acc[2] += aa * 1e-3;
     t_acc[3] += bb * 1e-3;
-    builds += 1;
+    builds += ev_nvec;
     ev_pending = false;
 }
 
@@ -645,24 +660,50 @@ void SigmaBuilder::avg_build_time(double* out) {
         out[i] = builds ? t_acc[i] / builds : 0.0;
 }
 
-void SigmaBuilder::hamiltonian(const double* C, double* sigma, cudaStream_t st) {
+// Vectors are built in batches of at most kBatchElems determinants (one launch per term for the
+// whole batch); the transposition scratch grows with the batch.
+constexpr int64_t kBatchElems = int64_t(1) << 24;
+
+int SigmaBuilder::batch_size(int nvec) const {
+    const int64_t nd = std::max<int64_t>(1, s->ndet);
+    return (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)nvec, kBatchElems / nd, 65535}));
+}
+
+void SigmaBuilder::hamiltonian(const double* C, double* sigma, cudaStream_t st, int nvec) {
     check_memory();
-    flush_timers();
     const int64_t nd = s->ndet;
-    if (nd == 0)
+    if (nd == 0 || nvec <= 0)
         return;
+    const int bs = batch_size(nvec);
+    for (int v0 = 0; v0 < nvec; v0 += bs) {
+        const int nv = std::min(bs, nvec - v0);
+        flush_timers();
+        apply_batch(C + (int64_t)v0 * nd, sigma + (int64_t)v0 * nd, st, nv, true, false);
+        ev_pending = true;
+        ev_nvec = nv;
+    }
+}
+
+// graph: use the scratch set reserved by prepare_untimed (never reallocated while graphs captured
+// with it exist); otherwise the growable scratch.
+void SigmaBuilder::apply_batch(const double* C, double* sigma, cudaStream_t st, int nvec, bool timed, bool graph) {
+    const int64_t nd = s->ndet;
+    const size_t tot = (size_t)nvec * nd;
     if (precision == kFP64) {
-        run<double>(C, sigma, st, 7, true);
+        double* ct = graph ? gCt.get() : Ct.reserve(tot);
+        double* tt = graph ? gTt.get() : Tt.reserve(tot);
+        run<double>(C, sigma, st, 7, timed, nvec, ct, tt);
     } else {
-        float* c = fC.reserve(nd);
-        float* sg = fS.reserve(nd);
-        k_convert<double, float><<<1024, 256, 0, st>>>(nd, C, c);
+        float* c = graph ? gfC.get() : fC.reserve(tot);
+        float* sg = graph ? gfS.get() : fS.reserve(tot);
+        float* ct = graph ? gfCt.get() : fCt.reserve(tot);
+        float* tt = graph ? gfTt.get() : fTt.reserve(tot);
+        k_convert<double, float><<<1024, 256, 0, st>>>((int64_t)tot, C, c);
         F2G_LAUNCH("k_convert C");
-        run<float>(c, sg, st, 7, true);
-        k_convert<float, double><<<1024, 256, 0, st>>>(nd, sg, sigma);
+        run<float>(c, sg, st, 7, timed, nvec, ct, tt);
+        k_convert<float, double><<<1024, 256, 0, st>>>((int64_t)tot, sg, sigma);
         F2G_LAUNCH("k_convert sigma");
     }
-    ev_pending = true;
 }
 
 void SigmaBuilder::term(int which, const double* C, double* sigma, cudaStream_t st) {
@@ -708,19 +749,19 @@ void SigmaBuilder::term(int which, const double* C, double* sigma, cudaStream_t 
     F2G_CUDA(cudaStreamSynchronize(st));
 }
 
+// Stream-ordered; the string-energy scratch is kept by the builder (no allocation after the first
+// call, so no implicit device synchronisation).
 void SigmaBuilder::det_energies(double* out, cudaStream_t st) {
     const int64_t NA = s->a.N0, NB = s->b.N0;
     if (NA * NB == 0)
         return;
-    DevBuf<double> ea, eb, jr;
-    ea.reserve(NA);
-    eb.reserve(NB);
-    jr.reserve((size_t)NA * std::max(1, n));
-    k_string_energy<<<ceil_div(NA, 128), 128, 0, st>>>(n, NA, s->a.str.get(), dH.get(), dV.get(), ea.get(), jr.get());
-    k_string_energy<<<ceil_div(NB, 128), 128, 0, st>>>(n, NB, s->b.str.get(), dH.get(), dV.get(), eb.get(), nullptr);
-    k_det_energy<<<ceil_div(NA * NB, 256), 256, 0, st>>>(n, NA, NB, E, s->b.str.get(), ea.get(), eb.get(), jr.get(), out);
+    double* ea = eA.reserve(NA);
+    double* eb = eB.reserve(NB);
+    double* jr = eJ.reserve((size_t)NA * std::max(1, n));
+    k_string_energy<<<ceil_div(NA, 128), 128, 0, st>>>(n, NA, s->a.str.get(), dH.get(), dV.get(), ea, jr);
+    k_string_energy<<<ceil_div(NB, 128), 128, 0, st>>>(n, NB, s->b.str.get(), dH.get(), dV.get(), eb, nullptr);
+    k_det_energy<<<ceil_div(NA * NB, 256), 256, 0, st>>>(n, NA, NB, E, s->b.str.get(), ea, eb, jr, out);
     F2G_LAUNCH("k_det_energy");
-    F2G_CUDA(cudaStreamSynchronize(st));
 }
 
 } // namespace f2g

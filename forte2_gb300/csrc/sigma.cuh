@@ -1,6 +1,7 @@
 // The sigma builder: sigma = H C for one or more determinant vectors, resident on the device.
 #pragma once
 
+#include <memory>
 #include <vector>
 
 #include "strings.cuh"
@@ -31,18 +32,21 @@ struct SigmaBuilder {
                              // 1 Harrison-Zarrabian (what the Python driver selects)
     size_t memory = size_t(1) << 30;
     int precision = kFP64;
+    int max_ctas = 0; // cap on the opposite-spin grid (0 = one CTA per alpha string)
     int log_level = 3;
 
     // scratch (grown on demand)
     DevBuf<double> Ct, Tt;
     DevBuf<float> fC, fCt, fTt, fS;
     DevBuf<double> hostC, hostS; // device staging for host-buffer calls
+    DevBuf<double> eA, eB, eJ, eDet; // determinant-energy scratch (string energies, exchange rows, energies)
 
     // timing: [total, aabb, aaaa, bbbb] accumulated from CUDA events
     double t_acc[4] = {0, 0, 0, 0};
     int builds = 0;
     cudaEvent_t ev[5] = {};
     bool ev_pending = false;
+    int ev_nvec = 1; // vectors covered by the pending events
 
     SigmaBuilder(CIStrings* s, double E, const double* H, const double* V, int log_level);
     ~SigmaBuilder();
@@ -50,13 +54,21 @@ struct SigmaBuilder {
     void ensure_fp32();
     bool fp32_ready = false;
     void check_memory() const;
-    void hamiltonian(const double* C, double* sigma, cudaStream_t st);
+    // nvec vectors back to back; built in batches of batch_size(nvec) vectors
+    void hamiltonian(const double* C, double* sigma, cudaStream_t st, int nvec = 1);
+    int batch_size(int nvec) const;
     // Stream-ordered variants for solves that share the device with others: no device-wide
     // synchronisation, no timers, no allocation (prepare_untimed() allocates the scratch first),
     // so the calls can be captured into a CUDA graph.
     void set_hamiltonian_async(double E, const double* H, const double* V, cudaStream_t st);
-    void prepare_untimed();
-    void apply_untimed(const double* C, double* sigma, cudaStream_t st);
+    void prepare_untimed(int nvec);
+    void apply_untimed(const double* C, double* sigma, cudaStream_t st, int nvec);
+    int untimed_nvec = 0;
+    // captured graphs that reference the graph scratch (shared so that a graph outliving the
+    // builder can still release its count)
+    std::shared_ptr<int> graph_users = std::make_shared<int>(0);
+    DevBuf<double> gCt, gTt;
+    DevBuf<float> gfC, gfS, gfCt, gfTt;
     // one HZ term into sigma (overwrites): 0 H0, 1 H1a, 2 H1b, 3 aabb, 4 aaaa(+H1a? no), 5 bbbb
     void term(int which, const double* C, double* sigma, cudaStream_t st);
     void det_energies(double* out, cudaStream_t st);
@@ -65,7 +77,9 @@ struct SigmaBuilder {
 
   private:
     void build_string_hamiltonian(int spin, StringHamiltonian& sh, bool with_e0, cudaStream_t st);
-    template <typename T> void run(const T* C, T* sig, cudaStream_t st, int mask, bool timed);
+    template <typename T>
+    void run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_);
+    void apply_batch(const double* C, double* sigma, cudaStream_t st, int nvec, bool timed, bool graph);
 };
 
 int ss_row_nnz(int n, int k);

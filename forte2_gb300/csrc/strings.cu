@@ -122,7 +122,7 @@ CIStrings::CIStrings(int na_, int nb_, int norb_) : norb(norb_), na(na_), nb(nb_
     F2G_CUDA(cudaMemcpy(binom.get(), h.data(), h.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
     a.build(norb, na, binom.get(), 0);
     b.build(norb, nb, binom.get(), 0);
-    F2G_CUDA(cudaDeviceSynchronize());
+    F2G_CUDA(cudaStreamSynchronize(0)); // set-up ran on the legacy stream: wait for it alone
     ndet = a.N0 * b.N0;
 }
 

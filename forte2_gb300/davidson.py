@@ -150,6 +150,12 @@ class DavidsonLiuSolver:
             raise ValueError("guesses must be shape (size, n_guess)")
         self._guesses = G.to("cuda").T.contiguous()  # rows
 
+    def add_guess_rows(self, rows):
+        """Guesses as a device tensor of rows (n_guess, size); no host round trip."""
+        if rows.dim() != 2 or rows.shape[1] != self.size:
+            raise ValueError("guess rows must be shape (n_guess, size)")
+        self._guesses = rows.contiguous()
+
     def add_project_out(self, project_out):
         """Vectors to project out (davidsonliu.py:150-172); shorter vectors are zero-padded."""
         torch = _torch()
@@ -363,42 +369,52 @@ class DavidsonLiuSolver:
         L = lib()
         nroot, maxm = self.nroot, self.max_subspace_size
         self.used_graph = True
+        g = self._graph_for(spec)
+        dev_m = None
         if not self._executed:
+            # Gram-Schmidt of the guesses decided on the device; the basis size stays on the device
+            # until the first read, which overlaps the first launch of the iterations
             G = self._guesses if hasattr(self, "_guesses") else self._random_rows(nroot)
             ncand = min(G.shape[0], maxm)
-            added = torch.zeros(1, dtype=torch.int32, device="cuda")
+            if getattr(self, "_added", None) is None:
+                self._added = torch.zeros(1, dtype=torch.int32, device="cuda")
+            dev_m = self._added
             check(L.f2g_dav_gs_append(_ptr(self.b), self.b.stride(0), maxm, 0, _ptr(G), G.stride(0), ncand, self.size,
                                       self.schmidt_discard_threshold, self.schmidt_orthogonality_threshold,
-                                      min(nroot, maxm), int(self.seed), _ptr(added), stream_handle()))
-            (a,) = yield [added]
-            self.basis_size = int(a[0])
+                                      min(nroot, maxm), int(self.seed), _ptr(dev_m), stream_handle()))
+            m = max(ncand, min(nroot, maxm))  # rows that may hold a basis vector
             self.sigma_size = 0
             self.lam_old[:] = 0.0
-        m = self.basis_size
+        else:
+            m = self.basis_size
         if m == 0:
             raise RuntimeError("Davidson-Liu solver: no basis vector survived orthonormalisation.")
-        S = self._dots_dev(self.b[:m], self.b[:m])
+        S = self._dots_dev(self.b[:m], self.b[:m]).contiguous()
         if m > self.sigma_size:
+            # with a device basis size this covers every row the Gram-Schmidt may have filled;
+            # rows beyond the accepted ones are computed needlessly and never used
             yield from self._sigma_steps(self.sigma_size, m)
-        self.sigma_size = m
-        g = self._graph_for(spec)
         lam_old = np.ascontiguousarray(self.lam_old[:nroot])
-        check(L.f2g_dgraph_reset(g, m, m, lam_old.ctypes.data, nroot, float(self.e_tol), float(self.r_tol),
-                                 int(self.maxiter), int(self.stall_window), float(self.stall_floor), stream_handle()))
-        check(L.f2g_dgraph_launch(g, stream_handle()))
-        (S,) = yield [S]
-        if not np.allclose(S, np.eye(S.shape[0]), atol=1e-11):
-            raise ValueError("Orthonormality check failed." +
-                             f" Largest deviation from orthonormality: {np.max(np.abs(S - np.eye(S.shape[0])))}")
+        # the reset checks the starting overlap on the device; the first host read is the state
+        # copied by the first launch
+        check(L.f2g_dgraph_reset(g, m, -1 if dev_m is not None else m, _ptr(dev_m) if dev_m is not None else None,
+                                 _ptr(S), S.stride(0), lam_old.ctypes.data, nroot, float(self.e_tol),
+                                 float(self.r_tol), int(self.maxiter), int(self.stall_window), float(self.stall_floor),
+                                 stream_handle()))
+        self._graph_S = S  # kept alive until the reset has run
         ints = np.zeros(8, dtype=np.int32)
-        dbl = np.zeros(130, dtype=np.float64)
+        dbl = np.zeros(131, dtype=np.float64)
         while True:
+            check(L.f2g_dgraph_launch(g, stream_handle()))
+            yield []
             check(L.f2g_dgraph_state(g, ints.ctypes.data, dbl.ctypes.data))
             if ints[3] != 0:
                 break
-            check(L.f2g_dgraph_launch(g, stream_handle()))
-            yield []
         m, iters, status = int(ints[0]), int(ints[2]), int(ints[3])
+        if status == 6:
+            if m == 0:
+                raise RuntimeError("Davidson-Liu solver: no basis vector survived orthonormalisation.")
+            raise ValueError(f"Orthonormality check failed. Largest deviation from orthonormality: {dbl[130]}")
         if status == 4:
             raise ValueError(f"Before collapse: Checking orthonormality of Bblk with size {m}")
         if status == 5:

@@ -48,6 +48,15 @@ def poisson_stream(n_requests=10000, rate=200.0, seed=5, sizes=(6, 8, 10, 12, 14
     return [Request(i, float(t[i]), int(n[i]), int(mult[i]), int(roots[i]), 7_000_000 + i) for i in range(n_requests)]
 
 
+def request_precision(r, precision, mixed_min_ndet=200_000):
+    """Precision a request runs in. In mixed mode only spaces of at least mixed_min_ndet
+    determinants use FP32 sigma builds: below that a solve is bound by launches and host steps,
+    not by sigma arithmetic, and plain FP64 is both faster and exact."""
+    if precision == "mixed" and comb(r.norb, r.norb // 2) ** 2 < mixed_min_ndet:
+        return "fp64"
+    return precision
+
+
 class SolverPool:
     """Idle solvers by shape (orbitals, multiplicity, roots, precision). A request of a shape seen
     before takes an idle solver and only uploads its integrals: strings, spin adapter, sigma-builder
@@ -55,17 +64,20 @@ class SolverPool:
     their device memory, so they count against the HBM budget and the least recently used ones are
     dropped when an admission needs the room."""
 
-    def __init__(self, precision, e_tol):
-        self.precision, self.e_tol = precision, e_tol
+    def __init__(self, precision, e_tol, mixed_min_ndet=200_000):
+        self.precision, self.e_tol, self.mixed_min_ndet = precision, e_tol, mixed_min_ndet
         self.idle = {}  # key -> list of (solver, footprint), most recent last
         self.order = deque()  # keys of idle solvers, least recent first
         self.idle_bytes = 0
         self.created = 0
         self.reused = 0
+        self.prewarmed = 0
 
-    @staticmethod
-    def key(r):
-        return (r.norb, r.multiplicity, r.nroot)
+    def prec(self, r):
+        return request_precision(r, self.precision, self.mixed_min_ndet)
+
+    def key(self, r):
+        return (r.norb, r.multiplicity, r.nroot, self.prec(r))
 
     def take(self, r):
         lst = self.idle.get(self.key(r))
@@ -78,7 +90,7 @@ class SolverPool:
             self.reused += 1
             return solver
         self.created += 1
-        return make_solver(r.inst, self.precision, e_tol=self.e_tol)
+        return make_solver(r.inst, self.prec(r), e_tol=self.e_tol)
 
     def has_idle(self, r):
         return bool(self.idle.get(self.key(r)))
@@ -87,6 +99,24 @@ class SolverPool:
         self.idle.setdefault(self.key(r), []).append((solver, fp))
         self.order.append(self.key(r))
         self.idle_bytes += fp
+
+    def prewarm(self, shapes, nstreams=16):
+        """Create idle solvers before requests arrive: for each (norb, multiplicity, nroot, count)
+        `count` solvers, each run once on seeded integrals so that its tables, buffers and
+        captured iteration graphs exist (creating them synchronises the device, which a running
+        server should not do per request). Returns the number created."""
+        jobs = []
+        for norb, mult, nroot, count in shapes:
+            for _ in range(count):
+                r = Request(-1, 0.0, norb, mult, nroot, 9_000_000 + len(jobs))
+                solver = make_solver(r.inst, self.prec(r), e_tol=self.e_tol)
+                jobs.append(((r, solver), solver.run_steps()))
+        StepScheduler(nstreams).run(jobs)
+        for (r, solver), _ in jobs:
+            self.give(r, solver, footprint_bytes(r.norb, r.norb // 2, r.norb // 2, r.nroot))
+        self.created += len(jobs)
+        self.prewarmed = len(jobs)
+        return len(jobs)
 
     def evict_one(self):
         if not self.order:
@@ -97,9 +127,28 @@ class SolverPool:
         return True
 
 
+def default_prewarm(sizes=(6, 8, 10), per_size=(16, 6, 2)):
+    """Idle solvers to create before a stream: for every multiplicity 1/3 and 1-3 roots, per_size[i]
+    solvers of (sizes[i] e, sizes[i] o) (the small spaces that make up almost all requests)."""
+    return [(n, mult, nroot, c) for n, c in zip(sizes, per_size) for mult in (1, 3) for nroot in (1, 2, 3)]
+
+
+def sm_count():
+    import torch
+
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
 def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1e-10, max_inflight=256,
-          pool=True):
-    """Serve a request stream in real time; returns per-request latencies and summary stats."""
+          pool=True, small_norb=10, mixed_min_ndet=200_000, prewarm=None, reserve_sms=48):
+    """Serve a request stream in real time; returns per-request latencies and summary stats.
+    prewarm: (norb, multiplicity, nroot, count) shapes of idle solvers to create before the clock
+    starts (see SolverPool.prewarm)."""
+    sp = SolverPool(precision, e_tol, mixed_min_ndet)
+    t0 = time.perf_counter()
+    if pool and prewarm:
+        sp.prewarm(prewarm, nstreams)
+    prewarm_s = time.perf_counter() - t0
     sched = StepScheduler(nstreams)
     pending = deque(sorted(requests, key=lambda r: r.arrival))
     waiting = deque()
@@ -108,7 +157,6 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
     energies = {}
     t_start = time.perf_counter()
     peak = [0, 0]
-    sp = SolverPool(precision, e_tol)
 
     def admit(now, active):
         rel = now - t_start
@@ -125,9 +173,14 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
             if used[0] + sp.idle_bytes + extra > hbm_budget and (active or new):
                 break
             waiting.popleft()
-            solver = sp.take(r) if pool else make_solver(r.inst, precision, e_tol=e_tol)
+            solver = sp.take(r) if pool else make_solver(r.inst, sp.prec(r), e_tol=e_tol)
+            if r.norb > small_norb:
+                # a large solve leaves reserve_sms SMs to the small latency-bound ones
+                solver.sigma_max_blocks = max(1, sm_count() - reserve_sms)
             used[0] += fp
-            new.append(((r, solver), solver.run_steps(), fp))
+            # small spaces (latency bound, many requests) on high-priority streams: a long kernel
+            # of a large request then does not hold their short kernels back
+            new.append(((r, solver), solver.run_steps(), fp, r.norb <= small_norb))
         peak[0] = max(peak[0], len(active) + len(new))
         peak[1] = max(peak[1], used[0] + sp.idle_bytes)
         if not new and not active and not waiting:
@@ -153,6 +206,8 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
         "solves_per_s": len(requests) / wall, "p50_latency_s": float(np.percentile(L, 50)),
         "p99_latency_s": float(np.percentile(L, 99)), "mean_latency_s": float(L.mean()),
         "max_inflight": peak[0], "peak_footprint_gb": peak[1] / 2**30, "rounds": sched.rounds,
-        "solvers_created": sp.created, "solvers_reused": sp.reused,
+        "solvers_created": sp.created, "solvers_reused": sp.reused, "solvers_prewarmed": sp.prewarmed,
+        "prewarm_s": round(prewarm_s, 3), "streams": sched.max_streams,
+        "host_s": {k: round(v, 3) for k, v in sched.host_s.items()}, "polls": sched.polls,
         "sizes": {int(n): int(sum(1 for r in requests if r.norb == n)) for n in sorted({r.norb for r in requests})},
     }, lat, energies

@@ -61,6 +61,10 @@ int f2g_sigma_set_memory(void* sigma, int mb);
 /* 0 = FP64 (the reference's arithmetic), 1 = FP32 compute for every sigma term (mixed mode;
  * the caller refines in FP64). No reference counterpart. */
 int f2g_sigma_set_precision(void* sigma, int precision);
+/* Cap the thread blocks of the opposite-spin kernel (one per SM; 0 = one per alpha string, the
+ * default). A capped build loops over the alpha strings and leaves the other SMs to concurrent
+ * work, e.g. small latency-bound solves beside a large one. Same results. No reference counterpart. */
+int f2g_sigma_set_max_blocks(void* sigma, int max_blocks);
 /* Hamiltonian(basis, sigma) for nvec vectors of length ndet stored back to back
  * (ci_sigma_builder.cc:187-218); sigma is overwritten. */
 int f2g_sigma_apply(void* sigma, const double* dev_C, double* dev_sigma, int nvec, void* stream);
@@ -90,6 +94,8 @@ int f2g_hdiag_csf(void* sigma, void* sa, double* dev_out, void* stream);
 /* Dense <I|H|J> over CSF indices idx[0..m) (slater_rules_csf, ci_sigma_builder.cc:278-315),
  * host_out is m x m row-major. */
 int f2g_csf_matrix(void* sigma, void* sa, const int64_t* host_idx, int m, double* host_out);
+/* The same with device indices and a device m x m output, ordered on stream (no host wait). */
+int f2g_csf_matrix_dev(void* sigma, void* sa, const int64_t* dev_idx, int m, double* dev_out, void* stream);
 /* The CSF->determinant couplings in the reference's order (bounds[ncsf+1], det index and
  * coefficient per coupling, conf_ranges[2*nconf]) for parity checks. */
 int f2g_spin_adapter_dump(void* sa, int64_t* host_bounds, int64_t* host_det_idx, double* host_coeff,
@@ -154,16 +160,23 @@ int f2g_dgraph_destroy(void* dgraph);
 int f2g_dgraph_set_correction(void* dgraph, const double* dev_X, const double* dev_D, int64_t ldx,
                               const double* dev_Mxd, int k);
 /* Start a solve: basis rows [0, m) orthonormal in b, sigma current for [0, sigma_size), at most
- * nroot rows without sigma; lam_old = previous roots (nlam of them, zeros otherwise). */
-int f2g_dgraph_reset(void* dgraph, int m, int sigma_size, const double* host_lam_old, int nlam, double e_tol,
-                     double r_tol, int maxiter, int stall_window, double stall_floor, void* stream);
+ * nroot rows without sigma; lam_old = previous roots (nlam of them, zeros otherwise). With
+ * dev_m != NULL the basis size is read on the device from *dev_m when the reset runs (m is then an
+ * upper bound) and sigma_size < 0 means "sigma current for all m rows". With dev_S != NULL the
+ * overlap S of the starting rows (leading dimension ldS) is checked on the device as the reference
+ * checks it at the start of a solve (status 6 if it fails). */
+int f2g_dgraph_reset(void* dgraph, int m, int sigma_size, const int32_t* dev_m, const double* dev_S, int ldS,
+                     const double* host_lam_old, int nlam, double e_tol, double r_tol, int maxiter,
+                     int stall_window, double stall_floor, void* stream);
 /* Enqueue iters_per_launch iterations on stream (the first launch captures the graph). */
 int f2g_dgraph_launch(void* dgraph, void* stream);
 /* The state copied by the last completed launch (synchronise the stream first):
  * ints = {m, sigma_size, iterations, status, collapse, added, m_eig, 0}; status 0 running,
- * 1 converged, 2 iteration limit, 3 stalled, 4/5 basis not orthonormal before/after a collapse;
- * doubles = {max |dE|, max |r|, the 64 subspace eigenvalues, the 64 previous roots}. */
-int f2g_dgraph_state(void* dgraph, int32_t* host_ints8, double* host_doubles130);
+ * 1 converged, 2 iteration limit, 3 stalled, 4/5 basis not orthonormal before/after a collapse,
+ * 6 starting basis not orthonormal (or empty);
+ * doubles = {max |dE|, max |r|, the 64 subspace eigenvalues, the 64 previous roots, max |S - I| of
+ * the starting basis}. */
+int f2g_dgraph_state(void* dgraph, int32_t* host_ints8, double* host_doubles131);
 /* Ritz vectors of the first nroot roots into rows of out (davidsonliu.py:380-387). */
 int f2g_dgraph_ritz(void* dgraph, double* dev_out, int64_t ldo, void* stream);
 /* Per-iteration {mean root energy, max |dE|, max |r|, basis size} of the current solve (blocking). */

@@ -24,14 +24,15 @@ def test_batched_equals_loop(cuda):
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
 def test_serving_results_equal_solo(cuda, precision, tol):
     from forte2_gb300.batch import make_solver
-    from forte2_gb300.serve import poisson_stream, serve
+    from forte2_gb300.serve import poisson_stream, request_precision, serve
 
     reqs = poisson_stream(40, rate=2000.0, seed=3, sizes=(6, 8, 10))
-    stats, lat, energies = serve(reqs, precision=precision, nstreams=8)
+    # mixed_min_ndet = 0: the mixed-precision path serves these small spaces too
+    stats, lat, energies = serve(reqs, precision=precision, nstreams=8, mixed_min_ndet=0)
     assert stats["requests"] == 40 and stats["max_inflight"] > 1
     assert len(lat) == 40 and all(v >= 0 for v in lat.values())
     for r in reqs[::5]:
-        solo = make_solver(r.inst, precision).run()
+        solo = make_solver(r.inst, request_precision(r, precision, 0)).run()
         np.testing.assert_allclose(energies[r.idx], solo.evals, rtol=0, atol=tol)
 
 

@@ -95,3 +95,28 @@ def test_gs_append_kernel(cuda):
     with pytest.raises(ValueError):
         check(lib().f2g_dav_gs_append(B.data_ptr(), n, cap, 10, R.data_ptr(), n, 8, n, 1e-8, 1e-12, 0, 5,
                                       added.data_ptr(), stream_handle()))
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 7, 16, 33, 64])
+def test_dav_eigh_matches_numpy(cuda, m):
+    import torch
+
+    from forte2_gb300._lib import check, lib, stream_handle
+
+    rng = np.random.default_rng(m)
+    A = rng.normal(size=(m, m))
+    A = A + A.T
+    if m >= 7:
+        A[:3, :] = 0.0  # a threefold-degenerate zero eigenvalue
+        A[:, :3] = 0.0
+    G = torch.as_tensor(A, device="cuda")
+    ev = torch.empty(m, dtype=torch.float64, device="cuda")
+    V = torch.empty((m, m), dtype=torch.float64, device="cuda")
+    check(lib().f2g_dav_eigh(m, G.data_ptr(), ev.data_ptr(), V.data_ptr(), stream_handle()))
+    w = ev.cpu().numpy()
+    Q = V.cpu().numpy()
+    scale = max(1.0, np.abs(A).max())
+    np.testing.assert_allclose(w, np.linalg.eigvalsh(A), rtol=0, atol=1e-12 * scale * m)
+    assert np.all(np.diff(w) >= 0)
+    np.testing.assert_allclose(Q.T @ Q, np.eye(m), atol=1e-12 * m)
+    np.testing.assert_allclose(A @ Q, Q * w, atol=1e-11 * scale * m)

@@ -244,3 +244,20 @@ def test_det_energies_match_reference(cuda, golden_sigma):
         s, sb, _ = builder(na, nb, n, int(iseed))
         got = sb.det_energies().cpu().numpy()
         assert np.abs(got - golden_sigma[f"{key}_det_energies"]).max() < 1e-12, key
+
+
+def test_capped_opposite_grid_same_sigma(cuda, golden_sigma):
+    """A capped opposite-spin grid (blocks loop over the alpha strings) gives the same sigma."""
+    torch = cuda
+    s, sb, _ = builder(4, 4, 8, 19)
+    X = torch.as_tensor(np.stack([random_ci_vector(s.ndet, 109), random_ci_vector(s.ndet, 5)]), device="cuda")
+    Y = torch.empty_like(X)
+    sb.Hamiltonian(X, Y)
+    sb.set_max_blocks(5)  # 70 alpha strings over 5 blocks
+    Y5 = torch.empty_like(X)
+    sb.Hamiltonian(X, Y5)
+    sb.set_max_blocks(0)
+    assert rel(Y5[0].cpu().numpy(), golden_sigma["4_4_8_sigma"]) <= 1e-12
+    np.testing.assert_allclose(Y5.cpu().numpy(), Y.cpu().numpy(), rtol=0, atol=1e-13)
+    with pytest.raises(ValueError):
+        sb.set_max_blocks(-1)
