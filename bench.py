@@ -337,6 +337,7 @@ def run_davidson(a):
                      "seconds_setup": sol.timings.get("startup", 0.0) + sol.timings.get("setup", 0.0),
                      "converged": bool(sol.converged), "phases": sol.phases, "energies": [float(e) for e in sol.evals],
                      "ncsf": sol.basis_size}
+        print(json.dumps({"partial": prec, **res[prec]}), flush=True)  # each precision as soon as it is done
     out.update(res)
     if "fp64" in res and "mixed" in res:
         out["mixed_vs_fp64_abs_dE"] = [abs(x - y) for x, y in zip(res["mixed"]["energies"], res["fp64"]["energies"])]
