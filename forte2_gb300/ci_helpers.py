@@ -297,6 +297,18 @@ class CISigmaBuilder:
     def set_memory(self, mb):
         check(lib().f2g_sigma_set_memory(self.h, int(mb)))
 
+    def set_tensor_cores(self, on=True):
+        """FP32 precision: opposite-spin term on the tensor cores (3xTF32). Returns whether this
+        space supports it (else the CUDA-core kernel runs). No counterpart in the reference."""
+        avail = np.zeros(1, dtype=np.int32)
+        check(lib().f2g_sigma_set_tensor_cores(self.h, int(bool(on)), avail.ctypes.data))
+        return bool(avail[0])
+
+    def tensor_core_error(self):
+        out = np.zeros(1, dtype=np.int32)
+        check(lib().f2g_sigma_tc_error(self.h, out.ctypes.data))
+        return int(out[0])
+
     def set_max_blocks(self, n):
         """Cap the opposite-spin kernel at n thread blocks (one per SM; 0 = no cap), leaving the
         other SMs to concurrent solves. Same sigma. No counterpart in the reference."""

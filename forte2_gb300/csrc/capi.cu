@@ -202,6 +202,24 @@ int f2g_sigma_set_memory(void* sb, int mb) {
     });
 }
 
+int f2g_sigma_set_tensor_cores(void* sb, int on, int* available) {
+    return guard([&] {
+        need(sb, "sigma");
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        b->use_tc = on != 0;
+        if (available)
+            *available = b->tensor_cores_available() ? 1 : 0;
+    });
+}
+
+int f2g_sigma_tc_error(void* sb, int* out) {
+    return guard([&] {
+        need(sb, "sigma");
+        need(out, "out");
+        *out = static_cast<SigmaBuilder*>(sb)->tc_error();
+    });
+}
+
 int f2g_sigma_set_max_blocks(void* sb, int max_blocks) {
     return guard([&] {
         need(sb, "sigma");

@@ -1,0 +1,385 @@
+// Opposite-spin sigma on the 5th-generation tensor cores (tcgen05, TF32 inputs, FP32 accumulation
+// in tensor memory), for the FP32 sigma of the mixed-precision mode.
+//
+// Operator (forte2/ci/ci_sigma_builder_harrison_zarrabian.cc:197-308, written per alpha string):
+//   sigma(Ja, Jb) += sum_{(p,q)} sum_{(r,s)} V[p][r][q][s] <Ja|E^a_pq|Ia> <Jb|E^b_rs|Ib> C(Ia, Ib)
+// with V the physicist integrals (pr|qs). For one output alpha string Ja the K = na * (n - na + 1)
+// alpha excitations (p in Ja, q not in Ja - p) give the rows T[k][Ib] = sign_k C(Ia_k, Ib) of C
+// (whole rows, gathered), and
+//   U[Ib][(r,s)] = sum_k T[k][Ib] V'[(r,s)][k],   V'[(r,s)][k] = V[p_k][r][q_k][s]
+// is a dense GEMM (M = 128 beta strings per tile, N = 8 values of s x 16 of r per pass, K padded to a
+// multiple of 8). Each beta string Ib then scatters its 8 x 9 valid (s in Ib, r not in Ib - s)
+// entries into sigma(Ja, Jb = Ib - s + r) with the beta signs; sigma(Ja, :) lives in shared memory,
+// so the scatter is shared-memory atomics and each CTA owns its output row (no global atomics).
+//
+// FP32 accuracy from TF32 tensor cores: every operand is split x = hi + lo with hi, lo TF32
+// (round to nearest), and D += A_hi B_hi + A_lo B_hi + A_hi B_lo ("3xTF32"; the dropped lo*lo term
+// is below FP32 rounding).
+//
+// One CTA per SM (persistent over Ja), 256 threads: all threads gather the operand tiles into
+// shared memory in the canonical K-major no-swizzle layout (8-row x 16-byte core matrices), one
+// thread issues the MMAs into one of two 128-lane x 128-column FP32 accumulators in tensor memory
+// and commits them to an mbarrier, and while they run all 8 warps read the previous tile's
+// accumulator back (warps w and w + 4 share lanes 32 (w % 4) .. +31 and split the s columns) for
+// its scatter. Waits are bounded; a wait that
+// gives up sets an error flag and the kernel leaves without touching tensor memory again except
+// to release it.
+#include <cstdint>
+
+#include "sigma.cuh"
+
+namespace f2g {
+
+namespace {
+
+constexpr int kTcThreads = 256;
+constexpr int kTcM = 128;      // beta strings per tile (accumulator lanes)
+constexpr int kTcN = 128;      // 8 values of s x 16 values of r per pass
+constexpr int kTcMaxK = 72;    // padded alpha-excitation count (na * (n - na + 1), n <= 16)
+constexpr int kTcCols = 256;   // tensor-memory columns allocated: two 128-column accumulators
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t y;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(y) : "f"(x));
+    return __uint_as_float(y);
+}
+
+// byte offset of element (row, k) in a K-major, no-swizzle operand of kp columns: core matrices of
+// 8 rows x 4 TF32 (16 B per row, 128 B each); adjacent core matrices along K are 128 B apart
+// (leading byte offset), along rows (kp / 4) * 128 B apart (stride byte offset)
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int kp) {
+    return (uint32_t)(((row >> 3) * (kp >> 2) + (k >> 2)) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+// tcgen05 shared-memory matrix descriptor: start >> 4 [0,14), leading byte offset >> 4 [16,30),
+// stride byte offset >> 4 [32,46), version 1 [46,48), base offset 0, no swizzle [61,64) = 0
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::tf32: D F32 [4,6) = 1, A TF32 [7,10) = 2, B TF32 [10,13) = 2,
+// both K-major (bits 15, 16 = 0), N >> 3 at [17,23), M >> 4 at [24,29)
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                            ((uint32_t)(kTcM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+                 :
+                 : "r"(tmem_d), "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+// bounded wait for the phase `parity` of an mbarrier; returns false if it gave up
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (long long it = 0; it < (1ll << 26); ++it) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
+// 16 consecutive accumulator columns of this warp's 32 lanes; complete after tmem_wait_ld()
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct TcShared {
+    // operands, K-major no-swizzle core-matrix layout (16-byte aligned)
+    alignas(128) float a_hi[kTcM * kTcMaxK];
+    alignas(128) float a_lo[kTcM * kTcMaxK];
+    alignas(128) float b_hi[kTcN * kTcMaxK];
+    alignas(128) float b_lo[kTcN * kTcMaxK];
+    uint32_t ia[kTcMaxK];  // alpha string of excitation k
+    float sgn[kTcMaxK];    // its sign
+    int pk[kTcMaxK], qk[kTcMaxK];
+    alignas(8) uint64_t mbar;
+    uint32_t tmem_base;
+    int abort;
+};
+
+} // namespace
+
+// exc[Ib][i][r] for the i-th occupied orbital s of Ib and r < 16: Jb | negative << 31 for the beta
+// string Jb = Ib - s + r (r not in Ib - s), 0x00FFFFFF otherwise.
+__global__ void k_build_beta_exc(int n, int k, int64_t N0, const uint64_t* __restrict__ str,
+                                 const uint64_t* __restrict__ binom, uint32_t* __restrict__ exc) {
+    const int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (I >= N0)
+        return;
+    const uint64_t mI = str[I];
+    int i = 0;
+    for (int s = 0; s < n; ++s) {
+        if (!(mI >> s & 1))
+            continue;
+        const uint64_t mK = mI & ~(uint64_t(1) << s);
+        const int neg_s = parity_below(mK, s);
+        for (int r = 0; r < 16; ++r) {
+            uint32_t e = 0x00FFFFFFu;
+            if (r < n && !(mK >> r & 1)) {
+                const uint64_t mJ = mK | (uint64_t(1) << r);
+                const uint32_t J = (uint32_t)string_rank(mJ, n, k, binom);
+                e = J | ((uint32_t)(parity_below(mK, r) ^ neg_s) << 31);
+            }
+            exc[(I * k + i) * 16 + r] = e;
+        }
+        ++i;
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_opposite_tc(int n, int na, int nb, int ma, int64_t N0a, int N0b, const uint32_t* __restrict__ down_a,
+                  const uint32_t* __restrict__ up_a, const uint64_t* __restrict__ str_b,
+                  const uint32_t* __restrict__ exc_b, const float* __restrict__ V, const float* __restrict__ C,
+                  float* __restrict__ sig, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    TcShared& sh = *reinterpret_cast<TcShared*>(smem_raw);
+    float* row = reinterpret_cast<float*>(smem_raw + sizeof(TcShared)); // sigma(Ja, :), N0b floats
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int K = na * ma, kp = (K + 7) & ~7;
+    C += blockIdx.y * N0a * (int64_t)N0b; // vector blockIdx.y of a batch
+    sig += blockIdx.y * N0a * (int64_t)N0b;
+    const uint32_t mbar = smem_u32(&sh.mbar);
+
+    if (tid == 0) {
+        mbar_init(mbar, 1);
+        sh.abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh.tmem_base)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = sh.tmem_base;
+    uint32_t phase = 0;
+    const uint32_t lbo = 128, sbo = (uint32_t)(kp >> 2) * 128;
+
+    // scatter of one finished tile: warp w reads lanes 32 (w % 4) + [0, 32) = beta strings ib0 + that;
+    // warps w and w + 4 take the even and odd s of the pass. The excitation entries are requested
+    // first, then the accumulator columns, then one wait for both, so their latencies overlap.
+    auto scatter = [&](int ib0, uint32_t acc, int s0) {
+        const int m = (warp & 3) * 32 + lane;
+        const int Ib = ib0 + m;
+        const bool valid = Ib < N0b;
+        const uint64_t mI = valid ? str_b[Ib] : 0;
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        uint4 e4[4][4];
+        bool has[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int s = s0 + (warp >> 2) + 2 * i;
+            has[i] = valid && s < n && (mI >> s & 1);
+            if (has[i]) {
+                const int si = popc64(mI & ((uint64_t(1) << s) - 1));
+                const uint4* src = reinterpret_cast<const uint4*>(exc_b + ((int64_t)Ib * nb + si) * 16);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    e4[i][q] = __ldg(src + q);
+            }
+        }
+        uint32_t v[4][16];
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            tmem_ld16(acc + lane_base + (uint32_t)(((warp >> 2) + 2 * i) * 16), v[i]);
+        tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (!has[i])
+                continue;
+            const uint32_t e[16] = {e4[i][0].x, e4[i][0].y, e4[i][0].z, e4[i][0].w, e4[i][1].x, e4[i][1].y,
+                                    e4[i][1].z, e4[i][1].w, e4[i][2].x, e4[i][2].y, e4[i][2].z, e4[i][2].w,
+                                    e4[i][3].x, e4[i][3].y, e4[i][3].z, e4[i][3].w};
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const uint32_t jb = e[r] & 0x00FFFFFFu;
+                if (jb != 0x00FFFFFFu) // the sign bit of the entry flips the sign bit of the value
+                    atomicAdd(row + jb, __uint_as_float(v[i][r] ^ (e[r] & 0x80000000u)));
+            }
+        }
+    };
+
+    for (int64_t Ja = blockIdx.x; Ja < N0a && !sh.abort; Ja += gridDim.x) {
+        float* srow = sig + Ja * (int64_t)N0b;
+        for (int c = tid; c < N0b; c += kTcThreads)
+            row[c] = srow[c];
+        // alpha excitations of Ja: k = pi * ma + qi
+        if (tid < K) {
+            const int pi = tid / ma, qi = tid % ma;
+            const uint32_t ep = down_a[Ja * na + pi];
+            const uint32_t eq = up_a[(int64_t)e_addr(ep) * ma + qi];
+            sh.ia[tid] = e_addr(eq);
+            sh.sgn[tid] = (e_neg(ep) ^ e_neg(eq)) ? -1.0f : 1.0f;
+            sh.pk[tid] = e_orb(ep);
+            sh.qk[tid] = e_orb(eq);
+        }
+        __syncthreads();
+        for (int s0 = 0; s0 < n && !sh.abort; s0 += 8) {
+            // B = V'[(s, r)][k] for s in [s0, s0 + 8), r < 16 (zero outside the space)
+            for (int t = tid; t < kTcN * kp; t += kTcThreads) {
+                const int nn = t / kp, kk = t % kp;
+                const int s = s0 + (nn >> 4), r = nn & 15;
+                float x = 0.0f; // the alpha sign of excitation k is folded into column k of B
+                if (kk < K && s < n && r < n)
+                    x = sh.sgn[kk] * V[(((size_t)sh.pk[kk] * n + r) * n + sh.qk[kk]) * n + s];
+                const float hi = tf32_rna(x);
+                const uint32_t off = kmajor_off(nn, kk, kp) >> 2;
+                sh.b_hi[off] = hi;
+                sh.b_lo[off] = tf32_rna(x - hi);
+            }
+            int prev_ib0 = -1, tile = 0;
+            uint32_t prev_acc = 0;
+            for (int ib0 = 0; ib0 < N0b && !sh.abort; ib0 += kTcM) {
+                // A = T[Ib][k] = C(Ia_k, Ib) for Ib in [ib0, ib0 + 128): each thread takes one Ib and
+                // groups of 4 consecutive k (one 16-byte row of a core matrix, stored as a float4);
+                // for fixed k a warp reads 32 consecutive floats. All loads are issued first.
+                {
+                    constexpr int kGroups = kTcMaxK / 4 / (kTcThreads / kTcM);
+                    const int m = tid & (kTcM - 1);
+                    const int Ib = ib0 + m;
+                    const int g0 = tid >> 7;
+                    const bool in = Ib < N0b;
+                    float x[kGroups][4];
+#pragma unroll
+                    for (int j = 0; j < kGroups; ++j)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            const int kk = 4 * (g0 + j * (kTcThreads / kTcM)) + c;
+                            x[j][c] = (kk < K && in) ? __ldg(C + (int64_t)sh.ia[kk] * N0b + Ib) : 0.0f;
+                        }
+#pragma unroll
+                    for (int j = 0; j < kGroups; ++j) {
+                        const int g = g0 + j * (kTcThreads / kTcM);
+                        if (4 * g < kp) {
+                            float4 hi, lo;
+                            hi.x = tf32_rna(x[j][0]);
+                            hi.y = tf32_rna(x[j][1]);
+                            hi.z = tf32_rna(x[j][2]);
+                            hi.w = tf32_rna(x[j][3]);
+                            lo.x = tf32_rna(x[j][0] - hi.x);
+                            lo.y = tf32_rna(x[j][1] - hi.y);
+                            lo.z = tf32_rna(x[j][2] - hi.z);
+                            lo.w = tf32_rna(x[j][3] - hi.w);
+                            const uint32_t off = kmajor_off(m, 4 * g, kp) >> 2;
+                            *reinterpret_cast<float4*>(sh.a_hi + off) = hi;
+                            *reinterpret_cast<float4*>(sh.a_lo + off) = lo;
+                        }
+                    }
+                }
+                // make the generic-proxy shared-memory writes visible to the tensor cores
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncthreads();
+                // two accumulators: the MMAs of this tile run while the previous tile is scattered
+                const uint32_t acc = tmem + (uint32_t)(tile & 1) * kTcN;
+                if (tid == 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t ahi = smem_u32(sh.a_hi), alo = smem_u32(sh.a_lo);
+                    const uint32_t bhi = smem_u32(sh.b_hi), blo = smem_u32(sh.b_lo);
+                    for (int t = 0; t < kp / 8; ++t) {
+                        const uint32_t adv = (uint32_t)t * 2 * lbo; // 8 TF32 = two core matrices along K
+                        mma_tf32(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), t > 0);
+                        mma_tf32(acc, smem_desc(alo + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), 1);
+                        mma_tf32(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(blo + adv, lbo, sbo), 1);
+                    }
+                    mma_commit(mbar);
+                }
+                if (prev_ib0 >= 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    scatter(prev_ib0, prev_acc, s0);
+                }
+                const bool ok = mbar_wait(mbar, phase);
+                phase ^= 1;
+                if (!ok) {
+                    if (lane == 0)
+                        atomicExch(err, 1);
+                    sh.abort = 1;
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncthreads();
+                prev_ib0 = ib0;
+                prev_acc = acc;
+                ++tile;
+            }
+            if (prev_ib0 >= 0 && !sh.abort) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                scatter(prev_ib0, prev_acc, s0);
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+        for (int c = tid; c < N0b; c += kTcThreads)
+            srow[c] = row[c];
+        __syncthreads();
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+}
+
+size_t opposite_tc_smem(int N0b) { return sizeof(TcShared) + (size_t)N0b * sizeof(float); }
+
+bool opposite_tc_supported(const CIStrings* s) {
+    const int n = s->norb;
+    if (n > 16 || s->na < 1 || s->nb < 1 || s->a.N1 == 0 || s->b.N1 == 0)
+        return false;
+    if (s->na * (n - s->na + 1) > kTcMaxK)
+        return false;
+    return opposite_tc_smem((int)s->b.N0) <= 227 * 1024;
+}
+
+void build_beta_exc(const CIStrings* s, DevBuf<uint32_t>& exc, cudaStream_t st) {
+    const SpinStrings& b = s->b;
+    exc.reserve((size_t)std::max<int64_t>(1, b.N0 * b.k * 16));
+    k_build_beta_exc<<<ceil_div(b.N0, 128), 128, 0, st>>>(s->norb, b.k, b.N0, b.str.get(), s->binom.get(), exc.get());
+    F2G_LAUNCH("k_build_beta_exc");
+}
+
+void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, const float* C, float* sig,
+                        int* err, int max_ctas, cudaStream_t st, int nvec) {
+    const size_t smem = opposite_tc_smem((int)s->b.N0);
+    F2G_CUDA(cudaFuncSetAttribute(k_opposite_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, sms = 0;
+    F2G_CUDA(cudaGetDevice(&dev));
+    F2G_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int64_t gx = std::min<int64_t>(s->a.N0, sms);
+    if (max_ctas > 0)
+        gx = std::min<int64_t>(gx, max_ctas);
+    k_opposite_tc<<<dim3((unsigned)gx, (unsigned)nvec), kTcThreads, smem, st>>>(
+        s->norb, s->na, s->nb, s->a.m1, s->a.N0, (int)s->b.N0, s->a.down1.get(), s->a.up1.get(), s->b.str.get(), exc,
+        V, C, sig, err);
+    F2G_LAUNCH("k_opposite_tc");
+}
+
+} // namespace f2g

@@ -356,11 +356,29 @@ __global__ void k_det_energy(int n, int64_t N0a, int64_t N0b, double E0, const u
 
 // ---- host side ---------------------------------------------------------------------------------
 
+size_t opposite_tc_smem(int N0b);
+bool opposite_tc_supported(const CIStrings* s);
+void build_beta_exc(const CIStrings* s, DevBuf<uint32_t>& exc, cudaStream_t st);
+void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, const float* C, float* sig,
+                        int* err, int max_ctas, cudaStream_t st, int nvec);
+
 SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const double* V_, int ll)
     : s(s_), n(s_->norb), log_level(ll) {
     for (auto& e : ev)
         F2G_CUDA(cudaEventCreate(&e));
+    tc_err.reserve(1);
+    F2G_CUDA(cudaMemsetAsync(tc_err.get(), 0, sizeof(int), 0));
+    if (opposite_tc_supported(s))
+        build_beta_exc(s, beta_exc, 0); // ordered before set_hamiltonian's wait on the legacy stream
     set_hamiltonian(E_, H_, V_);
+}
+
+bool SigmaBuilder::tensor_cores_available() const { return beta_exc.get() != nullptr; }
+
+int SigmaBuilder::tc_error() const {
+    int h = 0;
+    F2G_CUDA(cudaMemcpy(&h, tc_err.get(), sizeof(int), cudaMemcpyDeviceToHost));
+    return h;
 }
 
 SigmaBuilder::~SigmaBuilder() {
@@ -632,8 +650,17 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
         launch_spmm<T>(ha, vala, NA, (int)NB, C, sig, true, st, nvec);
     if (timed)
         F2G_CUDA(cudaEventRecord(ev[2], st));
-    if (mask & 4)
-        launch_opposite<T>(s, Vt, C, sig, st, nvec);
+    if (mask & 4) {
+        bool done = false;
+        if constexpr (sizeof(T) == 4) {
+            if (use_tc && tensor_cores_available()) {
+                launch_opposite_tc(s, beta_exc.get(), Vt, C, sig, tc_err.get(), max_ctas, st, nvec);
+                done = true;
+            }
+        }
+        if (!done)
+            launch_opposite<T>(s, Vt, C, sig, st, nvec);
+    }
     if (timed)
         F2G_CUDA(cudaEventRecord(ev[3], st));
 }

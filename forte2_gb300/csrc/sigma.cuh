@@ -33,6 +33,12 @@ struct SigmaBuilder {
     size_t memory = size_t(1) << 30;
     int precision = kFP64;
     int max_ctas = 0; // cap on the opposite-spin grid (0 = one CTA per alpha string)
+    // FP32 opposite-spin term on the tensor cores (3xTF32, opposite_tc.cu) when the space allows it
+    bool use_tc = true;
+    DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
+    DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
+    bool tensor_cores_available() const;
+    int tc_error() const;
     int log_level = 3;
 
     // scratch (grown on demand)

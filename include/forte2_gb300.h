@@ -65,6 +65,13 @@ int f2g_sigma_set_precision(void* sigma, int precision);
  * default). A capped build loops over the alpha strings and leaves the other SMs to concurrent
  * work, e.g. small latency-bound solves beside a large one. Same results. No reference counterpart. */
 int f2g_sigma_set_max_blocks(void* sigma, int max_blocks);
+/* FP32 precision only: compute the opposite-spin term on the tensor cores (tcgen05, operands split
+ * into two TF32 parts, three products accumulated in FP32: FP32-level accuracy). *available = 1
+ * if this space supports it (n <= 16 orbitals, na (n - na + 1) <= 72, one sigma row of beta
+ * strings in shared memory); otherwise the CUDA-core kernel is used. No reference counterpart. */
+int f2g_sigma_set_tensor_cores(void* sigma, int on, int* available);
+/* 1 if a tensor-core build gave up waiting for its matrix operations (results invalid). */
+int f2g_sigma_tc_error(void* sigma, int* out);
 /* Hamiltonian(basis, sigma) for nvec vectors of length ndet stored back to back
  * (ci_sigma_builder.cc:187-218); sigma is overwritten. */
 int f2g_sigma_apply(void* sigma, const double* dev_C, double* dev_sigma, int nvec, void* stream);

@@ -261,3 +261,30 @@ def test_capped_opposite_grid_same_sigma(cuda, golden_sigma):
     np.testing.assert_allclose(Y5.cpu().numpy(), Y.cpu().numpy(), rtol=0, atol=1e-13)
     with pytest.raises(ValueError):
         sb.set_max_blocks(-1)
+
+
+@pytest.mark.parametrize("na,nb,n", [(3, 3, 6), (4, 3, 7), (2, 5, 8), (5, 5, 10), (7, 7, 14)])
+def test_fp32_tensor_core_opposite_spin(cuda, na, nb, n):
+    """FP32 sigma with the opposite-spin term on the tensor cores (3xTF32) agrees with the FP64
+    sigma to FP32 accuracy, and with the CUDA-core FP32 kernel."""
+    torch = cuda
+    from forte2_gb300.ci_helpers import CISigmaBuilder
+
+    s = make(na, nb, n)
+    ints = make_integrals(n, 600 + n)
+    sb = CISigmaBuilder(s, ints.E, ints.H, ints.V, 0)
+    c = torch.as_tensor(np.stack([random_ci_vector(s.ndet, 3 + n), random_ci_vector(s.ndet, 4 + n)]), device="cuda")
+    ref = torch.empty_like(c)
+    sb.Hamiltonian(c, ref)
+    sb.set_precision("fp32")
+    assert sb.set_tensor_cores(False) is True  # available for these spaces
+    cc = torch.empty_like(c)
+    sb.Hamiltonian(c, cc)
+    sb.set_tensor_cores(True)
+    tc = torch.empty_like(c)
+    sb.Hamiltonian(c, tc)
+    assert sb.tensor_core_error() == 0
+    for i in range(2):
+        e_tc = rel(tc[i].cpu().numpy(), ref[i].cpu().numpy())
+        e_cc = rel(cc[i].cpu().numpy(), ref[i].cpu().numpy())
+        assert e_tc < 2e-6 and e_tc < 3 * e_cc + 1e-7
