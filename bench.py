@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="sigma mode: keep the default kernel variants")
     ap.add_argument("--instances", type=int, default=64, help="batched mode: number of instances")
     ap.add_argument("--requests", type=int, default=10000, help="serve mode: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve mode: mean arrivals per second")
@@ -194,9 +195,16 @@ def run_gb300(a):
     C = torch.as_tensor(c_host, device="cuda")
     S = torch.empty_like(C)
     stream = torch.cuda.current_stream()
+    tuned = None
+    if not a.no_autotune:
+        # kernel variants with identical results, timed on this workload (forte2_gb300.autotune)
+        from forte2_gb300.autotune import autotune_sigma
+
+        tuned = {p: autotune_sigma(sb, a.norb, na, nb, p, reps=1) for p in (("fp64",) if a.no_mixed else ("fp64", "fp32"))}
     for _ in range(a.warmup):
         sb.Hamiltonian(C, S)
     torch.cuda.synchronize()
+    sb.reset_build_times()
     clocks = Clocks(local)
     clocks.start()
     barrier(dist)
@@ -272,6 +280,8 @@ def run_gb300(a):
                          "flops_per_launch": f_sp["ab"], "launch_ms": 1e3 * t_ab},
             "terms_ms": {"total": 1e3 * tot, "aabb": 1e3 * t_ab, "aaaa_h1a_h0": 1e3 * t_aa, "bbbb_h1b": 1e3 * t_bb},
             "hz_dense_flops": f_hz, "sparse_flops": f_sp,
+            "autotune": None if tuned is None else {p: {"choice": r["choice"], "ms": r["ms"], "default_ms": r["default_ms"]}
+                                                    for p, r in tuned.items()},
             "mixed_fp32_sigma_builds_per_s": mixed,
             "mixed_fp32_terms_ms": mixed_terms,
             "clocks": clk,

@@ -40,6 +40,8 @@ def _declare(L):
         "f2g_sigma_set_precision": (i32, [vp, i32]),
         "f2g_sigma_set_max_blocks": (i32, [vp, i32]),
         "f2g_sigma_set_tensor_cores": (i32, [vp, i32, P]),
+        "f2g_sigma_set_variant": (i32, [vp, i32, i32]),
+        "f2g_sigma_reset_build_times": (i32, [vp]),
         "f2g_sigma_tc_error": (i32, [vp, P]),
         "f2g_sigma_apply": (i32, [vp, P, P, i32, vp]),
         "f2g_sigma_apply_host": (i32, [vp, P, P, i32]),

@@ -177,11 +177,12 @@ def batched_instances(n_inst: int = 64, seed: int = 4000):
     return out
 
 
-def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=400):
+def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=400, autotune=True):
+    """One instance's solver; its sigma kernel variants are autotuned once per shape."""
     ints = make_integrals(inst["norb"], inst["iseed"])
     return CASCISolver(norb=inst["norb"], na=inst["na"], nb=inst["nb"], multiplicity=inst["multiplicity"],
                        nroot=inst["nroot"], E=ints.E, H=ints.H, V=ints.V, ci_params=CIParams(precision=precision),
-                       davidson_liu_params=DavidsonLiuParams(e_tol=e_tol, maxiter=maxiter))
+                       davidson_liu_params=DavidsonLiuParams(e_tol=e_tol, maxiter=maxiter), autotune=autotune)
 
 
 def footprint_bytes(norb: int, na: int, nb: int, nroot: int, basis_per_root: int = 4) -> int:

@@ -54,6 +54,8 @@ class CASCISolver:
     use_graph: bool = None
     # cap on the opposite-spin kernel's thread blocks (0 = none); see CISigmaBuilder.set_max_blocks
     sigma_max_blocks: int = 0
+    # pick the fastest sigma kernel variants for this shape before solving (forte2_gb300.autotune)
+    autotune: bool = False
 
     def __post_init__(self):
         self._ready_event = None
@@ -180,6 +182,11 @@ class CASCISolver:
         if alg == "exact":
             return self._exact()
         self.sigma_builder.set_algorithm(alg)
+        if self.autotune:
+            from .autotune import autotune_sigma
+
+            for prec in ("fp64", "fp32") if self.ci_params.precision == "mixed" else ("fp64",):
+                autotune_sigma(self.sigma_builder, self.norb, self.na, self.nb, prec)
         hdiag = self.sigma_builder.hdiag_csf_device(self.spin_adapter)
         self.timings["setup"] = time.perf_counter() - t0
         if self.ndet == 1:

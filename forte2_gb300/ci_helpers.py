@@ -304,6 +304,12 @@ class CISigmaBuilder:
         check(lib().f2g_sigma_set_tensor_cores(self.h, int(bool(on)), avail.ctypes.data))
         return bool(avail[0])
 
+    _VARIANTS = {"tensor_cores": 0, "narrow_same_spin": 1, "persistent_opposite": 2}
+
+    def set_variant(self, name, value):
+        """Select a kernel variant with identical results (see forte2_gb300.autotune)."""
+        check(lib().f2g_sigma_set_variant(self.h, self._VARIANTS[name], int(value)))
+
     def tensor_core_error(self):
         out = np.zeros(1, dtype=np.int32)
         check(lib().f2g_sigma_tc_error(self.h, out.ctypes.data))
@@ -326,6 +332,9 @@ class CISigmaBuilder:
         p = {"fp64": 0, "fp32": 1, 0: 0, 1: 1}[precision]
         check(lib().f2g_sigma_set_precision(self.h, p))
         self._precision = p
+        # kernel variants chosen by the autotuner for this precision (forte2_gb300.autotune)
+        for name, value in getattr(self, "_tuned", {}).get(self.get_precision(), {}).items():
+            self.set_variant(name, value)
 
     def get_precision(self):
         return "fp64" if self._precision == 0 else "fp32"
@@ -359,6 +368,9 @@ class CISigmaBuilder:
         out = torch.empty_like(basis)
         check(lib().f2g_sigma_term(self.h, idx, basis.data_ptr(), out.data_ptr(), stream_handle()))
         return out
+
+    def reset_build_times(self):
+        check(lib().f2g_sigma_reset_build_times(self.h))
 
     def avg_build_time(self):
         out = np.zeros(4)

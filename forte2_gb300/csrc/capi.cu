@@ -202,6 +202,32 @@ int f2g_sigma_set_memory(void* sb, int mb) {
     });
 }
 
+int f2g_sigma_reset_build_times(void* sb) {
+    return guard([&] {
+        need(sb, "sigma");
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        b->flush_timers();
+        for (double& t : b->t_acc)
+            t = 0.0;
+        b->builds = 0;
+    });
+}
+
+int f2g_sigma_set_variant(void* sb, int which, int value) {
+    return guard([&] {
+        need(sb, "sigma");
+        auto* b = static_cast<SigmaBuilder*>(sb);
+        if (which == 0)
+            b->use_tc = value != 0;
+        else if (which == 1)
+            b->spmm_narrow = value != 0;
+        else if (which == 2)
+            b->opposite_persistent = value != 0;
+        else
+            throw Error(2, "variant must be 0 (tensor cores), 1 (narrow same-spin tiles) or 2 (persistent opposite grid)");
+    });
+}
+
 int f2g_sigma_set_tensor_cores(void* sb, int on, int* available) {
     return guard([&] {
         need(sb, "sigma");

@@ -356,6 +356,13 @@ __global__ void k_det_energy(int n, int64_t N0a, int64_t N0b, double E0, const u
 
 // ---- host side ---------------------------------------------------------------------------------
 
+static int sm_count() {
+    int dev = 0, sms = 0;
+    F2G_CUDA(cudaGetDevice(&dev));
+    F2G_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return sms;
+}
+
 size_t opposite_tc_smem(int N0b);
 bool opposite_tc_supported(const CIStrings* s);
 void build_beta_exc(const CIStrings* s, DevBuf<uint32_t>& exc, cudaStream_t st);
@@ -590,12 +597,13 @@ static void launch_opposite(const CIStrings* s, const T* V, const T* C, T* sig, 
         launch_opposite_r<T, false>(s, V, C, sig, st, nvec);
 }
 
-template <typename T>
-static void launch_spmm(const StringHamiltonian& sh, const T* val, int64_t nrows, int ncols, const T* X, T* Y,
-                        bool accumulate, cudaStream_t st, int nvec = 1) {
-    if (nrows == 0 || ncols == 0 || sh.nnz == 0)
-        return;
-    constexpr int VEC = sizeof(T) == 8 ? 4 : 8;
+// columns per thread of the same-spin kernel: 0 = the default (4 FP64 / 8 FP32), 1 = half of it
+// (more thread blocks for short rows); chosen by the autotuner (SigmaBuilder::spmm_narrow)
+static thread_local int g_spmm_narrow = 0;
+
+template <typename T, int VEC>
+static void launch_spmm_v(const StringHamiltonian& sh, const T* val, int64_t nrows, int ncols, const T* X, T* Y,
+                          bool accumulate, cudaStream_t st, int nvec) {
     const int tile = 128 * VEC;
     const size_t smem = (size_t)sh.nnz * (sizeof(T) + sizeof(int32_t));
     if (smem > 48 * 1024)
@@ -604,6 +612,18 @@ static void launch_spmm(const StringHamiltonian& sh, const T* val, int64_t nrows
     k_spmm_rows<T, VEC><<<grid, 128, smem, st>>>(nrows, ncols, sh.nnz, sh.col.get(), val, X, Y, accumulate ? 1 : 0,
                                                  nrows * (int64_t)ncols);
     F2G_LAUNCH("k_spmm_rows");
+}
+
+template <typename T>
+static void launch_spmm(const StringHamiltonian& sh, const T* val, int64_t nrows, int ncols, const T* X, T* Y,
+                        bool accumulate, cudaStream_t st, int nvec = 1) {
+    if (nrows == 0 || ncols == 0 || sh.nnz == 0)
+        return;
+    constexpr int VEC = sizeof(T) == 8 ? 4 : 8;
+    if (g_spmm_narrow)
+        launch_spmm_v<T, VEC / 2>(sh, val, nrows, ncols, X, Y, accumulate, st, nvec);
+    else
+        launch_spmm_v<T, VEC>(sh, val, nrows, ncols, X, Y, accumulate, st, nvec);
 }
 
 template <typename T>
@@ -620,7 +640,8 @@ static void launch_transpose(int64_t rows, int64_t cols, const T* in, T* out, cu
 template <typename T>
 void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_) {
     const int64_t NA = s->a.N0, NB = s->b.N0, nd = NA * NB;
-    g_opposite_max_ctas = max_ctas;
+    g_opposite_max_ctas = max_ctas > 0 ? max_ctas : (opposite_persistent ? sm_count() : 0);
+    g_spmm_narrow = spmm_narrow;
     const T* valb = nullptr;
     const T* vala = nullptr;
     const T* Vt = nullptr;

@@ -33,6 +33,10 @@ struct SigmaBuilder {
     size_t memory = size_t(1) << 30;
     int precision = kFP64;
     int max_ctas = 0; // cap on the opposite-spin grid (0 = one CTA per alpha string)
+    // kernel variants picked by the autotuner (same results): opposite-spin grid of one CTA per
+    // SM looping over the alpha strings; same-spin kernel with half the columns per thread
+    bool opposite_persistent = false;
+    int spmm_narrow = 0;
     // FP32 opposite-spin term on the tensor cores (3xTF32, opposite_tc.cu) when the space allows it
     bool use_tc = true;
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter

@@ -70,6 +70,10 @@ int f2g_sigma_set_max_blocks(void* sigma, int max_blocks);
  * if this space supports it (n <= 16 orbitals, na (n - na + 1) <= 72, one sigma row of beta
  * strings in shared memory); otherwise the CUDA-core kernel is used. No reference counterpart. */
 int f2g_sigma_set_tensor_cores(void* sigma, int on, int* available);
+/* Kernel variants with identical results, for the autotuner: which = 0 opposite spin on the tensor
+ * cores (FP32 only), 1 same-spin kernel with half the columns per thread, 2 opposite-spin grid of
+ * one thread block per SM. No reference counterpart. */
+int f2g_sigma_set_variant(void* sigma, int which, int value);
 /* 1 if a tensor-core build gave up waiting for its matrix operations (results invalid). */
 int f2g_sigma_tc_error(void* sigma, int* out);
 /* Hamiltonian(basis, sigma) for nvec vectors of length ndet stored back to back
@@ -83,6 +87,8 @@ int f2g_sigma_term(void* sigma, int term, const double* dev_C, double* dev_sigma
 /* avg_build_time: [total, aabb, aaaa, bbbb] seconds per build (ci_sigma_builder.h:93-102);
  * aaaa includes H0 and H1 alpha, bbbb includes H1 beta. */
 int f2g_sigma_avg_build_time(void* sigma, double* host_out4);
+/* Restart the build-time averages (after tuning or warm-up builds). No reference counterpart. */
+int f2g_sigma_reset_build_times(void* sigma);
 /* Slater-rule energy of every determinant, address order (slater_rules.cc:86-121). */
 int f2g_sigma_det_energies(void* sigma, double* dev_out, void* stream);
 
