@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--nroot", type=int, default=1)
     ap.add_argument("--e-tol", type=float, default=1e-10)
     ap.add_argument("--precisions", default="fp64,mixed", help="davidson mode: which solves to run")
+    ap.add_argument("--maxiter", type=int, default=400, help="davidson mode: iteration limit")
     return ap.parse_args()
 
 
@@ -341,12 +342,14 @@ def run_davidson(a):
         t0 = time.perf_counter()
         sol = CASCISolver(norb=a.norb, na=na, nb=nb, multiplicity=1, nroot=a.nroot, E=ints.E, H=ints.H, V=ints.V,
                           ci_params=CIParams(precision=prec),
-                          davidson_liu_params=DavidsonLiuParams(e_tol=a.e_tol, maxiter=400)).run()
+                          davidson_liu_params=DavidsonLiuParams(e_tol=a.e_tol, maxiter=a.maxiter)).run()
         torch.cuda.synchronize()
         res[prec] = {"seconds_total": time.perf_counter() - t0, "seconds_davidson": sol.timings["davidson"],
                      "seconds_setup": sol.timings.get("startup", 0.0) + sol.timings.get("setup", 0.0),
                      "converged": bool(sol.converged), "phases": sol.phases, "energies": [float(e) for e in sol.evals],
-                     "ncsf": sol.basis_size}
+                     "ncsf": sol.basis_size,
+                     "iterations": sum(p[1] for p in sol.phases if not p[0].endswith("check"))}
+        res[prec]["seconds_per_iteration"] = res[prec]["seconds_davidson"] / max(1, res[prec]["iterations"])
         print(json.dumps({"partial": prec, **res[prec]}), flush=True)  # each precision as soon as it is done
     out.update(res)
     if "fp64" in res and "mixed" in res:

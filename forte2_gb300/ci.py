@@ -49,6 +49,10 @@ class CASCISolver:
     mixed_e_tol: float = 1e-7
     mixed_r_tol: float = 1e-4
     mixed_max_outer: int = 6
+    # subspace of the mixed mode's Davidson (per root; the FP64 mode keeps the reference's
+    # basis_per_root / collapse_per_root): a larger subspace needs fewer FP32 iterations
+    mixed_basis_per_root: int = 12
+    mixed_collapse_per_root: int = 6
     seed: int = 12345
     # graph-captured Davidson iterations: None = automatic (small CSF spaces), True/False = force
     use_graph: bool = None
@@ -196,8 +200,15 @@ class CASCISolver:
             self.E_roots = self.evals
             return self
         if self.eigensolver is None:
+            dl = self.davidson_liu_params
+            if self.ci_params.precision == "mixed":
+                from dataclasses import replace
+
+                bpr = max(dl.basis_per_root, min(self.mixed_basis_per_root, 64 // self.nroot))
+                cpr = max(dl.collapse_per_root, min(self.mixed_collapse_per_root, bpr - 1))
+                dl = replace(dl, basis_per_root=bpr, collapse_per_root=cpr)
             self.eigensolver = DavidsonLiuSolver(size=self.basis_size, nroot=self.nroot,
-                                                 davidson_liu_params=self.davidson_liu_params,
+                                                 davidson_liu_params=dl,
                                                  energy_shift=self.ci_params.energy_shift,
                                                  log_level=self.log_level, seed=self.seed,
                                                  use_graph=self.use_graph)
