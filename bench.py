@@ -172,13 +172,21 @@ def barrier(dist):
 
 
 def max_over_ranks(x, dist):
+    """Largest value over the ranks (the job's time is its slowest replica's)."""
     if dist is None:
         return x
     import torch
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    device = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(units_per_rank, t_local, dist):
+    """Whole-job rate of independent replicas: all ranks' units over the slowest rank's time."""
+    world = dist.get_world_size() if dist is not None else 1
+    return world * units_per_rank / max_over_ranks(t_local, dist)
 
 
 def run_gb300(a):
@@ -220,7 +228,7 @@ def run_gb300(a):
     clk = clocks.stop()
     t_local = ev0.elapsed_time(ev1) / 1e3
     t = max_over_ranks(t_local, dist)
-    value = world * a.steps / t
+    value = replica_rate(a.steps, t_local, dist)
     # per-term averages over warmup + timed builds (CUDA events around each phase)
     tot, t_ab, t_aa, t_bb = sb.avg_build_time()
     f_sp = sparse_flops(a.norb, na, nb)
