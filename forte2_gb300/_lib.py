@@ -52,6 +52,7 @@ def _declare(L):
         "f2g_spin_adapter_destroy": (i32, [vp]),
         "f2g_spin_adapter_info": (i32, [vp, P]),
         "f2g_csf_to_det": (i32, [vp, P, P, i32, vp]),
+        "f2g_sigma_apply_csf": (i32, [vp, vp, P, P, i32, vp]),
         "f2g_det_to_csf": (i32, [vp, P, P, i32, vp]),
         "f2g_hdiag_csf": (i32, [vp, vp, P, vp]),
         "f2g_csf_matrix": (i32, [vp, vp, P, i32, P]),

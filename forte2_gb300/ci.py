@@ -103,21 +103,11 @@ class CASCISolver:
             self.eigensolver.restart()
 
     def _make_sigma_closure(self):
-        torch = _torch()
         sa, sb = self.spin_adapter, self.sigma_builder
-        ndet = self.ndet
-        bufs = {}
 
         def sigma_builder(B, S):
-            m = B.shape[0]
-            if bufs.get("m", 0) < m:
-                bufs["det"] = torch.empty((m, ndet), dtype=torch.float64, device="cuda")
-                bufs["sdet"] = torch.empty((m, ndet), dtype=torch.float64, device="cuda")
-                bufs["m"] = m
-            det, sdet = bufs["det"][:m], bufs["sdet"][:m]
-            sa.csf_C_to_det_C(B, det)
-            sb.Hamiltonian(det, sdet)
-            sa.det_C_to_csf_C(sdet, S)
+            # csf -> det -> H -> det -> csf in one native call (determinant scratch kept there)
+            sb.apply_csf(sa, B, S)
 
         sigma_builder.device_rows = True
         sigma_builder.graph = (sb, sa, None)  # lets the eigensolver capture the same closure in a CUDA graph

@@ -369,6 +369,17 @@ class CISigmaBuilder:
         check(lib().f2g_sigma_term(self.h, idx, basis.data_ptr(), out.data_ptr(), stream_handle()))
         return out
 
+    def apply_csf(self, spin_adapter, basis, sigma):
+        """sigma = P^T H P basis for CSF vectors (device tensors, rows or one vector): the CI
+        driver's sigma closure (ci.py:221-235) in one call; FP32 transforms in FP32 precision."""
+        nvec = 1 if basis.dim() == 1 else basis.shape[0]
+        if basis.shape != sigma.shape or basis.shape[-1] != spin_adapter.ncsf:
+            raise RuntimeError("CSF vectors must be (nvec, ncsf) with matching shapes")
+        if not (basis.is_contiguous() and sigma.is_contiguous()):
+            raise RuntimeError("CSF vectors must be contiguous")
+        check(lib().f2g_sigma_apply_csf(self.h, spin_adapter.h, basis.data_ptr(), sigma.data_ptr(), nvec,
+                                        stream_handle()))
+
     def reset_build_times(self):
         check(lib().f2g_sigma_reset_build_times(self.h))
 

@@ -346,6 +346,23 @@ int f2g_spin_adapter_info(void* h, int64_t* out) {
     });
 }
 
+int f2g_sigma_apply_csf(void* sb, void* sa, const double* csf_in, double* csf_out, int nvec, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        need(sa, "spin adapter");
+        if (nvec < 0)
+            throw Error(2, "nvec must be >= 0");
+        auto* a = static_cast<SpinAdapter*>(sa);
+        if (nvec > 0 && a->ncsf > 0) {
+            need(csf_in, "csf_in");
+            need(csf_out, "csf_out");
+        }
+        if (!a->host_scratch)
+            a->host_scratch = std::make_unique<CsfSigmaScratch>();
+        sigma_csf(*static_cast<SigmaBuilder*>(sb), *a, csf_in, csf_out, nvec, S(stream), *a->host_scratch, false);
+    });
+}
+
 int f2g_csf_to_det(void* h, const double* csf, double* det, int nvec, void* stream) {
     return guard([&] {
         need(h, "spin adapter");

@@ -236,10 +236,17 @@ struct CsfView {
     const int64_t* offN;
     const int* ncsfN;
     const int* ndetN;
+    const float* Of; // FP32 copy of the overlap tables (the FP32 transforms of the mixed mode)
 };
 
-// Vector blockIdx.y of a batch: csf + y * ncsf_stride, det + y * ndet_stride.
-__global__ void k_csf_to_det(int64_t nslot, CsfView v, const double* __restrict__ csf, double* __restrict__ det,
+template <typename T> __device__ __forceinline__ const T* overlaps(const CsfView& v);
+template <> __device__ __forceinline__ const double* overlaps<double>(const CsfView& v) { return v.O; }
+template <> __device__ __forceinline__ const float* overlaps<float>(const CsfView& v) { return v.Of; }
+
+// Vector blockIdx.y of a batch: csf + y * ncsf_stride, det + y * ndet_stride. T = double, or float
+// for the FP32 sigma of the mixed mode.
+template <typename T>
+__global__ void k_csf_to_det(int64_t nslot, CsfView v, const T* __restrict__ csf, T* __restrict__ det,
                              int64_t ncsf_stride, int64_t ndet_stride) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= nslot)
@@ -250,17 +257,17 @@ __global__ void k_csf_to_det(int64_t nslot, CsfView v, const double* __restrict_
     const int N = popc64(v.conf_s[c]);
     const int nd = v.ndetN[N], nc = v.ncsfN[N];
     const int64_t j = t - v.conf_slot[c];
-    const double* O = v.O + v.offN[N] + j;
-    const double* x = csf + v.conf_csf[c];
-    double acc = 0.0;
+    const T* O = overlaps<T>(v) + v.offN[N] + j;
+    const T* x = csf + v.conf_csf[c];
+    T acc = 0;
     for (int i = 0; i < nc; ++i)
         acc += O[(int64_t)i * nd] * x[i];
     const uint32_t e = v.perm[t];
     det[e & 0x7fffffffu] = (e >> 31) ? -acc : acc;
 }
 
-template <bool SQUARE>
-__global__ void k_det_to_csf(int64_t ncsf, CsfView v, const double* __restrict__ det, double* __restrict__ csf,
+template <bool SQUARE, typename T = double>
+__global__ void k_det_to_csf(int64_t ncsf, CsfView v, const T* __restrict__ det, T* __restrict__ csf,
                              int64_t ndet_stride, int64_t ncsf_stride) {
     const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (u >= ncsf)
@@ -271,15 +278,15 @@ __global__ void k_det_to_csf(int64_t ncsf, CsfView v, const double* __restrict__
     const int N = popc64(v.conf_s[c]);
     const int nd = v.ndetN[N];
     const int64_t i = u - v.conf_csf[c];
-    const double* O = v.O + v.offN[N] + i * nd;
+    const T* O = overlaps<T>(v) + v.offN[N] + i * nd;
     const uint32_t* pm = v.perm + v.conf_slot[c];
-    double acc = 0.0;
+    T acc = 0;
     for (int j = 0; j < nd; ++j) {
-        const double o = O[j];
-        if (o == 0.0)
+        const T o = O[j];
+        if (o == T(0))
             continue;
         const uint32_t e = pm[j];
-        const double x = det[e & 0x7fffffffu];
+        const T x = det[e & 0x7fffffffu];
         if (SQUARE)
             acc += o * o * x;
         else
@@ -413,6 +420,12 @@ __global__ void k_csf_matrix(int m, const int64_t* idx, CsfView v, int64_t N0b, 
 
 // ---- host ----------------------------------------------------------------------------------
 
+__global__ void k_convert_d2f(int64_t n, const double* __restrict__ in, float* __restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = (float)in[i];
+}
+
 template <typename T> static void exclusive_scan(const T* in, T* out, int64_t n, cudaStream_t st) {
     size_t bytes = 0;
     F2G_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, st));
@@ -542,7 +555,7 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
 
 static CsfView view_of(const SpinAdapter& a) {
     return CsfView{a.nconf, a.conf_s.get(), a.conf_csf.get(), a.conf_slot.get(), a.perm.get(),
-                   a.O.get(), a.dOff.get(), a.dNcsf.get(), a.dNdet.get()};
+                   a.O.get(), a.dOff.get(), a.dNcsf.get(), a.dNdet.get(), a.O32.get()};
 }
 
 void SpinAdapter::csf_to_det(const double* csf, double* det, cudaStream_t st, int nvec) const {
@@ -554,8 +567,8 @@ void SpinAdapter::csf_to_det(const double* csf, double* det, cudaStream_t st, in
         F2G_CUDA(cudaMemsetAsync(det, 0, (size_t)nvec * s->ndet * sizeof(double), st));
     if (nslot == 0)
         return;
-    k_csf_to_det<<<dim3((unsigned)ceil_div(nslot, 256), (unsigned)nvec), 256, 0, st>>>(nslot, view_of(*this), csf, det,
-                                                                                       ncsf, s->ndet);
+    k_csf_to_det<double><<<dim3((unsigned)ceil_div(nslot, 256), (unsigned)nvec), 256, 0, st>>>(
+        nslot, view_of(*this), csf, det, ncsf, s->ndet);
     F2G_LAUNCH("k_csf_to_det");
 }
 
@@ -567,6 +580,101 @@ void SpinAdapter::det_to_csf(const double* det, double* csf, cudaStream_t st, in
     k_det_to_csf<false><<<dim3((unsigned)ceil_div(ncsf, 256), (unsigned)nvec), 256, 0, st>>>(ncsf, view_of(*this), det,
                                                                                              csf, s->ndet, ncsf);
     F2G_LAUNCH("k_det_to_csf");
+}
+
+// The FP32 transforms (mixed mode): the overlap tables are copied to FP32 once (stream order st).
+void SpinAdapter::ensure_fp32_tables(cudaStream_t st) const {
+    if (O32.get() || offN.back() == 0)
+        return;
+    const int64_t nO = offN.back();
+    O32.reserve((size_t)nO);
+    k_convert_d2f<<<ceil_div(nO, 256), 256, 0, st>>>(nO, O.get(), O32.get());
+    F2G_LAUNCH("k_convert_d2f overlaps");
+}
+
+void SpinAdapter::csf_to_det(const float* csf, float* det, cudaStream_t st, int nvec) const {
+    if (nvec <= 0)
+        return;
+    if (nvec > 65535)
+        throw Error(2, "csf_to_det: at most 65535 vectors per call");
+    ensure_fp32_tables(st);
+    if (!covers_all_dets)
+        F2G_CUDA(cudaMemsetAsync(det, 0, (size_t)nvec * s->ndet * sizeof(float), st));
+    if (nslot == 0)
+        return;
+    k_csf_to_det<float><<<dim3((unsigned)ceil_div(nslot, 256), (unsigned)nvec), 256, 0, st>>>(
+        nslot, view_of(*this), csf, det, ncsf, s->ndet);
+    F2G_LAUNCH("k_csf_to_det<float>");
+}
+
+void SpinAdapter::det_to_csf(const float* det, float* csf, cudaStream_t st, int nvec) const {
+    if (ncsf == 0 || nvec <= 0)
+        return;
+    if (nvec > 65535)
+        throw Error(2, "det_to_csf: at most 65535 vectors per call");
+    ensure_fp32_tables(st);
+    k_det_to_csf<false, float><<<dim3((unsigned)ceil_div(ncsf, 256), (unsigned)nvec), 256, 0, st>>>(
+        ncsf, view_of(*this), det, csf, s->ndet, ncsf);
+    F2G_LAUNCH("k_det_to_csf<float>");
+}
+
+__global__ void k_convert_f2d(int64_t n, const float* __restrict__ in, double* __restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = (double)in[i];
+}
+
+void CsfSigmaScratch::reserve(const SigmaBuilder& sb, const SpinAdapter& sa, int nvec) {
+    const size_t nd = (size_t)std::max<int64_t>(1, sa.s->ndet), nc = (size_t)std::max<int64_t>(1, sa.ncsf);
+    if (sb.precision == kFP64) {
+        det_in.reserve(nvec * nd);
+        det_out.reserve(nvec * nd);
+    } else {
+        f_csf_in.reserve(nvec * nc);
+        f_csf_out.reserve(nvec * nc);
+        f_det_in.reserve(nvec * nd);
+        f_det_out.reserve(nvec * nd);
+    }
+    reserved_vec = std::max<int64_t>(reserved_vec, nvec);
+}
+
+void sigma_csf(SigmaBuilder& sb, const SpinAdapter& sa, const double* in, double* out, int nvec, cudaStream_t st,
+               CsfSigmaScratch& scr, bool graph) {
+    if (sa.s != sb.s)
+        throw Error(2, "sigma_csf: the spin adapter and the sigma builder use different strings");
+    const int64_t nd = sa.s->ndet, nc = sa.ncsf;
+    if (nvec <= 0 || nc == 0)
+        return;
+    if (!graph)
+        sb.check_memory();
+    const int bs = graph ? nvec : sb.batch_size(nvec);
+    if (graph && nvec > scr.reserved_vec)
+        throw Error(2, "sigma_csf: more vectors than the graph scratch holds");
+    for (int v0 = 0; v0 < nvec; v0 += bs) {
+        const int nv = std::min(bs, nvec - v0);
+        if (!graph)
+            scr.reserve(sb, sa, nv);
+        const double* x = in + (int64_t)v0 * nc;
+        double* y = out + (int64_t)v0 * nc;
+        if (sb.precision == kFP64) {
+            sa.csf_to_det(x, scr.det_in.get(), st, nv);
+            if (graph)
+                sb.apply_untimed(scr.det_in.get(), scr.det_out.get(), st, nv);
+            else
+                sb.hamiltonian(scr.det_in.get(), scr.det_out.get(), st, nv);
+            sa.det_to_csf(scr.det_out.get(), y, st, nv);
+        } else {
+            const int64_t tc = (int64_t)nv * nc;
+            k_convert_d2f<<<ceil_div(tc, 256), 256, 0, st>>>(tc, x, scr.f_csf_in.get());
+            F2G_LAUNCH("k_convert_d2f csf");
+            sa.csf_to_det(scr.f_csf_in.get(), scr.f_det_in.get(), st, nv);
+            sb.apply_f32(scr.f_det_in.get(), scr.f_det_out.get(), st, nv, !graph, graph);
+            sa.det_to_csf(scr.f_det_out.get(), scr.f_csf_out.get(), st, nv);
+            k_convert_f2d<<<ceil_div(tc, 256), 256, 0, st>>>(tc, scr.f_csf_out.get(), y);
+            F2G_LAUNCH("k_convert_f2d csf");
+        }
+    }
+    (void)nd;
 }
 
 void SpinAdapter::hdiag(const double* det_energy, double* out, cudaStream_t st) const {

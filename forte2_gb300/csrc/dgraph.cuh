@@ -77,7 +77,8 @@ struct DavGraph {
     const double* hdiag;
 
     DevBuf<DGState> st;
-    DevBuf<double> G, G2, evals, V, norms2, partial, Dp, hist, stage_c, stage_s, det_in, det_out, cA, cB;
+    DevBuf<double> G, G2, evals, V, norms2, partial, Dp, hist, stage_c, stage_s, cA, cB;
+    CsfSigmaScratch scr; // determinant-space scratch of the captured sigma (reserved at capture)
     DGState* host_state = nullptr;
 
     const double *X = nullptr, *D = nullptr, *Mxd = nullptr;
@@ -114,8 +115,6 @@ struct DavGraph {
         hist.reserve((size_t)4 * P.maxiter_cap);
         stage_c.reserve((size_t)R * n);
         stage_s.reserve((size_t)R * n);
-        det_in.reserve((size_t)R * nd);
-        det_out.reserve((size_t)R * nd);
         host_state = PinnedStateSlots::get().take();
     }
 
@@ -154,9 +153,7 @@ struct DavGraph {
         const int mm = P.maxm;
         DGState* S = st.get();
         dg_stage(S, b, ld, R, n, stage_c.get(), s);
-        sa->csf_to_det(stage_c.get(), det_in.get(), s, R);
-        sb->apply_untimed(det_in.get(), det_out.get(), s, R);
-        sa->det_to_csf(det_out.get(), stage_s.get(), s, R);
+        sigma_csf(*sb, *sa, stage_c.get(), stage_s.get(), R, s, scr, true);
         if (kc) {
             dg_dots(S, 4, X, ldx, stage_c.get(), n, n, kc, R, cA.get(), R, s);
             dg_dots(S, 4, D, ldx, stage_c.get(), n, n, kc, R, cB.get(), R, s);
@@ -185,8 +182,12 @@ struct DavGraph {
     void capture() {
         drop();
         sb->prepare_untimed(R);
-        if (sb->precision == kFP32)
+        if (sb->precision == kFP32) {
             sb->ensure_fp32();
+            sa->ensure_fp32_tables(0);
+        }
+        scr.reserve(*sb, *sa, R);
+        F2G_CUDA(cudaStreamSynchronize(0)); // set-up work of the legacy stream done before the capture
         sb->flush_timers();
         std::unique_lock<std::mutex> lock;
         cudaStream_t cap = capture_stream(lock);

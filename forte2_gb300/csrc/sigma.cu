@@ -499,6 +499,32 @@ void SigmaBuilder::prepare_untimed(int nvec) {
     untimed_nvec = nvec;
 }
 
+void SigmaBuilder::apply_f32(const float* C, float* S, cudaStream_t st, int nvec, bool timed, bool graph) {
+    const int64_t nd = s->ndet;
+    if (nd == 0 || nvec <= 0)
+        return;
+    if (!fp32_ready)
+        throw Error(1, "apply_f32: FP32 Hamiltonian copies are not ready (select FP32 precision first)");
+    const size_t tot = (size_t)nvec * nd;
+    float *ct, *tt;
+    if (graph) {
+        if (nvec > untimed_nvec)
+            throw Error(2, "apply_f32: more vectors than prepared");
+        ct = gfCt.get();
+        tt = gfTt.get();
+    } else {
+        ct = fCt.reserve(tot);
+        tt = fTt.reserve(tot);
+    }
+    if (timed)
+        flush_timers();
+    run<float>(C, S, st, 7, timed, nvec, ct, tt);
+    if (timed) {
+        ev_pending = true;
+        ev_nvec = nvec;
+    }
+}
+
 void SigmaBuilder::apply_untimed(const double* C, double* sigma, cudaStream_t st, int nvec) {
     if (s->ndet == 0 || nvec <= 0)
         return;

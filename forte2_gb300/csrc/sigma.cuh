@@ -71,6 +71,9 @@ struct SigmaBuilder {
     // synchronisation, no timers, no allocation (prepare_untimed() allocates the scratch first),
     // so the calls can be captured into a CUDA graph.
     void set_hamiltonian_async(double E, const double* H, const double* V, cudaStream_t st);
+    // FP32 vectors in and out (the mixed mode's CSF-space sigma): timed like hamiltonian, or
+    // untimed on the graph scratch
+    void apply_f32(const float* C, float* S, cudaStream_t st, int nvec, bool timed, bool graph);
     void prepare_untimed(int nvec);
     void apply_untimed(const double* C, double* sigma, cudaStream_t st, int nvec);
     int untimed_nvec = 0;

@@ -102,6 +102,12 @@ int f2g_spin_adapter_info(void* sa, int64_t* out);
 int f2g_csf_to_det(void* sa, const double* dev_csf, double* dev_det, int nvec, void* stream);
 /* det_C_to_csf_C (ci_spin_adapter.cc:69-82) */
 int f2g_det_to_csf(void* sa, const double* dev_det, double* dev_csf, int nvec, void* stream);
+/* sigma in the CSF basis for nvec vectors of length ncsf (the sigma closure of ci.py:221-235 as
+ * one call: csf_C_to_det_C, Hamiltonian, det_C_to_csf_C). In FP32 precision (mixed mode) the two
+ * transforms also run in FP32. Scratch is kept by the spin adapter: calls on one adapter must not
+ * overlap on the GPU. */
+int f2g_sigma_apply_csf(void* sigma, void* sa, const double* dev_csf_in, double* dev_csf_out, int nvec,
+                        void* stream);
 /* form_Hdiag_csf(dets, spin_adapter, false) (ci_sigma_builder.cc:317-370) */
 int f2g_hdiag_csf(void* sigma, void* sa, double* dev_out, void* stream);
 /* Dense <I|H|J> over CSF indices idx[0..m) (slater_rules_csf, ci_sigma_builder.cc:278-315),

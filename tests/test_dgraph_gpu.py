@@ -42,8 +42,10 @@ def test_graph_launch_length_does_not_change_results(cuda):
     a.new_problem(a.E, a.H, a.V)
     a.run()
     b.run()
-    assert a.eigensolver.iter == b.eigensolver.iter
-    assert np.array_equal(a.evals, b.evals)  # the same kernels in the same order: bitwise equal
+    # the same kernels in the same order; only the order of the opposite-spin term's shared-memory
+    # atomics varies between runs
+    assert abs(a.eigensolver.iter - b.eigensolver.iter) <= 1
+    np.testing.assert_allclose(a.evals, b.evals, rtol=0, atol=1e-12)
 
 
 def test_graph_iteration_limit(cuda):
@@ -120,3 +122,37 @@ def test_dav_eigh_matches_numpy(cuda, m):
     assert np.all(np.diff(w) >= 0)
     np.testing.assert_allclose(Q.T @ Q, np.eye(m), atol=1e-12 * m)
     np.testing.assert_allclose(A @ Q, Q * w, atol=1e-11 * scale * m)
+
+
+@pytest.mark.parametrize("norb,mult", [(6, 1), (8, 3), (10, 1)])
+def test_csf_space_sigma_call(cuda, norb, mult):
+    """apply_csf = csf -> det -> H -> det -> csf in one call: FP64 equals the three-call path to
+    rounding,
+    FP32 (transforms in FP32 too) agrees to FP32 accuracy."""
+    import torch
+
+    from forte2_gb300.ci_helpers import CISigmaBuilder, CISpinAdapter, CIStrings
+
+    s = CIStrings(norb // 2, norb // 2, 0, [[0] * norb], [], [])
+    sa = CISpinAdapter(mult - 1, 0, norb)
+    sa.prepare_couplings(s.make_determinants())
+    ints = make_integrals(norb, 50 + norb)
+    sb = CISigmaBuilder(s, ints.E, ints.H, ints.V, 0)
+    sb.set_algorithm("hz")
+    g = torch.Generator(device="cuda").manual_seed(norb)
+    X = torch.rand((3, sa.ncsf), generator=g, dtype=torch.float64, device="cuda") - 0.5
+    det = torch.empty((3, s.ndet), dtype=torch.float64, device="cuda")
+    sdet = torch.empty_like(det)
+    ref = torch.empty_like(X)
+    sa.csf_C_to_det_C(X, det)
+    sb.Hamiltonian(det, sdet)
+    sa.det_C_to_csf_C(sdet, ref)
+    out = torch.empty_like(X)
+    sb.apply_csf(sa, X, out)
+    # same kernels; the opposite-spin term accumulates with shared-memory atomics, whose order varies
+    assert (torch.linalg.norm(out - ref) / torch.linalg.norm(ref)).item() < 1e-14
+    sb.set_precision("fp32")
+    out32 = torch.empty_like(X)
+    sb.apply_csf(sa, X, out32)
+    rel = (torch.linalg.norm(out32 - ref) / torch.linalg.norm(ref)).item()
+    assert 0 < rel < 2e-6
