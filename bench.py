@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--instances", type=int, default=64, help="batched mode: number of instances")
     ap.add_argument("--requests", type=int, default=10000, help="serve mode: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve mode: mean arrivals per second")
+    ap.add_argument("--unbatched-requests", type=int, default=0,
+                    help="serve mode: also serve the first N requests one at a time with a fresh plain "
+                         "solver each (the unbatched plain path) and, for comparison, batched")
     ap.add_argument("--mode", default="sigma", choices=["sigma", "davidson", "batched", "serve"],
                     help="sigma: sigma-builds/s (default); davidson: time to solution, FP64 vs mixed")
     ap.add_argument("--nroot", type=int, default=1)
@@ -409,6 +412,15 @@ def run_serve(a):
     for prec in a.precisions.split(","):
         stats, _, _ = serve(reqs, precision=prec, prewarm=default_prewarm())
         out[prec] = stats
+    if a.unbatched_requests:
+        # the same arrivals served by the unbatched plain path (one solve at a time, new solver per
+        # request, FP64) against continuous batching
+        sub = reqs[: a.unbatched_requests]
+        plain, _, _ = serve(sub, precision="fp64", max_inflight=1, pool=False)
+        batched, _, _ = serve(sub, precision="fp64", prewarm=default_prewarm())
+        keys = ("wall_s", "solves_per_s", "p50_latency_s", "p99_latency_s", "mean_latency_s", "sizes")
+        out["unbatched_vs_batched_fp64"] = {"requests": len(sub), "unbatched": {k: plain[k] for k in keys},
+                                            "batched": {k: batched[k] for k in keys}}
     print(json.dumps(out), flush=True)
 
 
