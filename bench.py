@@ -192,6 +192,18 @@ def replica_rate(units_per_rank, t_local, dist):
     return world * units_per_rank / max_over_ranks(t_local, dist)
 
 
+def opposite_traffic(norb, na, nb):
+    """DRAM bytes of one FP64 opposite-spin launch, scaled from the ncu capture at norb 15, na 7,
+    nb 8 (dram__bytes_read + dram__bytes_write = 4.71 + 0.33 GB) by the gathered C elements
+    N0a * na * N1b * ma * mb (the kernel's reads; the traffic grows with them)."""
+    from math import comb
+
+    def gathered(n, a, b):
+        return comb(n, a) * a * comb(n, b - 1) * (n - a + 1) * (n - b + 1)
+
+    return 5.04e9 * gathered(norb, na, nb) / gathered(15, 7, 8)
+
+
 def run_gb300(a):
     import torch
 
@@ -287,7 +299,10 @@ def run_gb300(a):
             "gpu_launches": 5 * a.steps,
             "roofline": {"bound": "compute", "pipe": "fp64", "kernel": "k_opposite (opposite-spin sigma)",
                          "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                         "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+                         "frac": achieved / FP64_PEAK_TFLOPS, "traffic": opposite_traffic(a.norb, na, nb),
+                         "traffic_source": "dram read+write per gathered C element of the ncu capture at "
+                                           "CAS(15e,15o) (profiles/k_opposite_fp64_cas15.md: 5.04 GB for "
+                                           "2.09e10 elements), times this launch's gathered elements",
                          "peak_source": "measured FP64 DGEMM, profiles/gb300_gemm_peaks.md",
                          "flops_per_launch": f_sp["ab"], "launch_ms": 1e3 * t_ab},
             "terms_ms": {"total": 1e3 * tot, "aabb": 1e3 * t_ab, "aaaa_h1a_h0": 1e3 * t_aa, "bbbb_h1b": 1e3 * t_bb},
