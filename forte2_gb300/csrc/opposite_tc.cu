@@ -16,12 +16,12 @@
 // (round to nearest), and D += A_hi B_hi + A_lo B_hi + A_hi B_lo ("3xTF32"; the dropped lo*lo term
 // is below FP32 rounding).
 //
-// One CTA per SM (persistent over Ja), 256 threads: all threads gather the operand tiles into
+// One CTA per SM (persistent over Ja), 512 threads: all threads gather the operand tiles into
 // shared memory in the canonical K-major no-swizzle layout (8-row x 16-byte core matrices), one
 // thread issues the MMAs into one of two 128-lane x 128-column FP32 accumulators in tensor memory
-// and commits them to an mbarrier, and while they run all 8 warps read the previous tile's
-// accumulator back (warps w and w + 4 share lanes 32 (w % 4) .. +31 and split the s columns) for
-// its scatter. Waits are bounded; a wait that
+// and commits them to an mbarrier, and while they run all 16 warps read the previous tile's
+// accumulator back (warps w, w + 4, w + 8, w + 12 share lanes 32 (w % 4) .. +31 and split the s
+// columns) for its scatter. Waits are bounded; a wait that
 // gives up sets an error flag and the kernel leaves without touching tensor memory again except
 // to release it.
 #include <cstdint>
@@ -32,7 +32,10 @@ namespace f2g {
 
 namespace {
 
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 512;
+constexpr int kRowThreads = kTcThreads / 128;        // threads per beta string in the operand gather
+constexpr int kQuarterWarps = kTcThreads / 128;      // warps sharing one 32-lane quarter of the accumulator
+constexpr int kChunksPerWarp = 8 / kQuarterWarps;    // s columns (16 accumulator columns each) per warp
 constexpr int kTcM = 128;      // beta strings per tile (accumulator lanes)
 constexpr int kTcN = 128;      // 8 values of s x 16 values of r per pass
 constexpr int kTcMaxK = 72;    // padded alpha-excitation count (na * (n - na + 1), n <= 16)
@@ -185,19 +188,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t lbo = 128, sbo = (uint32_t)(kp >> 2) * 128;
 
     // scatter of one finished tile: warp w reads lanes 32 (w % 4) + [0, 32) = beta strings ib0 + that;
-    // warps w and w + 4 take the even and odd s of the pass. The excitation entries are requested
-    // first, then the accumulator columns, then one wait for both, so their latencies overlap.
+    // the warps sharing a lane quarter take every kQuarterWarps-th s of the pass. The excitation
+    // entries are requested first, then the accumulator columns, then one wait for both, so their
+    // latencies overlap.
     auto scatter = [&](int ib0, uint32_t acc, int s0) {
         const int m = (warp & 3) * 32 + lane;
         const int Ib = ib0 + m;
         const bool valid = Ib < N0b;
         const uint64_t mI = valid ? str_b[Ib] : 0;
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        uint4 e4[4][4];
-        bool has[4];
+        uint4 e4[kChunksPerWarp][4];
+        bool has[kChunksPerWarp];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int s = s0 + (warp >> 2) + 2 * i;
+        for (int i = 0; i < kChunksPerWarp; ++i) {
+            const int s = s0 + (warp >> 2) + kQuarterWarps * i;
             has[i] = valid && s < n && (mI >> s & 1);
             if (has[i]) {
                 const int si = popc64(mI & ((uint64_t(1) << s) - 1));
@@ -207,14 +211,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     e4[i][q] = __ldg(src + q);
             }
         }
-        uint32_t v[4][16];
+        uint32_t v[kChunksPerWarp][16];
         __syncwarp();
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-            tmem_ld16(acc + lane_base + (uint32_t)(((warp >> 2) + 2 * i) * 16), v[i]);
+        for (int i = 0; i < kChunksPerWarp; ++i)
+            tmem_ld16(acc + lane_base + (uint32_t)(((warp >> 2) + kQuarterWarps * i) * 16), v[i]);
         tmem_wait_ld();
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < kChunksPerWarp; ++i) {
             if (!has[i])
                 continue;
             const uint32_t e[16] = {e4[i][0].x, e4[i][0].y, e4[i][0].z, e4[i][0].w, e4[i][1].x, e4[i][1].y,
@@ -264,7 +268,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 // groups of 4 consecutive k (one 16-byte row of a core matrix, stored as a float4);
                 // for fixed k a warp reads 32 consecutive floats. All loads are issued first.
                 {
-                    constexpr int kGroups = kTcMaxK / 4 / (kTcThreads / kTcM);
+                    constexpr int kGroups = (kTcMaxK / 4 + kRowThreads - 1) / kRowThreads;
                     const int m = tid & (kTcM - 1);
                     const int Ib = ib0 + m;
                     const int g0 = tid >> 7;
@@ -274,12 +278,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     for (int j = 0; j < kGroups; ++j)
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {
-                            const int kk = 4 * (g0 + j * (kTcThreads / kTcM)) + c;
+                            const int kk = 4 * (g0 + j * kRowThreads) + c;
                             x[j][c] = (kk < K && in) ? __ldg(C + (int64_t)sh.ia[kk] * N0b + Ib) : 0.0f;
                         }
 #pragma unroll
                     for (int j = 0; j < kGroups; ++j) {
-                        const int g = g0 + j * (kTcThreads / kTcM);
+                        const int g = g0 + j * kRowThreads;
                         if (4 * g < kp) {
                             float4 hi, lo;
                             hi.x = tf32_rna(x[j][0]);
