@@ -16,12 +16,12 @@
 // (round to nearest), and D += A_hi B_hi + A_lo B_hi + A_hi B_lo ("3xTF32"; the dropped lo*lo term
 // is below FP32 rounding).
 //
-// One CTA per SM (persistent over Ja), 512 threads: all threads gather the operand tiles into
+// One CTA per SM (persistent over Ja), 1024 threads: all threads gather the operand tiles into
 // shared memory in the canonical K-major no-swizzle layout (8-row x 16-byte core matrices), one
 // thread issues the MMAs into one of two 128-lane x 128-column FP32 accumulators in tensor memory
-// and commits them to an mbarrier, and while they run all 16 warps read the previous tile's
-// accumulator back (warps w, w + 4, w + 8, w + 12 share lanes 32 (w % 4) .. +31 and split the s
-// columns) for its scatter. Waits are bounded; a wait that
+// and commits them to an mbarrier, and while they run all 32 warps read the previous tile's
+// accumulator back (the 8 warps w = q mod 4 share lanes 32 q .. +31 and take one s column block
+// each) for its scatter. Waits are bounded; a wait that
 // gives up sets an error flag and the kernel leaves without touching tensor memory again except
 // to release it.
 #include <cstdint>
@@ -32,7 +32,7 @@ namespace f2g {
 
 namespace {
 
-constexpr int kTcThreads = 512;
+constexpr int kTcThreads = 1024;
 constexpr int kRowThreads = kTcThreads / 128;        // threads per beta string in the operand gather
 constexpr int kQuarterWarps = kTcThreads / 128;      // warps sharing one 32-lane quarter of the accumulator
 constexpr int kChunksPerWarp = 8 / kQuarterWarps;    // s columns (16 accumulator columns each) per warp
