@@ -87,3 +87,25 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(L, "LIB_PATH", str(tmp_path / "nope.so"))
     with pytest.raises(L.CudaLibraryMissing):
         L.lib()
+
+
+def test_new_entry_points_validate_handles_without_gpu(libpath):
+    """The graph, CSF-sigma, variant and Gram-Schmidt entry points reject NULL handles and bad
+    sizes with status 2 before any device work."""
+    import numpy as np
+
+    from forte2_gb300._lib import lib
+
+    L = lib()
+    out = ctypes.c_void_p()
+    thr = np.array([1e-8, 1e-8, 1e-12])
+    assert L.f2g_dgraph_create(None, None, 10, 1, 4, 2, 10, 1, 8, thr.ctypes.data, None, None, None, None, 10, 10,
+                               10, None, ctypes.byref(out)) == 2
+    assert b"NULL" in L.f2g_last_error()
+    assert L.f2g_dgraph_reset(None, 1, 1, None, None, 0, None, 0, 1e-10, 1e-6, 10, 0, 0.0, None) == 2
+    assert L.f2g_dgraph_launch(None, None) == 2
+    assert L.f2g_sigma_apply_csf(None, None, None, None, 1, None) == 2
+    assert L.f2g_sigma_set_variant(None, 0, 1) == 2
+    assert L.f2g_sigma_set_max_blocks(None, 4) == 2
+    assert L.f2g_sigma_set_tensor_cores(None, 1, None) == 2
+    assert L.f2g_dav_gs_append(None, 10, 4, 0, None, 10, 1, 10, 1e-8, 1e-12, 1, 1, None, None) == 2
