@@ -316,7 +316,8 @@ class CASCISolver:
                 A = es._dots_dev(X, B)  # (k, m): <x_i, b_l>
                 Bd = es._dots_dev(D, B)  # (k, m): <d_i, b_l>
                 es._lincomb(D, A, S, 1.0)
-                es._lincomb(X, Bd - Mxd @ A, S, 1.0)
+                # Bd - Mxd A as a broadcast product and sum (tiny; keeps cuBLAS off per-job streams)
+                es._lincomb(X, Bd - (Mxd[:, :, None] * A[None, :, :]).sum(1), S, 1.0)
 
             corrected.device_rows = True
             corrected.graph = (sb, self.spin_adapter, (X, D, Mb, k))

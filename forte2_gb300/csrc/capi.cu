@@ -206,10 +206,7 @@ int f2g_sigma_reset_build_times(void* sb) {
     return guard([&] {
         need(sb, "sigma");
         auto* b = static_cast<SigmaBuilder*>(sb);
-        b->flush_timers();
-        for (double& t : b->t_acc)
-            t = 0.0;
-        b->builds = 0;
+        b->reset_timers();
     });
 }
 
@@ -262,10 +259,7 @@ int f2g_sigma_set_precision(void* sb, int precision) {
         if (precision != kFP64 && precision != kFP32)
             throw Error(2, "precision must be 0 (FP64) or 1 (FP32)");
         if (precision != b->precision) {
-            b->flush_timers();
-            b->builds = 0;
-            for (double& t : b->t_acc)
-                t = 0.0;
+            b->reset_timers(); // averages per precision; no wait for builds still running
             b->precision = precision;
             if (precision == kFP32)
                 b->ensure_fp32();

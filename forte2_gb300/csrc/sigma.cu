@@ -371,8 +371,9 @@ void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V,
 
 SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const double* V_, int ll)
     : s(s_), n(s_->norb), log_level(ll) {
-    for (auto& e : ev)
-        F2G_CUDA(cudaEventCreate(&e));
+    for (auto& slot : ev)
+        for (auto& e : slot)
+            F2G_CUDA(cudaEventCreate(&e));
     tc_err.reserve(1);
     F2G_CUDA(cudaMemsetAsync(tc_err.get(), 0, sizeof(int), 0));
     if (opposite_tc_supported(s))
@@ -389,9 +390,10 @@ int SigmaBuilder::tc_error() const {
 }
 
 SigmaBuilder::~SigmaBuilder() {
-    for (auto& e : ev)
-        if (e)
-            cudaEventDestroy(e);
+    for (auto& slot : ev)
+        for (auto& e : slot)
+            if (e)
+                cudaEventDestroy(e);
 }
 
 void SigmaBuilder::build_string_hamiltonian(int spin, StringHamiltonian& sh, bool with_e0, cudaStream_t st) {
@@ -517,12 +519,10 @@ void SigmaBuilder::apply_f32(const float* C, float* S, cudaStream_t st, int nvec
         tt = fTt.reserve(tot);
     }
     if (timed)
-        flush_timers();
+        timer_begin();
     run<float>(C, S, st, 7, timed, nvec, ct, tt);
-    if (timed) {
-        ev_pending = true;
-        ev_nvec = nvec;
-    }
+    if (timed)
+        timer_end(nvec);
 }
 
 void SigmaBuilder::apply_untimed(const double* C, double* sigma, cudaStream_t st, int nvec) {
@@ -681,7 +681,7 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
         Vt = fV.get();
     }
     if (timed)
-        F2G_CUDA(cudaEventRecord(ev[0], st));
+        F2G_CUDA(cudaEventRecord(cur_ev[0], st));
     // beta same spin: sigma = (Hbb C^T)^T
     if ((mask & 2) && s->nb >= 1) {
         launch_transpose<T>(NA, NB, C, Ct_, st, nvec);
@@ -691,12 +691,12 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
         F2G_CUDA(cudaMemsetAsync(sig, 0, (size_t)nvec * nd * sizeof(T), st));
     }
     if (timed)
-        F2G_CUDA(cudaEventRecord(ev[1], st));
+        F2G_CUDA(cudaEventRecord(cur_ev[1], st));
     // alpha same spin + H0
     if (mask & 1)
         launch_spmm<T>(ha, vala, NA, (int)NB, C, sig, true, st, nvec);
     if (timed)
-        F2G_CUDA(cudaEventRecord(ev[2], st));
+        F2G_CUDA(cudaEventRecord(cur_ev[2], st));
     if (mask & 4) {
         bool done = false;
         if constexpr (sizeof(T) == 4) {
@@ -709,23 +709,65 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
             launch_opposite<T>(s, Vt, C, sig, st, nvec);
     }
     if (timed)
-        F2G_CUDA(cudaEventRecord(ev[3], st));
+        F2G_CUDA(cudaEventRecord(cur_ev[3], st));
 }
 
-void SigmaBuilder::flush_timers() {
-    if (!ev_pending)
-        return;
-    F2G_CUDA(cudaEventSynchronize(ev[3]));
-    float bb = 0, aa = 0, ab = 0;
-    F2G_CUDA(cudaEventElapsedTime(&bb, ev[0], ev[1]));
-    F2G_CUDA(cudaEventElapsedTime(&aa, ev[1], ev[2]));
-    F2G_CUDA(cudaEventElapsedTime(&ab, ev[2], ev[3]));
-    t_acc[0] += (bb + aa + ab) * 1e-3;
-    t_acc[1] += ab * 1e-3;
-    t_acc[2] += aa * 1e-3;
-    t_acc[3] += bb * 1e-3;
-    builds += ev_nvec;
-    ev_pending = false;
+// Harvest finished timed builds, oldest first; with wait, all of them.
+void SigmaBuilder::poll_timers(bool wait) {
+    while (ev_count > 0) {
+        cudaEvent_t* e = ev[ev_head];
+        if (wait) {
+            F2G_CUDA(cudaEventSynchronize(e[3]));
+        } else {
+            const cudaError_t r = cudaEventQuery(e[3]);
+            if (r == cudaErrorNotReady) {
+                if (cudaPeekAtLastError() == cudaErrorNotReady)
+                    (void)cudaGetLastError(); // "not ready" is a status, not an error: do not leave it behind
+                break;
+            }
+            F2G_CUDA(r);
+        }
+        if (ev_gen[ev_head] == timer_gen) {
+            float bb = 0, aa = 0, ab = 0;
+            F2G_CUDA(cudaEventElapsedTime(&bb, e[0], e[1]));
+            F2G_CUDA(cudaEventElapsedTime(&aa, e[1], e[2]));
+            F2G_CUDA(cudaEventElapsedTime(&ab, e[2], e[3]));
+            t_acc[0] += (bb + aa + ab) * 1e-3;
+            t_acc[1] += ab * 1e-3;
+            t_acc[2] += aa * 1e-3;
+            t_acc[3] += bb * 1e-3;
+            builds += ev_nvec[ev_head];
+        }
+        ev_head = (ev_head + 1) % kTimerSlots;
+        --ev_count;
+    }
+}
+
+void SigmaBuilder::flush_timers() { poll_timers(true); }
+
+// The slot for the next timed build; the host waits only if every slot is still pending.
+void SigmaBuilder::timer_begin() {
+    poll_timers(false);
+    if (ev_count == kTimerSlots) {
+        F2G_CUDA(cudaEventSynchronize(ev[ev_head][3]));
+        poll_timers(false);
+    }
+    cur_ev = ev[(ev_head + ev_count) % kTimerSlots];
+}
+
+void SigmaBuilder::timer_end(int nvec) {
+    const int slot = (ev_head + ev_count) % kTimerSlots;
+    ev_nvec[slot] = nvec;
+    ev_gen[slot] = timer_gen;
+    ++ev_count;
+}
+
+// Restart the averages without waiting: builds still pending belong to the old generation.
+void SigmaBuilder::reset_timers() {
+    ++timer_gen;
+    for (double& t : t_acc)
+        t = 0.0;
+    builds = 0;
 }
 
 void SigmaBuilder::avg_build_time(double* out) {
@@ -751,10 +793,9 @@ void SigmaBuilder::hamiltonian(const double* C, double* sigma, cudaStream_t st, 
     const int bs = batch_size(nvec);
     for (int v0 = 0; v0 < nvec; v0 += bs) {
         const int nv = std::min(bs, nvec - v0);
-        flush_timers();
+        timer_begin();
         apply_batch(C + (int64_t)v0 * nd, sigma + (int64_t)v0 * nd, st, nv, true, false);
-        ev_pending = true;
-        ev_nvec = nv;
+        timer_end(nv);
     }
 }
 

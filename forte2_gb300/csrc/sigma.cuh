@@ -54,9 +54,19 @@ struct SigmaBuilder {
     // timing: [total, aabb, aaaa, bbbb] accumulated from CUDA events
     double t_acc[4] = {0, 0, 0, 0};
     int builds = 0;
-    cudaEvent_t ev[5] = {};
-    bool ev_pending = false;
-    int ev_nvec = 1; // vectors covered by the pending events
+    // build timing without host waits: a ring of event sets; finished builds are harvested in
+    // order when they are found complete, and the host waits only when all slots are pending
+    static constexpr int kTimerSlots = 8;
+    cudaEvent_t ev[kTimerSlots][4] = {};
+    int ev_nvec[kTimerSlots] = {}; // vectors covered by a slot's build
+    int ev_gen[kTimerSlots] = {};  // timer generation the slot was recorded in
+    int ev_head = 0, ev_count = 0; // oldest pending slot, number pending
+    int timer_gen = 0;             // bumped by reset_timers(): older pending builds are dropped
+    cudaEvent_t* cur_ev = nullptr; // events of the build being recorded
+    void timer_begin();
+    void timer_end(int nvec);
+    void poll_timers(bool wait);
+    void reset_timers();
 
     SigmaBuilder(CIStrings* s, double E, const double* H, const double* V, int log_level);
     ~SigmaBuilder();

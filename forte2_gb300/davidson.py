@@ -47,6 +47,13 @@ def _ptr(t):
     return t.data_ptr()
 
 
+def to_device(a):
+    """Small host array -> device tensor without a host wait: staged in pinned memory (torch's
+    caching host allocator) and copied in stream order."""
+    torch = _torch()
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).pin_memory().to("cuda", non_blocking=True)
+
+
 def drive(gen):
     """Run a step generator to completion on the current stream; returns its return value."""
     torch = _torch()
@@ -199,7 +206,7 @@ class DavidsonLiuSolver:
         if isinstance(coef, torch.Tensor):
             c = coef.contiguous()
         else:
-            c = torch.as_tensor(np.ascontiguousarray(coef, dtype=np.float64)).to("cuda", non_blocking=False)
+            c = to_device(coef)
         check(lib().f2g_dav_lincomb(_ptr(X), nx, X.stride(0), _ptr(c), ny, _ptr(Y), Y.stride(0), float(beta),
                                     self.size, stream_handle()))
 
@@ -498,8 +505,8 @@ class DavidsonLiuSolver:
             self.lam[:m] = lam
             self.alpha[:m, :m] = alpha
             lamr = lam[:nroot].copy()
-            d_alpha = torch.as_tensor(np.ascontiguousarray(alpha[:, :nroot])).to("cuda")
-            d_lam = torch.as_tensor(lamr).to("cuda")
+            d_alpha = to_device(alpha[:, :nroot])
+            d_lam = to_device(lamr)
             norms2 = torch.empty(nroot, dtype=torch.float64, device="cuda")
             check(lib().f2g_dav_residual(_ptr(self.b), _ptr(self.sigma), m, self.b.stride(0), _ptr(d_alpha),
                                          _ptr(d_lam), nroot, _ptr(self.h_diag), self.size,
