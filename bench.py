@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--unbatched-requests", type=int, default=0,
                     help="serve mode: also serve the first N requests one at a time with a fresh plain "
                          "solver each (the unbatched plain path) and, for comparison, batched")
-    ap.add_argument("--mode", default="sigma", choices=["sigma", "davidson", "batched", "serve"],
+    ap.add_argument("--mode", default="sigma", choices=["sigma", "davidson", "batched", "serve", "rdm"],
                     help="sigma: sigma-builds/s (default); davidson: time to solution, FP64 vs mixed")
     ap.add_argument("--nroot", type=int, default=1)
     ap.add_argument("--e-tol", type=float, default=1e-10)
@@ -384,6 +384,112 @@ def run_davidson(a):
     print(json.dumps(out), flush=True)
 
 
+def rdm_cpu_baseline(norb, na, nb, c, budget_s):
+    """The oracle's spin-free 1- and 2-RDM of one vector on all host cores, bounded sample: the
+    first fraction f of every hole-string loop; t = O + f T, one full set = O + T."""
+    from oracle.port import PortCI, build_port
+
+    build_port()
+    cores = cpu_cores()
+    os.environ["ORACLE_THREADS"] = str(cores)
+    p = PortCI(norb, na, nb)
+
+    def timed(f):
+        p.set_fraction(f)
+        t = time.perf_counter()
+        p.rdm("sf_1rdm", c, c)
+        p.rdm("sf_2rdm", c, c)
+        return time.perf_counter() - t
+
+    f0 = 0.001
+    t0 = timed(f0)
+    f1 = min(1.0, max(4 * f0, f0 * budget_s / max(t0, 1e-3)))
+    t1 = timed(f1)
+    T = max((t1 - t0) / (f1 - f0), 1e-9)
+    O = max(t0 - f0 * T, 0.0)
+    sample = (f"two samples of one CAS({na + nb}e,{norb}o) sf_1rdm + sf_2rdm: the first {f0:.4f} and {f1:.4f} of "
+              f"every hole-string loop ({t0:.1f} s, {t1:.1f} s); full set = fixed {O:.2f} s + {T:.1f} s linear part; "
+              f"{cores} threads")
+    return 1.0 / (O + T), sample, cores
+
+
+def run_rdm(a):
+    """Spin-free 1- and 2-RDM of one CI vector (the CI driver's make_sf_1rdm + make_sf_2rdm,
+    ci.py:655-699) at CAS(n e, n o), FP64, vector resident in HBM; e2e through the host-array API."""
+    import torch
+
+    from forte2_gb300.ci_helpers import CISigmaBuilder, CIStrings
+
+    torch.cuda.set_device(0)
+    n = a.norb
+    na, nb, N0a, N0b, ndet = cas_dims(n, n, 0)
+    ints = make_integrals(n, ISEED if n == NORB else 1000 + n)
+    strings = CIStrings(na, nb, 0, [[0] * n], [], [])
+    sb = CISigmaBuilder(strings, ints.E, ints.H, ints.V, 0)
+    c_host = random_ci_vector(ndet, CSEED)
+    c = torch.from_numpy(c_host).cuda()
+    st = torch.cuda.current_stream()
+
+    def step():
+        sb.sf_1rdm(c, c)
+        sb.sf_2rdm(c, c)
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(a.steps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    # dominant kernel: the mixed-spin 2-RDM (k_rdm_ab + its mirror), timed alone
+    ab_ms = []
+    for _ in range(3):
+        x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        x0.record(st)
+        sb.ab_2rdm(c, c)
+        x1.record(st)
+        torch.cuda.synchronize()
+        ab_ms.append(x0.elapsed_time(x1))
+    clk = clocks.stop()
+    # algorithmic FP64 work of k_rdm_ab with bra = ket: alpha pair entries with u <= x times all
+    # beta pair entries, one multiply-add each
+    from math import comb
+
+    alpha_sym = n * comb(n - 1, na - 1) + n * (n - 1) // 2 * comb(n - 2, na - 1)
+    beta_all = comb(n, nb - 1) * (n - nb + 1) ** 2
+    ab_flop = 2.0 * alpha_sym * beta_all
+    ab_s = statistics.median(ab_ms) / 1e3
+    # end to end through the host-array API (numpy in, numpy out)
+    t = time.perf_counter()
+    for _ in range(a.steps):
+        sb.sf_1rdm(c_host, c_host)
+        sb.sf_2rdm(c_host, c_host)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t) / a.steps
+    out = {"metric": f"CAS({n},{n}) spin-free 1+2-RDM sets/s", "value": 1e3 / ms, "unit": "RDM sets/s",
+           "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"CAS({n}e,{n}o) Ms=0, sf_1rdm + sf_2rdm of one seeded normalised vector "
+                                  f"(bra = ket), {ndet} determinants, vector {ndet * 8 / 2**30:.2f} GiB > L2"},
+           "e2e": {"value": 1.0 / e2e_s, "unit": "RDM sets/s", "h2d_bytes_per_step": 2 * ndet * 8,
+                   "d2h_bytes_per_step": (n * n + n ** 4) * 8},
+           "roofline": {"bound": "compute", "pipe": "fp64", "kernel": "k_rdm_ab (mixed-spin 2-RDM, with its mirror)",
+                        "achieved": ab_flop / ab_s / 1e12,
+                        "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": ab_flop / ab_s / 1e12 / FP64_PEAK_TFLOPS,
+                        "flop_per_launch": ab_flop, "ms": ab_s * 1e3, "traffic": None,
+                        "peak_source": "measured FP64 DGEMM, profiles/gb300_gemm_peaks.md"},
+           "clocks": clk}
+    if not a.no_cpu_baseline:
+        v, sample, cores = rdm_cpu_baseline(n, na, nb, c_host, a.cpu_seconds)
+        out["cpu_baseline"] = {"value": v, "unit": "RDM sets/s", "cores": cores, "kind": "port", "sample": sample}
+    print(json.dumps(out), flush=True)
+
+
 def run_batched(a):
     """64 independent CASCI instances, (8e,8o)-(12e,12o), multiplicities 1/3, 1-4 roots, solved
     concurrently by the step scheduler, against a loop of plain single solves."""
@@ -450,6 +556,8 @@ if __name__ == "__main__":
         run_serve(args)
     elif args.mode == "davidson":
         run_davidson(args)
+    elif args.mode == "rdm":
+        run_rdm(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

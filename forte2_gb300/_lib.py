@@ -48,6 +48,9 @@ def _declare(L):
         "f2g_sigma_term": (i32, [vp, i32, P, P, vp]),
         "f2g_sigma_avg_build_time": (i32, [vp, P]),
         "f2g_sigma_det_energies": (i32, [vp, P, vp]),
+        "f2g_rdm_size": (i64, [i32, i32]),
+        "f2g_sigma_rdm": (i32, [vp, i32, P, P, P, vp]),
+        "f2g_rdm_pair_list": (i32, [i32, i32, i32, P, P, P]),
         "f2g_spin_adapter_create": (i32, [vp, i32, i32, pp]),
         "f2g_spin_adapter_destroy": (i32, [vp]),
         "f2g_spin_adapter_info": (i32, [vp, P]),

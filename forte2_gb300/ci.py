@@ -60,6 +60,8 @@ class CASCISolver:
     sigma_max_blocks: int = 0
     # pick the fastest sigma kernel variants for this shape before solving (forte2_gb300.autotune)
     autotune: bool = False
+    # after the solve, check every root's energy against its RDMs (ci.py:203-204, 323-403)
+    do_test_rdms: bool = False
 
     def __post_init__(self):
         self._ready_event = None
@@ -222,6 +224,8 @@ class CASCISolver:
         self.E_roots = self.evals
         self.executed = True
         self.timings["total"] = time.perf_counter() - t_all
+        if self.do_test_rdms:
+            self._test_rdms()
         return self
 
     def _exact(self):
@@ -363,3 +367,88 @@ class CASCISolver:
 
     def avg_build_time(self):
         return self.sigma_builder.avg_build_time()
+
+    # ---- reduced density matrices of the solved roots (ci.py:476-768) ----------------------------
+
+    def _det_vector(self, root):
+        """Determinant-basis vector of a root, on the device (ci.py's csf_C_to_det_C)."""
+        torch = _torch()
+        v = self.evecs[:, root]
+        if isinstance(v, np.ndarray):
+            v = torch.from_numpy(np.ascontiguousarray(v))
+        v = v.to(device="cuda", dtype=torch.float64).contiguous()
+        det = torch.empty(self.ndet, dtype=torch.float64, device="cuda")
+        self.spin_adapter.csf_C_to_det_C(v, det)
+        return det
+
+    def _rdm_vectors(self, left_root, right_root):
+        L = self._det_vector(left_root)
+        R = L if right_root is None else self._det_vector(right_root)
+        return L, R
+
+    def _rdm(self, kinds, left_root, right_root):
+        L, R = self._rdm_vectors(left_root, right_root)
+        out = [getattr(self.sigma_builder, k)(L, R).cpu().numpy() for k in kinds]
+        return out[0] if len(out) == 1 else tuple(out)
+
+    def make_sd_1rdm(self, left_root: int, right_root: int | None = None):
+        """Spin-dependent 1-RDMs (a, b) between two roots (ci.py:576-599)."""
+        return self._rdm(("a_1rdm", "b_1rdm"), left_root, right_root)
+
+    def make_sd_2rdm(self, left_root: int, right_root: int | None = None):
+        """Spin-dependent 2-RDMs (aa packed, ab, bb packed) between two roots (ci.py:601-625)."""
+        return self._rdm(("aa_2rdm", "ab_2rdm", "bb_2rdm"), left_root, right_root)
+
+    def make_sf_1rdm(self, left_root: int, right_root: int | None = None):
+        return self._rdm(("sf_1rdm",), left_root, right_root)
+
+    def make_sf_2rdm(self, left_root: int, right_root: int | None = None):
+        return self._rdm(("sf_2rdm",), left_root, right_root)
+
+    def make_sf_2cumulant(self, left_root: int, right_root: int | None = None):
+        return self._rdm(("sf_2cumulant",), left_root, right_root)
+
+    make_1rdm = make_sf_1rdm
+    make_2rdm = make_sf_2rdm
+    make_2cumulant = make_sf_2cumulant
+
+    def rdm_energies(self, root):
+        """The root's energy from its RDMs in the three forms the reference checks (ci.py:323-403):
+        packed same-spin, expanded same-spin, spin-free."""
+        n = self.norb
+        g1 = self.make_sf_1rdm(root)
+        aa, ab, bb = self.make_sd_2rdm(root)
+        g2 = self.make_sf_2rdm(root)
+        H, V = np.asarray(self.H), np.asarray(self.V)
+        A = V - np.einsum("ijkl->ijlk", V)
+        i, j = np.tril_indices(n, k=-1)
+        M = A[i[:, None], j[:, None], i[None, :], j[None, :]]
+        e1 = float(np.einsum("ij,ij", g1, H))
+        packed = self.E + e1 + np.einsum("ij,ij", aa, M) + np.einsum("ijkl,ijkl", ab, V) + np.einsum("ij,ij", bb, M)
+        expanded = (self.E + e1 + 0.25 * np.einsum("ijkl,ijkl", packed_tensor4_to_tensor4(aa, n), A)
+                    + np.einsum("ijkl,ijkl", ab, V) + 0.25 * np.einsum("ijkl,ijkl", packed_tensor4_to_tensor4(bb, n), A))
+        spin_free = self.E + e1 + 0.5 * np.einsum("ijkl,ijkl", g2, V)
+        return float(packed), float(expanded), float(spin_free)
+
+    def _test_rdms(self):
+        for root in range(self.nroot):
+            for form, e in zip(("RDMs", "expanded RDMs", "spin-free RDMs"), self.rdm_energies(root)):
+                if not np.isclose(self.evals[root], e, rtol=1e-6, atol=1e-8):
+                    raise AssertionError(f"CI energy {self.evals[root]} Eh does not match {form} energy {e} Eh")
+
+
+def packed_tensor4_to_tensor4(packed, n):
+    """Expand a packed same-spin 2-RDM [pq][rs] (p > q, r > s) to the antisymmetric (n, n, n, n)
+    tensor (the reference's cpp_helpers.packed_tensor4_to_tensor4, used at ci.py:337-341)."""
+    out = np.zeros((n, n, n, n))
+    if n < 2:
+        return out
+    i, j = np.tril_indices(n, k=-1)
+    P = np.asarray(packed).reshape(len(i), len(i))
+    ii, jj = i[:, None], j[:, None]
+    kk, ll = i[None, :], j[None, :]
+    out[ii, jj, kk, ll] = P
+    out[jj, ii, kk, ll] = -P
+    out[ii, jj, ll, kk] = -P
+    out[jj, ii, ll, kk] = P
+    return out

@@ -361,6 +361,64 @@ class CISigmaBuilder:
             raise RuntimeError("vector length does not match the number of determinants")
         check(lib().f2g_sigma_apply_host(self.h, b.ctypes.data, s.ctypes.data, 1))
 
+    # ---- reduced density matrices (ci_sigma_builder_1rdm.cc:9-84, ci_sigma_builder_2rdm.cc:46-282)
+
+    _RDM_KINDS = {"a_1rdm": 0, "b_1rdm": 1, "sf_1rdm": 2, "aa_2rdm": 3, "bb_2rdm": 4, "ab_2rdm": 5,
+                  "sf_2rdm": 6, "sf_2cumulant": 7}
+
+    def _rdm(self, kind, C_left, C_right):
+        """RDM `kind` between the bra C_left and the ket C_right. numpy vectors give a numpy array
+        (the reference's return type); CUDA float64 tensors give a CUDA tensor and stay on the
+        device. Passing the same vector twice selects the symmetric kernels."""
+        torch = _torch()
+        n = self.lists.norb
+        k = self._RDM_KINDS[kind]
+        npair = n * (n - 1) // 2
+        shape = (n, n) if k <= 2 else (npair, npair) if k <= 4 else (n, n, n, n)
+        size = int(lib().f2g_rdm_size(n, k))
+        device = _is_cuda_tensor(C_left)
+        if device:
+            if not _is_cuda_tensor(C_right):
+                raise TypeError("C_left and C_right must both be CUDA tensors or both numpy arrays")
+            L, R = _dev_vec(C_left), _dev_vec(C_right)
+        else:
+            hl = _host_vec(C_left, "C_left")
+            L = torch.from_numpy(np.ascontiguousarray(hl)).cuda()
+            R = L if C_right is C_left else torch.from_numpy(np.ascontiguousarray(_host_vec(C_right, "C_right"))).cuda()
+        if L.numel() != self.lists.ndet or R.numel() != self.lists.ndet:
+            raise RuntimeError("vector length does not match the number of determinants")
+        out = torch.empty(max(size, 1), dtype=torch.float64, device="cuda")
+        check(lib().f2g_sigma_rdm(self.h, k, L.data_ptr(), R.data_ptr(), out.data_ptr(), stream_handle()))
+        res = out[:size].view(shape)
+        return res if device else res.cpu().numpy()
+
+    def a_1rdm(self, C_left, C_right):
+        """gamma[p][q] = <L| a+_p a_q |R>, alpha (ci_sigma_builder_1rdm.cc:9-65)."""
+        return self._rdm("a_1rdm", C_left, C_right)
+
+    def b_1rdm(self, C_left, C_right):
+        return self._rdm("b_1rdm", C_left, C_right)
+
+    def sf_1rdm(self, C_left, C_right):
+        return self._rdm("sf_1rdm", C_left, C_right)
+
+    def aa_2rdm(self, C_left, C_right):
+        """Packed alpha-alpha 2-RDM [pq][rs], p > q, r > s (ci_sigma_builder_2rdm.cc:46-117)."""
+        return self._rdm("aa_2rdm", C_left, C_right)
+
+    def bb_2rdm(self, C_left, C_right):
+        return self._rdm("bb_2rdm", C_left, C_right)
+
+    def ab_2rdm(self, C_left, C_right):
+        """Alpha-beta 2-RDM [u][v][x][y] (ci_sigma_builder_2rdm.cc:119-201)."""
+        return self._rdm("ab_2rdm", C_left, C_right)
+
+    def sf_2rdm(self, C_left, C_right):
+        return self._rdm("sf_2rdm", C_left, C_right)
+
+    def sf_2cumulant(self, C_left, C_right):
+        return self._rdm("sf_2cumulant", C_left, C_right)
+
     def term(self, which, basis):
         """One HZ term alone (device tensors): "h0", "h1_a", "h1_b", "aabb", "aaaa", "bbbb"."""
         torch = _torch()

@@ -10,6 +10,7 @@
 #include "../../include/forte2_gb300.h"
 #include "csf.cuh"
 #include "dgraph.cuh"
+#include "rdm.cuh"
 
 namespace f2g {
 void dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n, double* out,
@@ -315,6 +316,44 @@ int f2g_sigma_det_energies(void* sb, double* out, void* stream) {
     return guard([&] {
         need(sb, "sigma");
         static_cast<SigmaBuilder*>(sb)->det_energies(out, S(stream));
+    });
+}
+
+int64_t f2g_rdm_size(int norb, int kind) {
+    try {
+        return rdm_size(norb, kind);
+    } catch (const Error& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+int f2g_sigma_rdm(void* sb, int kind, const double* CL, const double* CR, double* out, void* stream) {
+    return guard([&] {
+        need(sb, "sigma");
+        compute_rdm(*static_cast<SigmaBuilder*>(sb), kind, CL, CR, out, S(stream));
+    });
+}
+
+int f2g_rdm_pair_list(int norb, int nel, int force_wide, void* entries, uint16_t* seg_pair, int64_t* counts) {
+    return guard([&] {
+        need(counts, "counts");
+        if (norb < 0 || norb > kMaxOrb || nel < 0 || nel > norb)
+            throw Error(2, "RDM pair list: need 0 <= nel <= norb <= 62");
+        PairListHost L;
+        build_pair_list(norb, nel, force_wide != 0, L);
+        counts[0] = L.nseg;
+        counts[1] = L.nentry;
+        counts[2] = L.wide ? 1 : 0;
+        counts[3] = L.N0;
+        if (entries) {
+            if (L.wide)
+                std::memcpy(entries, L.e64.data(), L.e64.size() * sizeof(uint64_t));
+            else
+                std::memcpy(entries, L.e32.data(), L.e32.size() * sizeof(uint32_t));
+        }
+        if (seg_pair)
+            std::memcpy(seg_pair, L.pair.data(), L.pair.size() * sizeof(uint16_t));
     });
 }
 

@@ -661,8 +661,13 @@ static void launch_transpose(int64_t rows, int64_t cols, const T* in, T* out, cu
     F2G_LAUNCH("k_transpose");
 }
 
+void transpose_f64(int64_t rows, int64_t cols, const double* in, double* out, cudaStream_t st) {
+    launch_transpose<double>(rows, cols, in, out, st);
+}
+
 // mask bits: 1 alpha same-spin (+H0 +H1a), 2 beta same-spin (+H1b), 4 opposite spin
 // Ct_, Tt_: transposition scratch of nvec * ndet elements.
+
 template <typename T>
 void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_) {
     const int64_t NA = s->a.N0, NB = s->b.N0, nd = NA * NB;

@@ -10,6 +10,8 @@ namespace f2g {
 
 enum Precision : int { kFP64 = 0, kFP32 = 1 };
 
+struct RdmScratch; // rdm.cuh
+
 // Same-spin string Hamiltonian of one spin: for every string J the list of (I, value) with
 // value = <J| sum_pq h_pq a+_p a_q + sum_{p>r,q>s} <pr||qs> a+_r a+_p a_q a_s |I>, i.e. the
 // reference's H1_hz + H2_hz_same_spin operator restricted to one spin's strings.
@@ -50,6 +52,7 @@ struct SigmaBuilder {
     DevBuf<float> fC, fCt, fTt, fS;
     DevBuf<double> hostC, hostS; // device staging for host-buffer calls
     DevBuf<double> eA, eB, eJ, eDet; // determinant-energy scratch (string energies, exchange rows, energies)
+    std::shared_ptr<RdmScratch> rdm;  // reduced-density-matrix lists and scratch, made on first use
 
     // timing: [total, aabb, aaaa, bbbb] accumulated from CUDA events
     double t_acc[4] = {0, 0, 0, 0};

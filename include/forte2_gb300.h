@@ -92,6 +92,32 @@ int f2g_sigma_reset_build_times(void* sigma);
 /* Slater-rule energy of every determinant, address order (slater_rules.cc:86-121). */
 int f2g_sigma_det_energies(void* sigma, double* dev_out, void* stream);
 
+/* ---- reduced density matrices between two determinant vectors: replaces
+ *      CISigmaBuilder::compute_{a,b,sf}_1rdm (forte2/ci/ci_sigma_builder_1rdm.cc:9-84),
+ *      compute_{aa,bb,ab,sf}_2rdm and compute_sf_2cumulant (ci_sigma_builder_2rdm.cc:46-282);
+ *      bound as a_1rdm ... sf_2cumulant (api/ci_helpers_api.cc:110-131). */
+/* Number of doubles of RDM `kind` for norb orbitals (or -1 for an unknown kind):
+ * 0 a_1rdm, 1 b_1rdm, 2 sf_1rdm: norb^2, [p][q] = <L|a+_p a_q|R>;
+ * 3 aa_2rdm, 4 bb_2rdm: P^2 with P = norb(norb-1)/2, [pq][rs] for p > q, r > s, pair index
+ *   p(p-1)/2 + q, element <L|a+_p a+_q a_s a_r|R> of one spin;
+ * 5 ab_2rdm: norb^4, [u][v][x][y] = <L|a+_u(alpha) a+_v(beta) a_y(beta) a_x(alpha)|R>;
+ * 6 sf_2rdm: norb^4, ab[p][q][r][s] + ab[q][p][s][r] + the antisymmetric expansion of aa + bb;
+ * 7 sf_2cumulant: norb^4, sf_2rdm[p][q][r][s] - G1[p][r] G1[q][s] + G1[p][s] G1[q][r] / 2. */
+int64_t f2g_rdm_size(int norb, int kind);
+/* RDM `kind` between the bra dev_C_left and the ket dev_C_right (device FP64, ndet each; the
+ * same pointer for both selects the symmetric kernels) into dev_out (f2g_rdm_size doubles,
+ * overwritten), ordered on `stream`. */
+int f2g_sigma_rdm(void* sigma, int kind, const double* dev_C_left, const double* dev_C_right, double* dev_out,
+                  void* stream);
+/* Host-side orbital-pair list of one spin (the mixed-spin 2-RDM's work list), for inspection and
+ * tests; no device call. With host_entries == NULL only counts[] is filled:
+ * counts = {segments (multiple of 32), real entries, wide (0/1), padding index N0}.
+ * Layout: entry j of segment g at ((g/32)*64 + j)*32 + g%32; narrow entries (32-bit)
+ * left | right << 15 | negative << 30, wide (64-bit) left | right << 24 | negative << 48;
+ * host_seg_pair[g] = p*norb + q. */
+int f2g_rdm_pair_list(int norb, int nel, int force_wide, void* host_entries, uint16_t* host_seg_pair,
+                      int64_t* host_counts4);
+
 /* ---- spin adapter: replaces CISpinAdapter(twoS, twoMs, norb) + prepare_couplings(dets)
  *      (forte2/determinant/ci_spin_adapter.cc:55-235; binding api/ci_helpers_api.cc:190-200). */
 int f2g_spin_adapter_create(void* strings, int twoS, int twoMs, void** out);

@@ -25,6 +25,8 @@ SOURCES=(
     ci/ci_sigma_builder.cc
     ci/ci_sigma_builder_harrison_zarrabian.cc
     ci/ci_sigma_builder_knowles_handy.cc
+    ci/ci_sigma_builder_1rdm.cc
+    ci/ci_sigma_builder_2rdm.cc
     determinant/slater_rules.cc
     determinant/ci_spin_adapter.cc
 )

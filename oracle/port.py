@@ -67,6 +67,8 @@ def lib():
     L.port_csf_to_det.argtypes = [vp, _f64p, _f64p, C.c_int64]
     L.port_det_to_csf.argtypes = [vp, _f64p, _f64p]
     L.port_hdiag_csf.argtypes = [vp, vp, _f64p]
+    L.port_rdm.restype = C.c_int64
+    L.port_rdm.argtypes = [vp, C.c_int, _f64p, _f64p, _f64p]
     L.oracle_blas_open.argtypes = [C.c_char_p]
     L.oracle_blas_set_threads.argtypes = [C.c_int]
     _lib = L
@@ -153,6 +155,21 @@ class PortCI:
         out = np.zeros(self.ndet)
         lib().port_det_energies(self.h, out)
         return out
+
+    RDM_KINDS = {"a_1rdm": 0, "b_1rdm": 1, "sf_1rdm": 2, "aa_2rdm": 3, "bb_2rdm": 4, "ab_2rdm": 5,
+                 "sf_2rdm": 6, "sf_2cumulant": 7}
+
+    def rdm(self, kind, CL, CR):
+        """Reduced density matrix `kind` between determinant vectors CL (bra) and CR (ket), flat."""
+        n = self.norb
+        npair = n * (n - 1) // 2
+        size = {0: n * n, 1: n * n, 2: n * n, 3: npair * npair, 4: npair * npair}.get(self.RDM_KINDS[kind], n ** 4)
+        out = np.zeros(max(size, 1))
+        got = lib().port_rdm(self.h, self.RDM_KINDS[kind], np.ascontiguousarray(CL, np.float64),
+                             np.ascontiguousarray(CR, np.float64), out)
+        if got < 0:
+            raise ValueError(f"unknown RDM kind {kind}")
+        return out[:got]
 
 
 class PortSpinAdapter:

@@ -16,7 +16,10 @@
 //     CSF diagonal (ci_sigma_builder.cc:317-370);
 //   * the CSF spin adapter (determinant/ci_spin_adapter.cc:23-288): configurations in the order
 //     of first appearance over determinants in address order, genealogical spin couplings,
-//     Clebsch-Gordan overlaps and the creation-order sign; csf<->det transforms.
+//     Clebsch-Gordan overlaps and the creation-order sign; csf<->det transforms;
+//   * reduced density matrices between two determinant vectors: spin-dependent and spin-free
+//     1-RDMs (ci_sigma_builder_1rdm.cc:9-84), same-spin packed and mixed-spin 2-RDMs, the
+//     spin-free 2-RDM and its cumulant (ci_sigma_builder_2rdm.cc:46-282).
 //
 // Work is spread over host threads (ORACLE_THREADS, default: all hardware threads) the way the
 // reference's parallel_for_chunked does (forte2/helpers/parallel.h:140-166).
@@ -569,6 +572,174 @@ struct Port {
     }
 };
 
+
+// ---- reduced density matrices -----------------------------------------------------------------
+//
+// Restated from the reference's RDM builders (forte2/ci/ci_sigma_builder_1rdm.cc:9-84 and
+// ci_sigma_builder_2rdm.cc:46-282) for one CAS block. A determinant vector holds C(Ia, Ib) at
+// Ia * NB + Ib; the spin-s "row" of string I is row I of C for alpha and column I for beta.
+
+// Sum over items [0, n) of per-item contributions into an accumulator of `size` doubles: each
+// host thread fills its own buffer, and the buffers are added in thread order (deterministic).
+template <typename F> std::vector<double> parallel_sum(size_t n, size_t size, F&& f) {
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(num_threads(), n));
+    std::vector<std::vector<double>> part(nt, std::vector<double>(size, 0.0));
+    const size_t block = n ? (n + nt - 1) / nt : 0;
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t) {
+        const size_t b = t * block, e = std::min(n, b + block);
+        if (b < e)
+            th.emplace_back([&f, &part, t, b, e]() { f(b, e, part[t].data()); });
+    }
+    for (auto& x : th)
+        x.join();
+    std::vector<double> out(size, 0.0);
+    for (size_t t = 0; t < nt; ++t)
+        for (size_t i = 0; i < size; ++i)
+            out[i] += part[t][i];
+    return out;
+}
+
+struct RdmPort {
+    const Port& P;
+    const double* CL;
+    const double* CR;
+
+    // bounded timing samples: only the first fraction P.frac of the hole strings contribute
+    size_t items(size_t n) const {
+        if (P.frac >= 1.0 || n == 0)
+            return n;
+        return std::max<size_t>(1, (size_t)std::ceil(P.frac * (double)n));
+    }
+
+    size_t NA() const { return P.A.size(); }
+    size_t NB() const { return P.B.size(); }
+    // <left row I | right row J> over the other spin's strings
+    double dot(int spin, size_t I, size_t J) const {
+        double acc = 0.0;
+        if (spin == 0) {
+            const double* a = CL + I * NB();
+            const double* b = CR + J * NB();
+            for (size_t L = 0; L < NB(); ++L)
+                acc += a[L] * b[L];
+        } else {
+            for (size_t L = 0; L < NA(); ++L)
+                acc += CL[L * NB() + I] * CR[L * NB() + J];
+        }
+        return acc;
+    }
+
+    // gamma[p][q] = <L| a+_p a_q |R> for one spin: every string I of the right vector, every
+    // occupied q and every p empty in I - q (p = q included) gives J = I - q + p with the sign
+    // of a_q on I times the sign of a+_p on I - q (ci_strings_makers.cc:75-110).
+    std::vector<double> one(int spin) const {
+        const int n = P.n;
+        const StringSpace& S = spin == 0 ? P.A : P.B;
+        if (S.k < 1 || n < 1)
+            return std::vector<double>((size_t)n * n, 0.0);
+        return parallel_sum(items(S.size()), (size_t)n * n, [&](size_t b, size_t e, double* g) {
+            for (size_t I = b; I < e; ++I) {
+                const uint64_t mI = S.s[I];
+                for (int q = 0; q < n; ++q) {
+                    if (!(mI >> q & 1))
+                        continue;
+                    const uint64_t mK = mI & ~(uint64_t(1) << q);
+                    for (int p = 0; p < n; ++p) {
+                        if (mK >> p & 1)
+                            continue;
+                        const uint64_t mJ = mK | (uint64_t(1) << p);
+                        const double sign = sgn(parity_below(mI, q) ^ parity_below(mK, p));
+                        g[p * n + q] += sign * dot(spin, S.rank(mJ), I);
+                    }
+                }
+            }
+        });
+    }
+
+    // gamma[pq][rs] (p > q, r > s, pair index p(p-1)/2 + q) = sum over 2-hole strings K of
+    // sign(K; p, q) sign(K; r, s) <row K+p+q | row K+r+s> (ci_sigma_builder_2rdm.cc:46-117).
+    std::vector<double> same_spin(int spin) const {
+        const int n = P.n;
+        const size_t np = n >= 2 ? (size_t)n * (n - 1) / 2 : 0;
+        const auto& L2 = spin == 0 ? P.a2 : P.b2;
+        const StringSpace& S = spin == 0 ? P.A : P.B;
+        if (S.k < 2 || np == 0)
+            return std::vector<double>(np * np, 0.0);
+        return parallel_sum(items(L2.size()), np * np, [&](size_t b, size_t e, double* g) {
+            for (size_t K = b; K < e; ++K) {
+                for (const auto& l : L2[K]) {
+                    const size_t pq = (size_t)l.p * (l.p - 1) / 2 + l.q;
+                    for (const auto& r : L2[K]) {
+                        const size_t rs = (size_t)r.p * (r.p - 1) / 2 + r.q;
+                        g[pq * np + rs] += l.sign * r.sign * dot(spin, l.I, r.I);
+                    }
+                }
+            }
+        });
+    }
+
+    // gamma[u][v][x][y] = sum over 1-hole strings Ka, Kb of
+    // s(Ka,u) s(Kb,v) CL(Ka+u, Kb+v) s(Ka,x) s(Kb,y) CR(Ka+x, Kb+y) (ci_sigma_builder_2rdm.cc:119-201).
+    std::vector<double> mixed() const {
+        const size_t n = P.n, n4 = n * n * n * n;
+        if (P.na < 1 || P.nb < 1 || n < 1)
+            return std::vector<double>(n4, 0.0);
+        const size_t nb = NB();
+        return parallel_sum(items(P.a1.size()), n4, [&](size_t b, size_t e, double* g) {
+            for (size_t Ka = b; Ka < e; ++Ka) {
+                for (const auto& u : P.a1[Ka]) {
+                    for (const auto& x : P.a1[Ka]) {
+                        const double sa = u.sign * x.sign;
+                        const double* rl = CL + (size_t)u.I * nb;
+                        const double* rr = CR + (size_t)x.I * nb;
+                        double* gux = g + (size_t)u.p * n * n * n + (size_t)x.p * n;
+                        for (const auto& Kb : P.b1) {
+                            for (const auto& v : Kb) {
+                                const double lv = sa * v.sign * rl[v.I];
+                                for (const auto& y : Kb)
+                                    gux[(size_t)v.p * n * n + y.p] += lv * y.sign * rr[y.I];
+                            }
+                        }
+                    }
+                }
+            }
+        });
+    }
+
+    // spin-free 2-RDM: ab(p,q,r,s) + ab(q,p,s,r) plus the antisymmetric expansion of aa + bb
+    // (ci_sigma_builder_2rdm.cc:203-250)
+    std::vector<double> spin_free2() const {
+        const size_t n = P.n;
+        std::vector<double> sf(n * n * n * n, 0.0);
+        if (n < 1)
+            return sf;
+        const auto ab = mixed();
+        auto at = [n](size_t p, size_t q, size_t r, size_t s) { return ((p * n + q) * n + r) * n + s; };
+        for (size_t p = 0; p < n; ++p)
+            for (size_t q = 0; q < n; ++q)
+                for (size_t r = 0; r < n; ++r)
+                    for (size_t s = 0; s < n; ++s)
+                        sf[at(p, q, r, s)] = ab[at(p, q, r, s)] + ab[at(q, p, s, r)];
+        if (n < 2)
+            return sf;
+        const size_t np = n * (n - 1) / 2;
+        for (int spin = 0; spin < 2; ++spin) {
+            const auto ss = same_spin(spin);
+            for (size_t p = 1; p < n; ++p)
+                for (size_t q = 0; q < p; ++q)
+                    for (size_t r = 1; r < n; ++r)
+                        for (size_t s = 0; s < r; ++s) {
+                            const double e = ss[(p * (p - 1) / 2 + q) * np + r * (r - 1) / 2 + s];
+                            sf[at(p, q, r, s)] += e;
+                            sf[at(q, p, r, s)] -= e;
+                            sf[at(p, q, s, r)] -= e;
+                            sf[at(q, p, s, r)] += e;
+                        }
+        }
+        return sf;
+    }
+};
+
 } // namespace
 
 extern "C" {
@@ -756,6 +927,50 @@ void port_hdiag_csf(void* h, void* s, double* out) {
             out[i] = acc;
         }
     });
+}
+
+/// Reduced density matrices between two determinant vectors (kinds as in the GPU library:
+/// 0 a_1rdm, 1 b_1rdm, 2 sf_1rdm, 3 aa_2rdm, 4 bb_2rdm, 5 ab_2rdm, 6 sf_2rdm, 7 sf_2cumulant).
+/// Returns the number of doubles written to out, or -1 for an unknown kind.
+int64_t port_rdm(void* h, int kind, const double* CL, const double* CR, double* out) {
+    const auto& P = *static_cast<Port*>(h);
+    RdmPort R{P, CL, CR};
+    const size_t n = P.n;
+    std::vector<double> r;
+    switch (kind) {
+    case 0: r = R.one(0); break;
+    case 1: r = R.one(1); break;
+    case 2: {
+        r = R.one(0);
+        const auto b = R.one(1);
+        for (size_t i = 0; i < r.size(); ++i)
+            r[i] += b[i];
+        break;
+    }
+    case 3: r = R.same_spin(0); break;
+    case 4: r = R.same_spin(1); break;
+    case 5: r = R.mixed(); break;
+    case 6: r = R.spin_free2(); break;
+    case 7: {
+        // L2[p,q,r,s] = G2[p,q,r,s] - G1[p,r] G1[q,s] + G1[p,s] G1[q,r] / 2
+        // (ci_sigma_builder_2rdm.cc:252-278)
+        r = R.spin_free2();
+        auto g1 = R.one(0);
+        const auto b = R.one(1);
+        for (size_t i = 0; i < g1.size(); ++i)
+            g1[i] += b[i];
+        for (size_t p = 0; p < n; ++p)
+            for (size_t q = 0; q < n; ++q)
+                for (size_t a = 0; a < n; ++a)
+                    for (size_t s = 0; s < n; ++s)
+                        r[((p * n + q) * n + a) * n + s] +=
+                            -g1[p * n + a] * g1[q * n + s] + 0.5 * g1[p * n + s] * g1[q * n + a];
+        break;
+    }
+    default: return -1;
+    }
+    std::copy(r.begin(), r.end(), out);
+    return (int64_t)r.size();
 }
 
 } // extern "C"

@@ -413,4 +413,35 @@ double ref_slater_rules_csf(void* hsig, void* hsa, void* hs, int64_t I, int64_t 
     return r->sb->slater_rules_csf(s->dets, *sa, I, J);
 }
 
+
+/// Reduced density matrices of the reference (ci_sigma_builder_1rdm.cc:9-84,
+/// ci_sigma_builder_2rdm.cc:46-282) between two determinant vectors, copied into `out`:
+/// kind 0 a_1rdm, 1 b_1rdm, 2 sf_1rdm (n*n); 3 aa_2rdm, 4 bb_2rdm (P*P, P = n(n-1)/2);
+/// 5 ab_2rdm, 6 sf_2rdm, 7 sf_2cumulant (n^4). Returns the number of elements written.
+int64_t ref_rdm(void* h, int kind, double* CL, double* CR, int64_t ndet, double* out) {
+    try {
+        auto* sb = static_cast<RefSigma*>(h)->sb;
+        auto l = vec_view(CL, ndet), r = vec_view(CR, ndet);
+        auto copy = [&](const auto& a) {
+            const size_t n = a.size();
+            std::memcpy(out, a.data(), n * sizeof(double));
+            return (int64_t)n;
+        };
+        switch (kind) {
+        case 0: return copy(sb->compute_a_1rdm(l, r));
+        case 1: return copy(sb->compute_b_1rdm(l, r));
+        case 2: return copy(sb->compute_sf_1rdm(l, r));
+        case 3: return copy(sb->compute_aa_2rdm(l, r));
+        case 4: return copy(sb->compute_bb_2rdm(l, r));
+        case 5: return copy(sb->compute_ab_2rdm(l, r));
+        case 6: return copy(sb->compute_sf_2rdm(l, r));
+        case 7: return copy(sb->compute_sf_2cumulant(l, r));
+        default: throw std::runtime_error("unknown RDM kind");
+        }
+    } catch (const std::exception& e) {
+        fail(e, 1);
+    }
+    return -1;
+}
+
 } // extern "C"

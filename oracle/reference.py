@@ -81,6 +81,8 @@ def lib():
     L.ref_hdiag_csf.argtypes = [vp, vp, vp, C.c_int, _f64p, C.c_int64]
     L.ref_slater_rules_csf.restype = C.c_double
     L.ref_slater_rules_csf.argtypes = [vp, vp, vp, C.c_int64, C.c_int64]
+    L.ref_rdm.restype = C.c_int64
+    L.ref_rdm.argtypes = [vp, C.c_int, _f64p, _f64p, C.c_int64, _f64p]
     L.oracle_blas_open.argtypes = [C.c_char_p]
     L.oracle_blas_set_threads.argtypes = [C.c_int]
     _lib = L
@@ -214,6 +216,21 @@ class RefSigmaBuilder:
         out = np.zeros(self.strings.ndet)
         lib().ref_det_energies(self.h, self.strings.h, out)
         return out
+
+    RDM_KINDS = {"a_1rdm": 0, "b_1rdm": 1, "sf_1rdm": 2, "aa_2rdm": 3, "bb_2rdm": 4, "ab_2rdm": 5,
+                 "sf_2rdm": 6, "sf_2cumulant": 7}
+
+    def rdm(self, kind, CL, CR):
+        """The reference's compute_<kind> (ci_sigma_builder_1rdm.cc, _2rdm.cc) as a flat array."""
+        n = self.strings.norb
+        size = {0: n * n, 1: n * n, 2: n * n, 3: (n * (n - 1) // 2) ** 2, 4: (n * (n - 1) // 2) ** 2}.get(
+            self.RDM_KINDS[kind], n ** 4)
+        out = np.zeros(max(size, 1))
+        got = lib().ref_rdm(self.h, self.RDM_KINDS[kind], np.ascontiguousarray(CL, dtype=np.float64),
+                            np.ascontiguousarray(CR, dtype=np.float64), CL.shape[0], out)
+        if got < 0:
+            _raise(1)
+        return out[:got]
 
     def form_Hdiag_csf(self, spin_adapter, full=False):
         out = np.zeros(spin_adapter.ncsf)

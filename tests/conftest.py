@@ -32,6 +32,11 @@ def golden_sigma():
 
 
 @pytest.fixture(scope="session")
+def golden_rdm():
+    return np.load(os.path.join(GOLDEN, "rdm.npz"))
+
+
+@pytest.fixture(scope="session")
 def golden_checksums():
     with open(os.path.join(GOLDEN, "sigma_checksums.json")) as f:
         return json.load(f)

@@ -5,8 +5,8 @@ Run in a checkout that has the reference sources (default /root/reference):
     oracle/build_ref.sh /root/reference
     python tests/golden/make_golden.py [--big]
 
-Everything here comes from the reference's own code: its C++ CIStrings / CISigmaBuilder /
-CISpinAdapter compiled unmodified by oracle/build_ref.sh, and its helpers/davidsonliu.py
+Everything here comes from the reference's own code: its C++ CIStrings / CISigmaBuilder
+(sigma and RDM builders) / CISpinAdapter compiled unmodified by oracle/build_ref.sh, and its helpers/davidsonliu.py
 driven exactly as forte2/ci/ci.py:245-303 drives it (CSF basis, Hdiag from form_Hdiag_csf,
 guess vectors from ci.py:411-452, sigma closure from ci.py:221-235). Integrals are the seeded
 synthetic recipe of forte2_gb300.synthetic. The fixtures are small .npz files; large cases are
@@ -44,6 +44,12 @@ SIGMA_CASES = [(1, 1, 2, 11, 101), (2, 2, 4, 12, 102), (3, 3, 6, 13, 103), (2, 3
                (4, 4, 8, 19, 109), (5, 5, 10, 1000, 110), (4, 5, 9, 21, 111)]
 SIGMA_CHECKSUM_CASES = [(6, 6, 12, 22, 112), (7, 7, 14, 2000, 113)]
 SIGMA_CHECKSUM_BIG = [(8, 8, 16, 3000, 114)]
+
+# (na, nb, norb, bra seed, ket seed) for the reduced-density-matrix fixtures: every RDM kind of
+# the reference between two different vectors and of one vector with itself.
+RDM_CASES = [(1, 1, 1, 201, 202), (1, 1, 2, 203, 204), (2, 2, 4, 205, 206), (3, 3, 6, 207, 208),
+             (2, 3, 6, 209, 210), (3, 1, 6, 211, 212), (1, 4, 6, 213, 214), (4, 0, 6, 215, 216),
+             (0, 3, 5, 217, 218), (3, 2, 7, 219, 220), (4, 4, 8, 221, 222)]
 
 # (na, nb, norb, multiplicity, twice_ms, nroot, integral seed, e_tol, maxiter). The CAS(10,10)
 # four-root case does not converge within the reference's default 100 iterations on these
@@ -149,6 +155,24 @@ def gen_sigma(out):
             data[f"{tag}_slater_csf"] = np.array(
                 [[sb.slater_rules_csf(sa, i, j) for j in range(m)] for i in range(m)])
     np.savez_compressed(os.path.join(out, "sigma.npz"), **data)
+
+
+def gen_rdm(out):
+    data = {}
+    for na, nb, n, sl, sr in RDM_CASES:
+        ints = make_integrals(n, sl)
+        s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+        sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
+        cl = random_ci_vector(s.ndet, sl)
+        cr = random_ci_vector(s.ndet, sr)
+        key = f"{na}_{nb}_{n}"
+        data[f"{key}_seeds"] = np.array([sl, sr])
+        data[f"{key}_CL_sha"] = np.frombuffer(sha(cl).encode(), dtype=np.uint8)
+        data[f"{key}_CR_sha"] = np.frombuffer(sha(cr).encode(), dtype=np.uint8)
+        for kind in sb.RDM_KINDS:
+            data[f"{key}_{kind}_LR"] = sb.rdm(kind, cl, cr)
+            data[f"{key}_{kind}_LL"] = sb.rdm(kind, cl, cl)
+    np.savez_compressed(os.path.join(out, "rdm.npz"), **data)
 
 
 def checksums(sig, ndet, seed):
@@ -264,7 +288,7 @@ def main():
     ref.open_blas(threads=os.cpu_count())
     steps = {"lists": lambda: gen_lists(HERE), "sigma": lambda: gen_sigma(HERE),
              "checksums": lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_CASES, "sigma_checksums.json"),
-             "davidson": lambda: gen_davidson(HERE, a.reference)}
+             "davidson": lambda: gen_davidson(HERE, a.reference), "rdm": lambda: gen_rdm(HERE)}
     if a.big:
         steps["big"] = lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_BIG, "sigma_checksums_16.json")
     for name, f in steps.items():

@@ -154,3 +154,40 @@ def test_reference_oracle_matches_port_when_built(golden_sigma):
     out = np.zeros(s.ndet)
     sb.Hamiltonian(c, out)
     np.testing.assert_allclose(out, golden_sigma["3_3_6_sigma"], rtol=0, atol=1e-13)
+
+
+RDM_KINDS = ("a_1rdm", "b_1rdm", "sf_1rdm", "aa_2rdm", "bb_2rdm", "ab_2rdm", "sf_2rdm", "sf_2cumulant")
+
+
+def test_port_rdms_match_reference(golden_rdm):
+    """Every RDM kind of the restatement equals the reference's (ci_sigma_builder_1rdm.cc,
+    ci_sigma_builder_2rdm.cc) for a transition pair and for one vector with itself."""
+    for na, nb, n in list_cases(golden_rdm):
+        key = f"{na}_{nb}_{n}"
+        sl, sr = golden_rdm[f"{key}_seeds"]
+        p = PortCI(n, na, nb)
+        cl = random_ci_vector(p.ndet, int(sl))
+        cr = random_ci_vector(p.ndet, int(sr))
+        assert sha(cl) == bytes(golden_rdm[f"{key}_CL_sha"]).decode()
+        assert sha(cr) == bytes(golden_rdm[f"{key}_CR_sha"]).decode()
+        for kind in RDM_KINDS:
+            for tag, b in (("LR", cr), ("LL", cl)):
+                ref = golden_rdm[f"{key}_{kind}_{tag}"]
+                got = p.rdm(kind, cl, b)
+                assert got.shape == ref.shape, (key, kind)
+                scale = max(1.0, float(np.abs(ref).max())) if ref.size else 1.0
+                assert np.abs(got - ref).max(initial=0.0) <= 1e-13 * scale, (key, kind, tag)
+
+
+def test_port_rdm_energy_identity():
+    """<C|H|C> from the oracle's sigma equals the energy from its spin-free RDMs."""
+    for na, nb, n, seed in ((3, 3, 6, 5), (4, 3, 8, 6), (5, 5, 10, 7)):
+        ints = make_integrals(n, seed)
+        p = PortCI(n, na, nb)
+        p.set_hamiltonian(ints.E, ints.H, ints.V)
+        c = random_ci_vector(p.ndet, seed + 100)
+        e_sigma = float(c @ p.sigma(c))
+        g1 = p.rdm("sf_1rdm", c, c).reshape(n, n)
+        g2 = p.rdm("sf_2rdm", c, c).reshape(n, n, n, n)
+        e_rdm = ints.E + np.einsum("ij,ij", g1, ints.H) + 0.5 * np.einsum("ijkl,ijkl", g2, ints.V)
+        assert abs(e_sigma - e_rdm) < 1e-11 * max(1.0, abs(e_sigma)), (n, e_sigma, e_rdm)
