@@ -130,13 +130,14 @@ def test_casci_rdm_self_check(cuda, mult):
     from forte2_gb300.ci import CASCISolver
     from forte2_gb300.params import DavidsonLiuParams
 
+    # the CAS(8,8) cases of the reference Davidson fixtures (singlet 4 roots, triplet 3 roots)
     n = 8
-    ints = make_integrals(n, 35 + mult)
-    solver = CASCISolver(norb=n, na=4, nb=4, multiplicity=mult, nroot=3, E=ints.E, H=ints.H, V=ints.V,
-                         davidson_liu_params=DavidsonLiuParams(e_tol=1e-12, r_tol=1e-8, maxiter=400),
-                         do_test_rdms=True).run()
+    seed, nroot = (35, 4) if mult == 1 else (36, 3)
+    ints = make_integrals(n, seed)
+    solver = CASCISolver(norb=n, na=4, nb=4, multiplicity=mult, nroot=nroot, E=ints.E, H=ints.H, V=ints.V,
+                         davidson_liu_params=DavidsonLiuParams(e_tol=1e-12, maxiter=1000), do_test_rdms=True).run()
     assert solver.converged
-    for root in range(3):
+    for root in range(nroot):
         for e in solver.rdm_energies(root):
             assert abs(e - solver.evals[root]) < 1e-9
     a, b = solver.make_sd_1rdm(0)
