@@ -341,7 +341,7 @@ int f2g_rdm_pair_list(int norb, int nel, int force_wide, void* entries, uint16_t
         if (norb < 0 || norb > kMaxOrb || nel < 0 || nel > norb)
             throw Error(2, "RDM pair list: need 0 <= nel <= norb <= 62");
         PairListHost L;
-        build_pair_list(norb, nel, force_wide != 0, L);
+        build_pair_list(norb, nel, force_wide != 0, kRdmSeg, L);
         counts[0] = L.nseg;
         counts[1] = L.nentry;
         counts[2] = L.wide ? 1 : 0;

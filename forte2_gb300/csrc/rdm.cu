@@ -55,10 +55,11 @@ int64_t rdm_size(int n, int kind) {
 
 // ---- orbital-pair lists (host) ---------------------------------------------------------------
 
-void build_pair_list(int n, int k, bool force_wide, PairListHost& L) {
+void build_pair_list(int n, int k, bool force_wide, int seg, PairListHost& L) {
     L = PairListHost{};
     L.n = n;
     L.k = k;
+    L.seg = seg;
     L.N0 = (int64_t)host_binom(n, k);
     if (k < 1 || n < 1)
         return;
@@ -75,18 +76,18 @@ void build_pair_list(int n, int k, bool force_wide, PairListHost& L) {
         for (int q = 0; q < n; ++q) {
             len[p * n + q] = (int64_t)(p == q ? host_binom(n - 1, k - 1) : host_binom(n - 2, k - 1));
             start[p * n + q] = nseg;
-            nseg += (len[p * n + q] + kRdmSeg - 1) / kRdmSeg;
+            nseg += (len[p * n + q] + seg - 1) / seg;
         }
     nseg = (nseg + 31) / 32 * 32;
     L.nseg = nseg;
     L.pair.assign(nseg, 0);
     for (int pq = 0; pq < n * n; ++pq) {
-        const int64_t ns = (len[pq] + kRdmSeg - 1) / kRdmSeg;
+        const int64_t ns = (len[pq] + seg - 1) / seg;
         for (int64_t g = 0; g < ns; ++g)
             L.pair[start[pq] + g] = (uint16_t)pq;
     }
     const uint64_t pad = (uint64_t)L.N0;
-    const size_t total = (size_t)nseg * kRdmSeg;
+    const size_t total = (size_t)nseg * seg;
     if (L.wide)
         L.e64.assign(total, pad | (pad << 24));
     else
@@ -111,8 +112,8 @@ void build_pair_list(int n, int k, bool force_wide, PairListHost& L) {
                 const int64_t idx = cur[pq]++;
                 if (idx >= len[pq])
                     throw Error(1, "RDM pair list: list longer than its binomial count");
-                const int64_t g = start[pq] + idx / kRdmSeg, j = idx % kRdmSeg;
-                const size_t at = (size_t)(((g / 32) * kRdmSeg + j) * 32 + g % 32);
+                const int64_t g = start[pq] + idx / seg, j = idx % seg;
+                const size_t at = (size_t)(((g / 32) * seg + j) * 32 + g % 32);
                 const uint64_t neg = (uint64_t)(sgn[p] ^ sgn[q]);
                 if (L.wide)
                     L.e64[at] = (uint64_t)addr[p] | ((uint64_t)addr[q] << 24) | (neg << 48);
@@ -312,32 +313,32 @@ __device__ __forceinline__ double row_at(const double* r, int64_t i, int64_t NB)
     return i < NB ? __ldg(r + i) : 0.0;
 }
 
-// gamma[u][v][x][y] += sum over the segments of the alpha pair list A given to this block
-// (see the file comment). Shared memory: bra row, ket row (NB + 1 each when SM) and the
-// n x n slab of the current alpha pair.
+// gamma[u][v][x][y] += sum over the alpha segments of the work list given to this block (all
+// segments, or those with u <= x when bra = ket; see the file comment). Shared memory: bra row,
+// ket row (NB + 1 each when SM) and the n x n slab of the current alpha pair.
 template <typename EB, bool SM>
 __global__ void __launch_bounds__(1024, 1)
-    k_rdm_ab(int n, int64_t nsega, const uint64_t* __restrict__ ea, const uint16_t* __restrict__ pa, int64_t nsegb,
-             const EB* __restrict__ eb, const uint16_t* __restrict__ pb, int64_t NA, int64_t NB,
-             const double* __restrict__ CL, const double* __restrict__ CR, int sym, double* __restrict__ out) {
+    k_rdm_ab(int n, int64_t nwork, const int32_t* __restrict__ work, const uint64_t* __restrict__ ea,
+             const uint16_t* __restrict__ pa, int64_t nsegb, const EB* __restrict__ eb, const uint16_t* __restrict__ pb,
+             int64_t NA, int64_t NB, const double* __restrict__ CL, const double* __restrict__ CR,
+             double* __restrict__ out) {
     extern __shared__ double sm[];
     double* g = sm;                           // n * n slab
     double* a = g + n * n;                    // bra row (SM)
     double* b = a + (SM ? NB + 1 : 0);        // ket row (SM)
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31;
     const int64_t n2 = (int64_t)n * n;
-    for (int64_t sa = blockIdx.x; sa < nsega; sa += gridDim.x) {
+    for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const int64_t sa = work[w];
         const int pair_a = pa[sa];
         const int u = pair_a / n, x = pair_a - u * n;
-        if (sym && u > x)
-            continue; // the mirror fills it (same decision in every thread)
         __syncthreads(); // the previous segment's slab has been flushed
         for (int i = tid; i < n2; i += T)
             g[i] = 0.0;
-        for (int e = 0; e < kRdmSeg; ++e) {
+        for (int e = 0; e < kRdmSegA; ++e) {
             int64_t IL, IR;
             uint32_t nega;
-            pair_entry(ea[((sa >> 5) * kRdmSeg + e) * 32 + (sa & 31)], IL, IR, nega);
+            pair_entry(ea[((sa >> 5) * kRdmSegA + e) * 32 + (sa & 31)], IL, IR, nega);
             if (IL >= NA)
                 continue; // padding (same entry in every thread)
             const double* rl = CL + IL * NB;
@@ -431,16 +432,36 @@ static void ensure_pair_lists(SigmaBuilder& sb, RdmScratch& R, cudaStream_t st) 
         return;
     const CIStrings& s = *sb.s;
     PairListHost A, B;
-    build_pair_list(s.norb, s.na, true, A);
-    build_pair_list(s.norb, s.nb, false, B);
+    build_pair_list(s.norb, s.na, true, kRdmSegA, A);
+    build_pair_list(s.norb, s.nb, false, kRdmSeg, B);
     R.nsega = A.nseg;
     R.nsegb = B.nseg;
     R.wideb = B.wide;
+    std::vector<int32_t> all, sym;
     if (A.nseg) {
         R.ea.reserve(A.e64.size());
         R.pa.reserve(A.pair.size());
         F2G_CUDA(cudaMemcpyAsync(R.ea.get(), A.e64.data(), A.e64.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
         F2G_CUDA(cudaMemcpyAsync(R.pa.get(), A.pair.data(), A.pair.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
+        // work lists: segments whose first entry is real (padding segments hold none)
+        const uint64_t pad = (uint64_t)A.N0;
+        for (int64_t g = 0; g < A.nseg; ++g) {
+            const uint64_t first = A.e64[(size_t)(((g / 32) * A.seg) * 32 + g % 32)] & 0xffffffull;
+            if (first == pad)
+                continue;
+            all.push_back((int32_t)g);
+            const int u = A.pair[g] / s.norb, x = A.pair[g] % s.norb;
+            if (u <= x)
+                sym.push_back((int32_t)g);
+        }
+        R.nwork_all = (int64_t)all.size();
+        R.nwork_sym = (int64_t)sym.size();
+        R.work_all.reserve(all.size());
+        R.work_sym.reserve(sym.size());
+        if (!all.empty())
+            F2G_CUDA(cudaMemcpyAsync(R.work_all.get(), all.data(), all.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        if (!sym.empty())
+            F2G_CUDA(cudaMemcpyAsync(R.work_sym.get(), sym.data(), sym.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     }
     if (B.nseg) {
         if (B.wide) {
@@ -462,10 +483,14 @@ static void ensure_pair_lists(SigmaBuilder& sb, RdmScratch& R, cudaStream_t st) 
 template <typename EB, bool SM>
 static void launch_ab(int n, RdmScratch& R, const EB* eb, int64_t NA, int64_t NB, const double* CL, const double* CR,
                       bool sym, double* out, cudaStream_t st, size_t smem) {
+    const int64_t nwork = sym ? R.nwork_sym : R.nwork_all;
+    if (nwork == 0)
+        return;
+    const int32_t* work = sym ? R.work_sym.get() : R.work_all.get();
     F2G_CUDA(cudaFuncSetAttribute(k_rdm_ab<EB, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(R.nsega, device_sms()));
-    k_rdm_ab<EB, SM><<<grid, 1024, smem, st>>>(n, R.nsega, R.ea.get(), R.pa.get(), R.nsegb, eb, R.pb.get(), NA, NB,
-                                                CL, CR, sym ? 1 : 0, out);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(nwork, device_sms()));
+    k_rdm_ab<EB, SM><<<grid, 1024, smem, st>>>(n, nwork, work, R.ea.get(), R.pa.get(), R.nsegb, eb, R.pb.get(), NA,
+                                                NB, CL, CR, out);
     F2G_LAUNCH("k_rdm_ab");
 }
 

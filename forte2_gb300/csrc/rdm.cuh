@@ -25,17 +25,20 @@ int64_t rdm_size(int norb, int kind);
 // Orbital-pair lists of one spin (k electrons in n orbitals), the work lists of the mixed-spin
 // 2-RDM: for every ordered orbital pair (p, q) the (k-1)-electron strings K that contain
 // neither p nor q, each as an entry (K+p, K+q, s(K,p) s(K,q)) with s(K,p) = (-1)^{#occupied
-// below p in K}. A list is cut into segments of kRdmSeg entries (the last one padded with
+// below p in K}. A list is cut into segments of `seg` entries (the last one padded with
 // entries that point at index N0, a zero sentinel) and the segment count is padded to a
 // multiple of 32. Segments are stored interleaved by 32 so that the 32 lanes of a warp, each
 // reading its own segment, read 32 consecutive entries:
-//   entry j of segment g is at ((g / 32) * kRdmSeg + j) * 32 + g % 32.
+//   entry j of segment g is at ((g / 32) * seg + j) * 32 + g % 32.
+// The beta lists (summed per thread) use kRdmSeg entries per segment; the alpha lists (the
+// blocks' work units) use kRdmSegA, small enough to balance the blocks.
 // Narrow entries (N0 <= 32766): left | right << 15 | negative << 30 (32 bit);
 // wide entries: left | right << 24 | negative << 48 (64 bit).
 constexpr int kRdmSeg = 64;
+constexpr int kRdmSegA = 16;
 
 struct PairListHost {
-    int n = 0, k = 0;
+    int n = 0, k = 0, seg = kRdmSeg;
     int64_t N0 = 0;      // strings with k electrons (also the padding index)
     int64_t nseg = 0;    // segments, a multiple of 32
     int64_t nentry = 0;  // real (unpadded) entries
@@ -44,13 +47,16 @@ struct PairListHost {
     std::vector<uint64_t> e64;
     std::vector<uint16_t> pair; // per segment: p * n + q
 };
-void build_pair_list(int n, int k, bool force_wide, PairListHost& out);
+void build_pair_list(int n, int k, bool force_wide, int seg, PairListHost& out);
 
 // Device scratch of the RDM builder, owned by a SigmaBuilder (created on first use).
 struct RdmScratch {
     bool lists_ready = false;
     int64_t nsega = 0, nsegb = 0;
     bool wideb = false;
+    // alpha segments that hold entries: all of them, and those with u <= x (bra = ket)
+    int64_t nwork_all = 0, nwork_sym = 0;
+    DevBuf<int32_t> work_all, work_sym;
     DevBuf<uint64_t> ea;       // alpha pair list, always wide (read once per row pair)
     DevBuf<uint32_t> eb32;     // beta pair list, narrow or wide
     DevBuf<uint64_t> eb64;
