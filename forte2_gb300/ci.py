@@ -370,16 +370,44 @@ class CASCISolver:
 
     # ---- reduced density matrices of the solved roots (ci.py:476-768) ----------------------------
 
-    def _det_vector(self, root):
-        """Determinant-basis vector of a root, on the device (ci.py's csf_C_to_det_C)."""
+    def _csf_to_det_device(self, csf_vec):
         torch = _torch()
-        v = self.evecs[:, root]
+        v = csf_vec
         if isinstance(v, np.ndarray):
             v = torch.from_numpy(np.ascontiguousarray(v))
         v = v.to(device="cuda", dtype=torch.float64).contiguous()
         det = torch.empty(self.ndet, dtype=torch.float64, device="cuda")
         self.spin_adapter.csf_C_to_det_C(v, det)
         return det
+
+    def _det_vector(self, root):
+        """Determinant-basis vector of a root, on the device."""
+        return self._csf_to_det_device(self.evecs[:, root])
+
+    def csf_C_to_det_C(self, csf_vec):
+        """A CSF-basis vector in the determinant basis, as a numpy array (ci.py:454-470)."""
+        return self._csf_to_det_device(csf_vec).cpu().numpy()
+
+    def _root_vector_det(self, root: int):
+        """CI vector of a root in the determinant basis (ci.py:472-474)."""
+        return self.csf_C_to_det_C(self.evecs[:, root])
+
+    def compute_natural_occupation_numbers(self):
+        """Natural occupation numbers (norb, nroot), each column descending (ci.py:770-785)."""
+        if not self.executed:
+            raise RuntimeError("CI solver has not been executed yet.")
+        no = np.zeros((self.norb, self.nroot))
+        for i in range(self.nroot):
+            no[:, i] = np.linalg.eigvalsh(self.make_1rdm(i))[::-1]
+        return no
+
+    def get_top_determinants(self, n=5):
+        """Per root, the n determinants with the largest |coefficient| as ((alpha mask, beta mask),
+        coefficient) pairs (ci.py:804-832)."""
+        if not self.executed:
+            raise RuntimeError("CI solver has not been executed yet.")
+        dets = self.ci_strings.make_determinants()
+        return [top_determinants(self._root_vector_det(i), dets, n) for i in range(self.nroot)]
 
     def _rdm_vectors(self, left_root, right_root):
         L = self._det_vector(left_root)
@@ -435,6 +463,13 @@ class CASCISolver:
             for form, e in zip(("RDMs", "expanded RDMs", "spin-free RDMs"), self.rdm_energies(root)):
                 if not np.isclose(self.evals[root], e, rtol=1e-6, atol=1e-8):
                     raise AssertionError(f"CI energy {self.evals[root]} Eh does not match {form} energy {e} Eh")
+
+
+def top_determinants(det_vec, dets, n):
+    """The n entries of a determinant vector with the largest |coefficient|, descending, as
+    (determinant, coefficient) pairs (the selection of ci.py:823-830)."""
+    order = np.argsort(np.abs(det_vec))[::-1]
+    return [(dets[int(j)], float(det_vec[j])) for j in order[: min(n, len(order))]]
 
 
 def packed_tensor4_to_tensor4(packed, n):

@@ -419,6 +419,29 @@ class CISigmaBuilder:
     def sf_2cumulant(self, C_left, C_right):
         return self._rdm("sf_2cumulant", C_left, C_right)
 
+    # transition 1-RDMs between two wave functions (ci_sigma_builder_1trdm.cc:10-131): both must
+    # have the same orbitals and electron counts; in a CAS space they then share one determinant
+    # list, so the transition RDM is the RDM between the two vectors
+    def _check_trdm_partner(self, sigmabuilder_right):
+        left, right = self.lists, sigmabuilder_right.lists
+        if left.norb != right.norb:
+            raise RuntimeError("FCI transition RDMs: The number of MOs must be the same in the two wave functions.")
+        if left.na != right.na or left.nb != right.nb:
+            raise RuntimeError("FCI transition RDMs: The number of alpha and beta electrons must be the same in the "
+                               "two wave functions.")
+
+    def a_1trdm(self, sigmabuilder_right, C_left, C_right):
+        self._check_trdm_partner(sigmabuilder_right)
+        return self._rdm("a_1rdm", C_left, C_right)
+
+    def b_1trdm(self, sigmabuilder_right, C_left, C_right):
+        self._check_trdm_partner(sigmabuilder_right)
+        return self._rdm("b_1rdm", C_left, C_right)
+
+    def sf_1trdm(self, sigmabuilder_right, C_left, C_right):
+        self._check_trdm_partner(sigmabuilder_right)
+        return self._rdm("sf_1rdm", C_left, C_right)
+
     def term(self, which, basis):
         """One HZ term alone (device tensors): "h0", "h1_a", "h1_b", "aabb", "aaaa", "bbbb"."""
         torch = _torch()

@@ -69,6 +69,16 @@ def test_rdm_device_tensors_and_shapes(cuda):
         sb.a_1rdm(dl, cr)
     s1, sb1, _ = builder(1, 1, 1, 3)
     assert sb1.aa_2rdm(np.ones(1), np.ones(1)).shape == (0, 0)
+    # transition 1-RDMs between two wave functions of the same space (ci_sigma_builder_1trdm.cc)
+    _, sb2, _ = builder(n, na, nb, 8)
+    assert close(sb.a_1trdm(sb2, cl, cr), sb.a_1rdm(cl, cr), 1e-14)
+    assert close(sb.sf_1trdm(sb2, cl, cr), sb.sf_1rdm(cl, cr), 1e-14)
+    _, sb3, _ = builder(n, nb, na, 8)
+    with pytest.raises(RuntimeError, match="alpha and beta electrons"):
+        sb.b_1trdm(sb3, cl, cr)
+    _, sb4, _ = builder(n - 1, na, nb, 8)
+    with pytest.raises(RuntimeError, match="number of MOs"):
+        sb.a_1trdm(sb4, cl, cr)
 
 
 def test_rdms_wide_lists_global_rows_vs_oracle(cuda):
@@ -144,3 +154,17 @@ def test_casci_rdm_self_check(cuda, mult):
     assert abs(np.trace(a) - 4) < 1e-10 and abs(np.trace(b) - 4) < 1e-10
     # transition 1-RDM between orthogonal roots is traceless
     assert abs(np.trace(solver.make_1rdm(0, 1))) < 1e-10
+    # natural occupations (ci.py:770-785): 8 electrons, each in [0, 2], descending per root
+    no = solver.compute_natural_occupation_numbers()
+    assert no.shape == (n, nroot)
+    assert np.allclose(no.sum(axis=0), 8.0, atol=1e-10)
+    assert np.all(no > -1e-10) and np.all(no < 2.0 + 1e-10)
+    assert np.all(np.diff(no, axis=0) <= 1e-12)
+    # leading determinants (ci.py:804-832)
+    c0 = solver._root_vector_det(0)
+    assert abs(np.linalg.norm(c0) - 1.0) < 1e-10
+    top = solver.get_top_determinants(3)
+    assert len(top) == nroot and all(len(t) == 3 for t in top)
+    (alpha, beta), coef = top[0][0]
+    assert abs(abs(coef) - np.abs(c0).max()) < 1e-12
+    assert bin(alpha).count("1") == 4 and bin(beta).count("1") == 4

@@ -180,3 +180,32 @@ def test_hole_gram_replay_matches_oracle(n, na, nb):
         got2 = replay_hole_gram(byK.values(), ncol, L, R, npair)
         ref2 = port.rdm(kind2, CL, CR).reshape(npair, npair)
         assert np.abs(got2 - ref2).max(initial=0) < 1e-13
+
+
+def test_packed_expansion_and_top_determinants():
+    """Host helpers of the CI driver: the packed same-spin 2-RDM expansion used by the RDM energy
+    check (ci.py:337-341) reproduces the oracle's energy through the antisymmetrised integrals, and
+    the top-determinant selection of ci.py:823-830."""
+    from forte2_gb300.ci import packed_tensor4_to_tensor4, top_determinants
+    from forte2_gb300.synthetic import make_integrals
+
+    build_port()
+    n, na, nb = 6, 3, 3
+    ints = make_integrals(n, 41)
+    port = PortCI(n, na, nb)
+    port.set_hamiltonian(ints.E, ints.H, ints.V)
+    c = random_ci_vector(port.ndet, 42)
+    npair = n * (n - 1) // 2
+    aa = port.rdm("aa_2rdm", c, c).reshape(npair, npair)
+    full = packed_tensor4_to_tensor4(aa, n)
+    assert np.allclose(full, -full.transpose(1, 0, 2, 3)) and np.allclose(full, -full.transpose(0, 1, 3, 2))
+    assert full[3, 1, 2, 0] == aa[3 * 2 // 2 + 1, 1]
+    V = ints.V
+    A = V - V.transpose(0, 1, 3, 2)
+    i, j = np.tril_indices(n, k=-1)
+    M = A[i[:, None], j[:, None], i[None, :], j[None, :]]
+    assert abs(np.einsum("ij,ij", aa, M) - 0.25 * np.einsum("ijkl,ijkl", full, A)) < 1e-12
+    assert packed_tensor4_to_tensor4(np.zeros((0, 0)), 1).shape == (1, 1, 1, 1)
+    top = top_determinants(np.array([0.1, -0.9, 0.3, 0.0]), ["a", "b", "c", "d"], 3)
+    assert top == [("b", -0.9), ("c", 0.3), ("a", 0.1)]
+    assert top_determinants(np.array([0.5]), ["a"], 5) == [("a", 0.5)]
