@@ -27,6 +27,7 @@ SOURCES=(
     ci/ci_sigma_builder_knowles_handy.cc
     ci/ci_sigma_builder_1rdm.cc
     ci/ci_sigma_builder_2rdm.cc
+    ci/ci_sigma_builder_3rdm.cc
     determinant/slater_rules.cc
     determinant/ci_spin_adapter.cc
 )

@@ -157,13 +157,15 @@ class PortCI:
         return out
 
     RDM_KINDS = {"a_1rdm": 0, "b_1rdm": 1, "sf_1rdm": 2, "aa_2rdm": 3, "bb_2rdm": 4, "ab_2rdm": 5,
-                 "sf_2rdm": 6, "sf_2cumulant": 7}
+                 "sf_2rdm": 6, "sf_2cumulant": 7, "aaa_3rdm": 8, "bbb_3rdm": 9, "aab_3rdm": 10, "abb_3rdm": 11,
+                 "sf_3rdm": 12, "sf_3cumulant": 13}
 
     def rdm(self, kind, CL, CR):
         """Reduced density matrix `kind` between determinant vectors CL (bra) and CR (ket), flat."""
         n = self.norb
-        npair = n * (n - 1) // 2
-        size = {0: n * n, 1: n * n, 2: n * n, 3: npair * npair, 4: npair * npair}.get(self.RDM_KINDS[kind], n ** 4)
+        npair, ntrip = n * (n - 1) // 2, n * (n - 1) * (n - 2) // 6
+        size = {0: n * n, 1: n * n, 2: n * n, 3: npair * npair, 4: npair * npair, 5: n ** 4, 6: n ** 4, 7: n ** 4,
+                8: ntrip ** 2, 9: ntrip ** 2, 10: (npair * n) ** 2, 11: (npair * n) ** 2}.get(self.RDM_KINDS[kind], n ** 6)
         out = np.zeros(max(size, 1))
         got = lib().port_rdm(self.h, self.RDM_KINDS[kind], np.ascontiguousarray(CL, np.float64),
                              np.ascontiguousarray(CR, np.float64), out)

@@ -19,7 +19,8 @@
 //     Clebsch-Gordan overlaps and the creation-order sign; csf<->det transforms;
 //   * reduced density matrices between two determinant vectors: spin-dependent and spin-free
 //     1-RDMs (ci_sigma_builder_1rdm.cc:9-84), same-spin packed and mixed-spin 2-RDMs, the
-//     spin-free 2-RDM and its cumulant (ci_sigma_builder_2rdm.cc:46-282).
+//     spin-free 2-RDM and its cumulant (ci_sigma_builder_2rdm.cc:46-282), and the 3-RDMs
+//     (same-spin packed, aab, abb, spin-free) and 3-cumulant (ci_sigma_builder_3rdm.cc:84-542).
 //
 // Work is spread over host threads (ORACLE_THREADS, default: all hardware threads) the way the
 // reference's parallel_for_chunked does (forte2/helpers/parallel.h:140-166).
@@ -149,6 +150,12 @@ struct H2E {
     uint32_t I;
 };
 
+struct H3E {
+    int16_t sign;
+    uint8_t p, q, r;
+    uint32_t I;
+};
+
 // 1-hole list grouped by K (N-1 electrons): entries in ascending address of I = K + p.
 void make_1h(const StringSpace& S, const StringSpace& S1, std::vector<std::vector<H1E>>& L) {
     L.assign(S1.size(), {});
@@ -183,6 +190,28 @@ void make_2h(const StringSpace& S, const StringSpace& S2, std::vector<std::vecto
                 L[S2.rank(K)].push_back({(int16_t)((qs ^ ps) ? -1 : 1), (uint8_t)p, (uint8_t)q, (uint32_t)I});
             }
         }
+    }
+}
+
+// 3-hole list grouped by K (N-3 electrons), p > q > r; the sign removes r, then q, then p, each
+// with (-1)^{#occupied below it} (ci_strings_makers.cc:276-318).
+void make_3h(const StringSpace& S, const StringSpace& S3, std::vector<std::vector<H3E>>& L) {
+    L.assign(S3.size(), {});
+    if (S.k < 3)
+        return;
+    for (size_t I = 0; I < S.size(); ++I) {
+        const uint64_t m = S.s[I];
+        for (int r = 0; r < S.n; ++r)
+            for (int q = r + 1; q < S.n; ++q)
+                for (int p = q + 1; p < S.n; ++p) {
+                    if (!((m >> p & 1) && (m >> q & 1) && (m >> r & 1)))
+                        continue;
+                    const uint64_t J1 = m & ~(uint64_t(1) << r);
+                    const uint64_t J2 = J1 & ~(uint64_t(1) << q);
+                    const uint64_t K = J2 & ~(uint64_t(1) << p);
+                    const int neg = parity_below(m, r) ^ parity_below(J1, q) ^ parity_below(J2, p);
+                    L[S3.rank(K)].push_back({(int16_t)(neg ? -1 : 1), (uint8_t)p, (uint8_t)q, (uint8_t)r, (uint32_t)I});
+                }
     }
 }
 
@@ -259,9 +288,21 @@ struct SpinAdapter {
 
 struct Port {
     int n = 0, na = 0, nb = 0;
-    StringSpace A, B, A1, B1, A2, B2;
+    StringSpace A, B, A1, B1, A2, B2, A3, B3;
     std::vector<std::vector<H1E>> a1, b1;
     std::vector<std::vector<H2E>> a2, b2;
+    std::vector<std::vector<H3E>> a3, b3; // built on first use (3-RDMs)
+    bool lists3 = false;
+
+    void build_3h() {
+        if (lists3)
+            return;
+        A3.build(n, na - 3);
+        B3.build(n, nb - 3);
+        make_3h(A, A3, a3);
+        make_3h(B, B3, b3);
+        lists3 = true;
+    }
     double E = 0.0;
     std::vector<double> h, V; // h[p*n+q], V[((p*n+q)*n+r)*n+s] physicist
     std::vector<double> v_pr_qs, v_pr_qs_a;
@@ -738,6 +779,160 @@ struct RdmPort {
         }
         return sf;
     }
+
+    // ---- 3-RDMs (ci_sigma_builder_3rdm.cc:84-542); P.build_3h() must have run ----
+
+    // gamma[pqr][stu] (p > q > r, s > t > u, triplet index p(p-1)(p-2)/6 + q(q-1)/2 + r) =
+    // sum over 3-hole strings K of sign(K; p,q,r) sign(K; s,t,u) <row K+p+q+r | row K+s+t+u>
+    std::vector<double> same_spin3(int spin) const {
+        const int n = P.n;
+        const size_t nt = n >= 3 ? (size_t)n * (n - 1) * (n - 2) / 6 : 0;
+        const auto& L3 = spin == 0 ? P.a3 : P.b3;
+        const StringSpace& S = spin == 0 ? P.A : P.B;
+        if (S.k < 3 || nt == 0)
+            return std::vector<double>(nt * nt, 0.0);
+        auto tri = [](size_t p, size_t q, size_t r) { return p * (p - 1) * (p - 2) / 6 + q * (q - 1) / 2 + r; };
+        return parallel_sum(items(L3.size()), nt * nt, [&](size_t b, size_t e, double* g) {
+            for (size_t K = b; K < e; ++K)
+                for (const auto& l : L3[K])
+                    for (const auto& r : L3[K])
+                        g[tri(l.p, l.q, l.r) * nt + tri(r.p, r.q, r.r)] += l.sign * r.sign * dot(spin, l.I, r.I);
+        });
+    }
+
+    // gamma[pq][r][st][u] (alpha pairs p > q, s > t; beta r, u) = sum over 2-hole alpha strings Ka
+    // and 1-hole beta strings Kb of s(Ka;p,q) s(Kb,r) CL(Ka+p+q, Kb+r) s(Ka;s,t) s(Kb,u) CR(Ka+s+t, Kb+u)
+    std::vector<double> aab() const {
+        const size_t n = P.n, np = n >= 2 ? n * (n - 1) / 2 : 0, M = np * n;
+        if (P.na < 2 || P.nb < 1 || n < 2)
+            return std::vector<double>(M * M, 0.0);
+        const size_t nb = NB();
+        return parallel_sum(items(P.a2.size()), M * M, [&](size_t b, size_t e, double* g) {
+            for (size_t Ka = b; Ka < e; ++Ka)
+                for (const auto& l : P.a2[Ka])
+                    for (const auto& r : P.a2[Ka]) {
+                        const double sa = l.sign * r.sign;
+                        const double* rl = CL + (size_t)l.I * nb;
+                        const double* rr = CR + (size_t)r.I * nb;
+                        const size_t row = ((size_t)l.p * (l.p - 1) / 2 + l.q) * n;
+                        const size_t col = ((size_t)r.p * (r.p - 1) / 2 + r.q) * n;
+                        for (const auto& Kb : P.b1)
+                            for (const auto& v : Kb) {
+                                const double lv = sa * v.sign * rl[v.I];
+                                for (const auto& y : Kb)
+                                    g[(row + v.p) * M + col + y.p] += lv * y.sign * rr[y.I];
+                            }
+                    }
+        });
+    }
+
+    // gamma[p][qr][s][tu] (alpha p, s; beta pairs q > r, t > u) over 1-hole alpha and 2-hole beta
+    std::vector<double> abb() const {
+        const size_t n = P.n, np = n >= 2 ? n * (n - 1) / 2 : 0, M = n * np;
+        if (P.na < 1 || P.nb < 2 || n < 2)
+            return std::vector<double>(M * M, 0.0);
+        const size_t nb = NB();
+        return parallel_sum(items(P.a1.size()), M * M, [&](size_t b, size_t e, double* g) {
+            for (size_t Ka = b; Ka < e; ++Ka)
+                for (const auto& l : P.a1[Ka])
+                    for (const auto& r : P.a1[Ka]) {
+                        const double sa = l.sign * r.sign;
+                        const double* rl = CL + (size_t)l.I * nb;
+                        const double* rr = CR + (size_t)r.I * nb;
+                        for (const auto& Kb : P.b2)
+                            for (const auto& v : Kb) {
+                                const double lv = sa * v.sign * rl[v.I];
+                                const size_t row = (size_t)l.p * np + (size_t)v.p * (v.p - 1) / 2 + v.q;
+                                for (const auto& y : Kb)
+                                    g[row * M + (size_t)r.p * np + (size_t)y.p * (y.p - 1) / 2 + y.q] +=
+                                        lv * y.sign * rr[y.I];
+                            }
+                    }
+        });
+    }
+
+    // spin-free 3-RDM G3[p][q][r][s][t][u] = sum over spins of <a+_p a+_q a+_r a_u a_t a_s>: the
+    // same-spin blocks with all permutation signs, and each mixed block in its three placements of
+    // the odd spin (ci_sigma_builder_3rdm.cc:320-497)
+    std::vector<double> spin_free3() const {
+        const size_t n = P.n;
+        const size_t n6 = n * n * n * n * n * n;
+        std::vector<double> sf(n6, 0.0);
+        if (n < 2)
+            return sf;
+        auto at = [n](size_t a, size_t b, size_t c, size_t d, size_t e, size_t f) {
+            return ((((a * n + b) * n + c) * n + d) * n + e) * n + f;
+        };
+        const size_t np = n * (n - 1) / 2;
+        // pair variants (x, y, sign): (hi, lo, +1) and (lo, hi, -1)
+        auto variants = [](size_t hi, size_t lo, size_t* x, size_t* y, double* sg) {
+            x[0] = hi, y[0] = lo, sg[0] = 1.0;
+            x[1] = lo, y[1] = hi, sg[1] = -1.0;
+        };
+        const auto g_aab = aab();
+        for (size_t p = 1; p < n; ++p)
+            for (size_t q = 0; q < p; ++q)
+                for (size_t r = 0; r < n; ++r)
+                    for (size_t s = 1; s < n; ++s)
+                        for (size_t t = 0; t < s; ++t)
+                            for (size_t u = 0; u < n; ++u) {
+                                const double el = g_aab[(((p * (p - 1) / 2 + q) * n + r) * np + s * (s - 1) / 2 + t) * n + u];
+                                size_t a1[2], a2[2], b1[2], b2[2];
+                                double sa[2], sb[2];
+                                variants(p, q, a1, a2, sa);
+                                variants(s, t, b1, b2, sb);
+                                for (int i = 0; i < 2; ++i)
+                                    for (int j = 0; j < 2; ++j) {
+                                        const double v = sa[i] * sb[j] * el;
+                                        sf[at(a1[i], a2[i], r, b1[j], b2[j], u)] += v; // beta third
+                                        sf[at(a1[i], r, a2[i], b1[j], u, b2[j])] += v; // beta second
+                                        sf[at(r, a1[i], a2[i], u, b1[j], b2[j])] += v; // beta first
+                                    }
+                            }
+        const auto g_abb = abb();
+        for (size_t p = 0; p < n; ++p)
+            for (size_t q = 1; q < n; ++q)
+                for (size_t r = 0; r < q; ++r)
+                    for (size_t s = 0; s < n; ++s)
+                        for (size_t t = 1; t < n; ++t)
+                            for (size_t u = 0; u < t; ++u) {
+                                const double el = g_abb[((p * np + q * (q - 1) / 2 + r) * n + s) * np + t * (t - 1) / 2 + u];
+                                size_t a1[2], a2[2], b1[2], b2[2];
+                                double sa[2], sb[2];
+                                variants(q, r, a1, a2, sa);
+                                variants(t, u, b1, b2, sb);
+                                for (int i = 0; i < 2; ++i)
+                                    for (int j = 0; j < 2; ++j) {
+                                        const double v = sa[i] * sb[j] * el;
+                                        sf[at(p, a1[i], a2[i], s, b1[j], b2[j])] += v; // alpha first
+                                        sf[at(a1[i], p, a2[i], b1[j], s, b2[j])] += v; // alpha second
+                                        sf[at(a1[i], a2[i], p, b1[j], b2[j], s)] += v; // alpha third
+                                    }
+                            }
+        if (n < 3)
+            return sf;
+        const size_t nt = n * (n - 1) * (n - 2) / 6;
+        // the six orderings of a triple (x, y, z) = (0, 1, 2) with their permutation signs
+        const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {2, 0, 1}, {2, 1, 0}, {1, 2, 0}, {1, 0, 2}};
+        const double psign[6] = {1, -1, 1, -1, 1, -1};
+        for (int spin = 0; spin < 2; ++spin) {
+            const auto g = same_spin3(spin);
+            for (size_t p = 2, pqr = 0; p < n; ++p)
+                for (size_t q = 1; q < p; ++q)
+                    for (size_t r = 0; r < q; ++r, ++pqr)
+                        for (size_t s = 2, stu = 0; s < n; ++s)
+                            for (size_t t = 1; t < s; ++t)
+                                for (size_t u = 0; u < t; ++u, ++stu) {
+                                    const double el = g[pqr * nt + stu];
+                                    const size_t bra[3] = {p, q, r}, ket[3] = {s, t, u};
+                                    for (int i = 0; i < 6; ++i)
+                                        for (int j = 0; j < 6; ++j)
+                                            sf[at(bra[perm[i][0]], bra[perm[i][1]], bra[perm[i][2]], ket[perm[j][0]],
+                                                  ket[perm[j][1]], ket[perm[j][2]])] += psign[i] * psign[j] * el;
+                                }
+        }
+        return sf;
+    }
 };
 
 } // namespace
@@ -930,10 +1125,13 @@ void port_hdiag_csf(void* h, void* s, double* out) {
 }
 
 /// Reduced density matrices between two determinant vectors (kinds as in the GPU library:
-/// 0 a_1rdm, 1 b_1rdm, 2 sf_1rdm, 3 aa_2rdm, 4 bb_2rdm, 5 ab_2rdm, 6 sf_2rdm, 7 sf_2cumulant).
+/// 0 a_1rdm, 1 b_1rdm, 2 sf_1rdm, 3 aa_2rdm, 4 bb_2rdm, 5 ab_2rdm, 6 sf_2rdm, 7 sf_2cumulant;
+/// and 8 aaa_3rdm, 9 bbb_3rdm, 10 aab_3rdm, 11 abb_3rdm, 12 sf_3rdm, 13 sf_3cumulant).
 /// Returns the number of doubles written to out, or -1 for an unknown kind.
 int64_t port_rdm(void* h, int kind, const double* CL, const double* CR, double* out) {
-    const auto& P = *static_cast<Port*>(h);
+    auto& P = *static_cast<Port*>(h);
+    if (kind >= 8)
+        P.build_3h();
     RdmPort R{P, CL, CR};
     const size_t n = P.n;
     std::vector<double> r;
@@ -965,6 +1163,41 @@ int64_t port_rdm(void* h, int kind, const double* CL, const double* CR, double* 
                     for (size_t s = 0; s < n; ++s)
                         r[((p * n + q) * n + a) * n + s] +=
                             -g1[p * n + a] * g1[q * n + s] + 0.5 * g1[p * n + s] * g1[q * n + a];
+        break;
+    }
+    case 8: r = R.same_spin3(0); break;
+    case 9: r = R.same_spin3(1); break;
+    case 10: r = R.aab(); break;
+    case 11: r = R.abb(); break;
+    case 12: r = R.spin_free3(); break;
+    case 13: {
+        // spin-free 3-cumulant (ci_sigma_builder_3rdm.cc:499-540): G3 minus the products of
+        // G1 with G2 and of three G1 that the cumulant expansion removes
+        r = R.spin_free3();
+        if (n < 2)
+            break;
+        auto g1 = R.one(0);
+        const auto b1 = R.one(1);
+        for (size_t i = 0; i < g1.size(); ++i)
+            g1[i] += b1[i];
+        const auto g2 = R.spin_free2();
+        auto G1 = [&](size_t a, size_t b) { return g1[a * n + b]; };
+        auto G2 = [&](size_t a, size_t b, size_t c, size_t d) { return g2[((a * n + b) * n + c) * n + d]; };
+        size_t i = 0;
+        for (size_t p = 0; p < n; ++p)
+            for (size_t q = 0; q < n; ++q)
+                for (size_t a = 0; a < n; ++a)
+                    for (size_t s = 0; s < n; ++s)
+                        for (size_t t = 0; t < n; ++t)
+                            for (size_t u = 0; u < n; ++u, ++i) {
+                                double v = -G1(p, s) * G2(q, a, t, u) - G1(q, t) * G2(p, a, s, u) - G1(a, u) * G2(p, q, s, t);
+                                v += 0.5 * (G1(p, t) * G2(q, a, s, u) + G1(p, u) * G2(q, a, t, s) + G1(q, s) * G2(p, a, t, u) +
+                                            G1(q, u) * G2(p, a, s, t) + G1(a, s) * G2(p, q, u, t) + G1(a, t) * G2(p, q, s, u));
+                                v += 2.0 * G1(p, s) * G1(q, t) * G1(a, u) - G1(p, s) * G1(q, u) * G1(a, t) -
+                                     G1(p, u) * G1(q, t) * G1(a, s) - G1(p, t) * G1(q, s) * G1(a, u) +
+                                     0.5 * (G1(p, t) * G1(q, u) * G1(a, s) + G1(p, u) * G1(q, s) * G1(a, t));
+                                r[i] += v;
+                            }
         break;
     }
     default: return -1;

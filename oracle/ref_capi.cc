@@ -415,9 +415,11 @@ double ref_slater_rules_csf(void* hsig, void* hsa, void* hs, int64_t I, int64_t 
 
 
 /// Reduced density matrices of the reference (ci_sigma_builder_1rdm.cc:9-84,
-/// ci_sigma_builder_2rdm.cc:46-282) between two determinant vectors, copied into `out`:
-/// kind 0 a_1rdm, 1 b_1rdm, 2 sf_1rdm (n*n); 3 aa_2rdm, 4 bb_2rdm (P*P, P = n(n-1)/2);
-/// 5 ab_2rdm, 6 sf_2rdm, 7 sf_2cumulant (n^4). Returns the number of elements written.
+/// ci_sigma_builder_2rdm.cc:46-282, ci_sigma_builder_3rdm.cc:84-542) between two determinant
+/// vectors, copied into `out`: kind 0 a_1rdm, 1 b_1rdm, 2 sf_1rdm (n*n); 3 aa_2rdm, 4 bb_2rdm
+/// (P*P, P = n(n-1)/2); 5 ab_2rdm, 6 sf_2rdm, 7 sf_2cumulant (n^4); 8 aaa_3rdm, 9 bbb_3rdm
+/// (T*T, T = n(n-1)(n-2)/6); 10 aab_3rdm (P, n, P, n); 11 abb_3rdm (n, P, n, P); 12 sf_3rdm,
+/// 13 sf_3cumulant (n^6). Returns the number of elements written.
 int64_t ref_rdm(void* h, int kind, double* CL, double* CR, int64_t ndet, double* out) {
     try {
         auto* sb = static_cast<RefSigma*>(h)->sb;
@@ -436,6 +438,12 @@ int64_t ref_rdm(void* h, int kind, double* CL, double* CR, int64_t ndet, double*
         case 5: return copy(sb->compute_ab_2rdm(l, r));
         case 6: return copy(sb->compute_sf_2rdm(l, r));
         case 7: return copy(sb->compute_sf_2cumulant(l, r));
+        case 8: return copy(sb->compute_aaa_3rdm(l, r));
+        case 9: return copy(sb->compute_bbb_3rdm(l, r));
+        case 10: return copy(sb->compute_aab_3rdm(l, r));
+        case 11: return copy(sb->compute_abb_3rdm(l, r));
+        case 12: return copy(sb->compute_sf_3rdm(l, r));
+        case 13: return copy(sb->compute_sf_3cumulant(l, r));
         default: throw std::runtime_error("unknown RDM kind");
         }
     } catch (const std::exception& e) {

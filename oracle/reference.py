@@ -218,13 +218,15 @@ class RefSigmaBuilder:
         return out
 
     RDM_KINDS = {"a_1rdm": 0, "b_1rdm": 1, "sf_1rdm": 2, "aa_2rdm": 3, "bb_2rdm": 4, "ab_2rdm": 5,
-                 "sf_2rdm": 6, "sf_2cumulant": 7}
+                 "sf_2rdm": 6, "sf_2cumulant": 7, "aaa_3rdm": 8, "bbb_3rdm": 9, "aab_3rdm": 10, "abb_3rdm": 11,
+                 "sf_3rdm": 12, "sf_3cumulant": 13}
 
     def rdm(self, kind, CL, CR):
-        """The reference's compute_<kind> (ci_sigma_builder_1rdm.cc, _2rdm.cc) as a flat array."""
+        """The reference's compute_<kind> (ci_sigma_builder_1rdm.cc, _2rdm.cc, _3rdm.cc) as a flat array."""
         n = self.strings.norb
-        size = {0: n * n, 1: n * n, 2: n * n, 3: (n * (n - 1) // 2) ** 2, 4: (n * (n - 1) // 2) ** 2}.get(
-            self.RDM_KINDS[kind], n ** 4)
+        P, T = n * (n - 1) // 2, n * (n - 1) * (n - 2) // 6
+        size = {0: n * n, 1: n * n, 2: n * n, 3: P * P, 4: P * P, 5: n ** 4, 6: n ** 4, 7: n ** 4, 8: T * T,
+                9: T * T, 10: (P * n) ** 2, 11: (P * n) ** 2}.get(self.RDM_KINDS[kind], n ** 6)
         out = np.zeros(max(size, 1))
         got = lib().ref_rdm(self.h, self.RDM_KINDS[kind], np.ascontiguousarray(CL, dtype=np.float64),
                             np.ascontiguousarray(CR, dtype=np.float64), CL.shape[0], out)

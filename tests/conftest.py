@@ -37,6 +37,29 @@ def golden_rdm():
 
 
 @pytest.fixture(scope="session")
+def golden_rdm3():
+    with open(os.path.join(GOLDEN, "rdm3_checksums.json")) as f:
+        meta = json.load(f)
+    return meta, np.load(os.path.join(GOLDEN, "rdm3.npz"))
+
+
+def rdm_checksum_matches(a, ref, seed, tol=1e-12):
+    """a against a checksum of tests/golden/make_golden.py:rdm_checksum (same seed recipe)."""
+    a = np.asarray(a).reshape(-1)
+    if ref["size"] == 0:
+        return a.size == 0
+    if a.size != ref["size"]:
+        return False
+    rng = np.random.default_rng(seed)
+    w = rng.normal(size=a.size)
+    idx = np.sort(rng.choice(a.size, size=min(64, a.size), replace=False))
+    scale = max(1.0, ref["norm"])
+    return (idx.tolist() == ref["idx"] and abs(float(np.linalg.norm(a)) - ref["norm"]) <= tol * scale
+            and abs(float(a @ w) - ref["dot_w"]) <= tol * scale * np.sqrt(a.size)
+            and np.abs(a[idx] - np.array(ref["vals"])).max() <= tol * scale)
+
+
+@pytest.fixture(scope="session")
 def golden_checksums():
     with open(os.path.join(GOLDEN, "sigma_checksums.json")) as f:
         return json.load(f)

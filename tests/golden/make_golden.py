@@ -175,6 +175,44 @@ def gen_rdm(out):
     np.savez_compressed(os.path.join(out, "rdm.npz"), **data)
 
 
+RDM3_KINDS = ("aaa_3rdm", "bbb_3rdm", "aab_3rdm", "abb_3rdm", "sf_3rdm", "sf_3cumulant")
+
+
+def rdm_checksum(a, seed):
+    """Compact pin of a large array: its norm, its dot product with a seeded normal vector and
+    64 entries at seeded positions."""
+    a = np.asarray(a).reshape(-1)
+    if a.size == 0:
+        return dict(size=0)
+    rng = np.random.default_rng(seed)
+    w = rng.normal(size=a.size)
+    idx = np.sort(rng.choice(a.size, size=min(64, a.size), replace=False))
+    return dict(size=int(a.size), norm=float(np.linalg.norm(a)), dot_w=float(a @ w), idx=idx.tolist(),
+                vals=a[idx].tolist())
+
+
+def gen_rdm3(out):
+    """The reference's 3-RDMs (ci_sigma_builder_3rdm.cc) on the RDM_CASES vectors: checksums for
+    every case, full arrays for the spaces of at most 4 orbitals."""
+    data, meta = {}, {}
+    for na, nb, n, sl, sr in RDM_CASES:
+        ints = make_integrals(n, sl)
+        s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+        sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
+        cl = random_ci_vector(s.ndet, sl)
+        cr = random_ci_vector(s.ndet, sr)
+        key = f"{na}_{nb}_{n}"
+        for j, kind in enumerate(RDM3_KINDS):
+            for tag, b in (("LR", cr), ("LL", cl)):
+                a = sb.rdm(kind, cl, b)
+                meta[f"{key}_{kind}_{tag}"] = rdm_checksum(a, 7000 + 10 * j + (tag == "LL"))
+                if n <= 4:
+                    data[f"{key}_{kind}_{tag}"] = a
+    np.savez_compressed(os.path.join(out, "rdm3.npz"), **data)
+    with open(os.path.join(out, "rdm3_checksums.json"), "w") as f:
+        json.dump(meta, f)
+
+
 def checksums(sig, ndet, seed):
     rng = np.random.default_rng(seed)
     w = rng.normal(size=ndet)
@@ -288,7 +326,8 @@ def main():
     ref.open_blas(threads=os.cpu_count())
     steps = {"lists": lambda: gen_lists(HERE), "sigma": lambda: gen_sigma(HERE),
              "checksums": lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_CASES, "sigma_checksums.json"),
-             "davidson": lambda: gen_davidson(HERE, a.reference), "rdm": lambda: gen_rdm(HERE)}
+             "davidson": lambda: gen_davidson(HERE, a.reference), "rdm": lambda: gen_rdm(HERE),
+             "rdm3": lambda: gen_rdm3(HERE)}
     if a.big:
         steps["big"] = lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_BIG, "sigma_checksums_16.json")
     for name, f in steps.items():

@@ -191,3 +191,40 @@ def test_port_rdm_energy_identity():
         g2 = p.rdm("sf_2rdm", c, c).reshape(n, n, n, n)
         e_rdm = ints.E + np.einsum("ij,ij", g1, ints.H) + 0.5 * np.einsum("ijkl,ijkl", g2, ints.V)
         assert abs(e_sigma - e_rdm) < 1e-11 * max(1.0, abs(e_sigma)), (n, e_sigma, e_rdm)
+
+
+RDM3_KINDS = ("aaa_3rdm", "bbb_3rdm", "aab_3rdm", "abb_3rdm", "sf_3rdm", "sf_3cumulant")
+
+
+def test_port_3rdms_match_reference(golden_rdm, golden_rdm3):
+    """The restatement's 3-RDMs and 3-cumulant equal the reference's (ci_sigma_builder_3rdm.cc):
+    full arrays for up to 4 orbitals, checksums (norm, seeded dot product, 64 sampled entries)
+    for all spaces of the RDM fixtures."""
+    from conftest import rdm_checksum_matches
+
+    meta, full = golden_rdm3
+    for na, nb, n in list_cases(golden_rdm):
+        key = f"{na}_{nb}_{n}"
+        sl, sr = golden_rdm[f"{key}_seeds"]
+        p = PortCI(n, na, nb)
+        cl = random_ci_vector(p.ndet, int(sl))
+        cr = random_ci_vector(p.ndet, int(sr))
+        for j, kind in enumerate(RDM3_KINDS):
+            for tag, b in (("LR", cr), ("LL", cl)):
+                got = p.rdm(kind, cl, b)
+                name = f"{key}_{kind}_{tag}"
+                assert rdm_checksum_matches(got, meta[name], 7000 + 10 * j + (tag == "LL")), name
+                if name in full.files:
+                    ref = full[name]
+                    assert got.shape == ref.shape
+                    assert np.abs(got - ref).max(initial=0.0) <= 1e-13 * max(1.0, np.abs(ref).max(initial=0.0))
+
+
+def test_port_3rdm_partial_trace():
+    """sum_r G3[p,q,r,s,t,r] = (N - 2) G2[p,q,s,t] for the spin-free RDMs of one vector."""
+    for na, nb, n in ((3, 3, 6), (4, 2, 7)):
+        p = PortCI(n, na, nb)
+        c = random_ci_vector(p.ndet, 77)
+        g3 = p.rdm("sf_3rdm", c, c).reshape((n,) * 6)
+        g2 = p.rdm("sf_2rdm", c, c).reshape((n,) * 4)
+        assert np.abs(np.einsum("pqrstr->pqst", g3) - (na + nb - 2) * g2).max() < 1e-12
