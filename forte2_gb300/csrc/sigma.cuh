@@ -95,7 +95,8 @@ struct SigmaBuilder {
     std::shared_ptr<int> graph_users = std::make_shared<int>(0);
     DevBuf<double> gCt, gTt;
     DevBuf<float> gfC, gfS, gfCt, gfTt;
-    // one HZ term into sigma (overwrites): 0 H0, 1 H1a, 2 H1b, 3 aabb, 4 aaaa(+H1a? no), 5 bbbb
+    // one HZ term into sigma (overwrites): 0 H0, 1 H1 alpha, 2 H1 beta, 3 opposite spin (aabb),
+    // 4 alpha same-spin two-electron part alone (aaaa), 5 beta same-spin two-electron part (bbbb)
     void term(int which, const double* C, double* sigma, cudaStream_t st);
     void det_energies(double* out, cudaStream_t st);
     void flush_timers();
