@@ -483,7 +483,9 @@ def run_rdm(a):
                         "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": ab_flop / ab_s / 1e12 / FP64_PEAK_TFLOPS,
                         "flop_per_launch": ab_flop, "ms": ab_s * 1e3, "traffic": None,
                         "peak_source": "measured FP64 DGEMM, profiles/gb300_gemm_peaks.md"},
-           "clocks": clk}
+           "clocks": clk,
+           # per set: k_rdm_hole<1> x2, k_transpose x2, k_rdm_ab, its mirror, k_rdm_hole<2> x2, k_rdm_sf2
+           "gpu_launches": 9 * a.steps}
     if not a.no_cpu_baseline:
         v, sample, cores = rdm_cpu_baseline(n, na, nb, c_host, a.cpu_seconds)
         out["cpu_baseline"] = {"value": v, "unit": "RDM sets/s", "cores": cores, "kind": "port", "sample": sample}
