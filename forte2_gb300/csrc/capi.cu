@@ -187,10 +187,12 @@ int f2g_sigma_set_algorithm(void* sb, const char* name) {
 int f2g_sigma_get_algorithm(void* sb, char* buf, int buflen) {
     return guard([&] {
         need(sb, "sigma");
+        need(buf, "buf");
+        if (buflen <= 0)
+            throw Error(2, "buflen must be positive");
         const char* name = static_cast<SigmaBuilder*>(sb)->algorithm == 0 ? "Knowles-Handy" : "Harrison-Zarrabian";
-        std::strncpy(buf, name, buflen);
-        if (buflen > 0)
-            buf[buflen - 1] = 0;
+        std::strncpy(buf, name, (size_t)buflen);
+        buf[buflen - 1] = 0;
     });
 }
 
@@ -273,6 +275,10 @@ int f2g_sigma_apply(void* sb, const double* C, double* sigma, int nvec, void* st
         need(sb, "sigma");
         auto* b = static_cast<SigmaBuilder*>(sb);
         const int64_t nd = b->s->ndet;
+        if (nvec < 0)
+            throw Error(2, "nvec must be >= 0");
+        if (nvec == 0)
+            return;
         if (nd && (!C || !sigma))
             throw Error(2, "NULL vector");
         b->hamiltonian(C, sigma, S(stream), nvec);
@@ -284,8 +290,12 @@ int f2g_sigma_apply_host(void* sb, const double* C, double* sigma, int nvec) {
         need(sb, "sigma");
         auto* b = static_cast<SigmaBuilder*>(sb);
         const int64_t nd = b->s->ndet;
-        if (nd == 0)
+        if (nvec < 0)
+            throw Error(2, "nvec must be >= 0");
+        if (nd == 0 || nvec == 0)
             return;
+        if (!C || !sigma)
+            throw Error(2, "NULL vector");
         double* dc = b->hostC.reserve(nd);
         double* ds = b->hostS.reserve(nd);
         for (int v = 0; v < nvec; ++v) {
@@ -301,6 +311,8 @@ int f2g_sigma_term(void* sb, int term, const double* C, double* sigma, void* str
         need(sb, "sigma");
         if (term < 0 || term > 5)
             throw Error(2, "term must be 0..5");
+        if (static_cast<SigmaBuilder*>(sb)->s->ndet && (!C || !sigma))
+            throw Error(2, "NULL vector");
         static_cast<SigmaBuilder*>(sb)->term(term, C, sigma, S(stream));
     });
 }
@@ -308,6 +320,7 @@ int f2g_sigma_term(void* sb, int term, const double* C, double* sigma, void* str
 int f2g_sigma_avg_build_time(void* sb, double* out) {
     return guard([&] {
         need(sb, "sigma");
+        need(out, "out");
         static_cast<SigmaBuilder*>(sb)->avg_build_time(out);
     });
 }
@@ -315,6 +328,8 @@ int f2g_sigma_avg_build_time(void* sb, double* out) {
 int f2g_sigma_det_energies(void* sb, double* out, void* stream) {
     return guard([&] {
         need(sb, "sigma");
+        if (static_cast<SigmaBuilder*>(sb)->s->ndet)
+            need(out, "out");
         static_cast<SigmaBuilder*>(sb)->det_energies(out, S(stream));
     });
 }
@@ -400,6 +415,12 @@ int f2g_csf_to_det(void* h, const double* csf, double* det, int nvec, void* stre
     return guard([&] {
         need(h, "spin adapter");
         auto* a = static_cast<SpinAdapter*>(h);
+        if (nvec < 0)
+            throw Error(2, "nvec must be >= 0");
+        if (nvec > 0 && a->ncsf > 0)
+            need(csf, "csf");
+        if (nvec > 0 && a->s->ndet > 0)
+            need(det, "det");
         for (int v0 = 0; v0 < nvec; v0 += 65535)
             a->csf_to_det(csf + v0 * a->ncsf, det + v0 * a->s->ndet, S(stream), std::min(65535, nvec - v0));
     });
@@ -409,6 +430,12 @@ int f2g_det_to_csf(void* h, const double* det, double* csf, int nvec, void* stre
     return guard([&] {
         need(h, "spin adapter");
         auto* a = static_cast<SpinAdapter*>(h);
+        if (nvec < 0)
+            throw Error(2, "nvec must be >= 0");
+        if (nvec > 0 && a->s->ndet > 0)
+            need(det, "det");
+        if (nvec > 0 && a->ncsf > 0)
+            need(csf, "csf");
         for (int v0 = 0; v0 < nvec; v0 += 65535)
             a->det_to_csf(det + v0 * a->s->ndet, csf + v0 * a->ncsf, S(stream), std::min(65535, nvec - v0));
     });
@@ -420,6 +447,8 @@ int f2g_hdiag_csf(void* sb, void* h, double* out, void* stream) {
         need(h, "spin adapter");
         auto* b = static_cast<SigmaBuilder*>(sb);
         auto* a = static_cast<SpinAdapter*>(h);
+        if (a->ncsf > 0)
+            need(out, "out");
         double* e = b->eDet.reserve(std::max<int64_t>(1, b->s->ndet));
         b->det_energies(e, S(stream));
         a->hdiag(e, out, S(stream));
@@ -431,6 +460,12 @@ int f2g_csf_matrix(void* sb, void* h, const int64_t* idx, int m, double* out) {
         need(sb, "sigma");
         need(h, "spin adapter");
         auto* a = static_cast<SpinAdapter*>(h);
+        if (m < 0)
+            throw Error(2, "csf_matrix: negative size");
+        if (m > 0) {
+            need(idx, "idx");
+            need(out, "out");
+        }
         for (int i = 0; i < m; ++i)
             if (idx[i] < 0 || idx[i] >= a->ncsf)
                 throw Error(2, "CSF index out of range");
@@ -463,7 +498,17 @@ int64_t f2g_dav_scratch_size(int64_t n) { return dav_scratch_size(n); }
 
 int f2g_dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n, double* out,
                  double* scratch, void* stream) {
-    return guard([&] { dav_dots(A, na, lda, B, nb, ldb, n, out, scratch, S(stream)); });
+    return guard([&] {
+        if (na < 0 || nb < 0 || n < 0)
+            throw Error(2, "dots: negative size");
+        if (na > 0 && nb > 0) {
+            need(A, "A");
+            need(B, "B");
+            need(out, "out");
+            need(scratch, "scratch");
+        }
+        dav_dots(A, na, lda, B, nb, ldb, n, out, scratch, S(stream));
+    });
 }
 
 int f2g_dav_dots_noalloc(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n,
@@ -473,19 +518,53 @@ int f2g_dav_dots_noalloc(const double* A, int na, int64_t lda, const double* B, 
 
 int f2g_dav_lincomb(const double* X, int nx, int64_t ldx, const double* coef, int ny, double* Y, int64_t ldy,
                     double beta, int64_t n, void* stream) {
-    return guard([&] { dav_lincomb(X, nx, ldx, coef, ny, Y, ldy, beta, n, S(stream)); });
+    return guard([&] {
+        if (nx < 0 || ny < 0 || n < 0)
+            throw Error(2, "lincomb: negative size");
+        if (ny > 0 && n > 0) {
+            need(Y, "Y");
+            if (nx > 0) {
+                need(X, "X");
+                need(coef, "coef");
+            }
+        }
+        dav_lincomb(X, nx, ldx, coef, ny, Y, ldy, beta, n, S(stream));
+    });
 }
 
 int f2g_dav_residual(const double* B, const double* Sv, int m, int64_t ld, const double* alpha, const double* lam,
                      int nroot, const double* hdiag, int64_t n, double thresh, double* R, int64_t ldr, double* norms2,
                      double* scratch, void* stream) {
     return guard([&] {
+        if (m < 0 || nroot < 0 || n < 0)
+            throw Error(2, "residual: negative size");
+        if (nroot > 0) {
+            need(alpha, "alpha");
+            need(lam, "lam");
+            need(norms2, "norms2");
+            need(scratch, "scratch");
+            if (n > 0) {
+                need(B, "B");
+                need(Sv, "S");
+                need(hdiag, "hdiag");
+                need(R, "R");
+            }
+        }
         dav_residual(B, Sv, m, ld, alpha, lam, nroot, hdiag, n, thresh, R, ldr, norms2, scratch, S(stream));
     });
 }
 
 int f2g_dav_eigh(int m, const double* G, double* evals, double* evecs, void* stream) {
-    return guard([&] { dav_eigh(m, G, evals, evecs, S(stream)); });
+    return guard([&] {
+        if (m < 0)
+            throw Error(2, "eigh: negative size");
+        if (m > 0) {
+            need(G, "G");
+            need(evals, "evals");
+            need(evecs, "evecs");
+        }
+        dav_eigh(m, G, evals, evecs, S(stream));
+    });
 }
 
 int f2g_dav_gs_append(double* B, int64_t ld, int cap, int m0, const double* R, int64_t ldr, int ncand, int64_t n,
