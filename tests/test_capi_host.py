@@ -109,3 +109,27 @@ def test_new_entry_points_validate_handles_without_gpu(libpath):
     assert L.f2g_sigma_set_max_blocks(None, 4) == 2
     assert L.f2g_sigma_set_tensor_cores(None, 1, None) == 2
     assert L.f2g_dav_gs_append(None, 10, 4, 0, None, 10, 1, 10, 1e-8, 1e-12, 1, 1, None, None) == 2
+
+
+def test_davidson_and_sigma_entry_points_validate_sizes_without_gpu(libpath):
+    """Negative sizes and NULL buffers of the Davidson vector operations and of the sigma, CSF and
+    RDM entry points give status 2 (ValueError) before any device work."""
+    from forte2_gb300._lib import lib
+
+    L = lib()
+    assert L.f2g_dav_dots(None, -1, 8, None, 2, 8, 8, None, None, None) == 2
+    assert L.f2g_dav_dots(None, 2, 8, None, 2, 8, 8, None, None, None) == 2  # NULL operands
+    assert L.f2g_dav_lincomb(None, 2, 8, None, -3, None, 8, 0.0, 8, None) == 2
+    assert L.f2g_dav_lincomb(None, 2, 8, None, 2, None, 8, 0.0, 8, None) == 2
+    assert L.f2g_dav_residual(None, None, 2, 8, None, None, -1, None, 8, 1e-8, None, 8, None, None, None) == 2
+    assert L.f2g_dav_residual(None, None, 2, 8, None, None, 1, None, 8, 1e-8, None, 8, None, None, None) == 2
+    assert L.f2g_dav_eigh(-1, None, None, None, None) == 2
+    assert L.f2g_dav_eigh(3, None, None, None, None) == 2
+    for f in ("f2g_sigma_apply", "f2g_sigma_term", "f2g_sigma_det_energies", "f2g_sigma_avg_build_time"):
+        assert getattr(L, f) is not None
+    assert L.f2g_sigma_apply(None, None, None, 1, None) == 2
+    assert L.f2g_sigma_apply_host(None, None, None, 1) == 2
+    assert L.f2g_sigma_avg_build_time(None, None) == 2
+    assert L.f2g_csf_to_det(None, None, None, 1, None) == 2
+    assert L.f2g_det_to_csf(None, None, None, 1, None) == 2
+    assert L.f2g_sigma_rdm(None, 0, None, None, None, None) == 2
