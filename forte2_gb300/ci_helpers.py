@@ -298,13 +298,14 @@ class CISigmaBuilder:
         check(lib().f2g_sigma_set_memory(self.h, int(mb)))
 
     def set_tensor_cores(self, on=True):
-        """FP32 precision: opposite-spin term on the tensor cores (3xTF32). Returns whether this
-        space supports it (else the CUDA-core kernel runs). No counterpart in the reference."""
+        """FP32 precision: opposite-spin term on the tensor cores (split-FP16 products, FP32
+        accumulation, exact fixed-point row sums). Returns whether this space supports it (else the
+        CUDA-core kernel runs). No counterpart in the reference."""
         avail = np.zeros(1, dtype=np.int32)
         check(lib().f2g_sigma_set_tensor_cores(self.h, int(bool(on)), avail.ctypes.data))
         return bool(avail[0])
 
-    _VARIANTS = {"tensor_cores": 0, "narrow_same_spin": 1, "persistent_opposite": 2}
+    _VARIANTS = {"tensor_cores": 0, "narrow_same_spin": 1, "persistent_opposite": 2, "tc_wait_limit": 3}
 
     def set_variant(self, name, value):
         """Select a kernel variant with identical results (see forte2_gb300.autotune)."""

@@ -223,8 +223,16 @@ int f2g_sigma_set_variant(void* sb, int which, int value) {
             b->spmm_narrow = value != 0;
         else if (which == 2)
             b->opposite_persistent = value != 0;
-        else
-            throw Error(2, "variant must be 0 (tensor cores), 1 (narrow same-spin tiles) or 2 (persistent opposite grid)");
+        else if (which == 3) {
+            // polls per bounded wait of the tensor-core kernel (0 = the default limit); also clears
+            // its error flag. A small limit makes the waits give up: the error path, for tests.
+            if (value < 0)
+                throw Error(2, "tensor-core wait limit must be >= 0");
+            b->tc_poll_limit = value;
+            F2G_CUDA(cudaMemset(b->tc_err.get(), 0, sizeof(int)));
+        } else
+            throw Error(2, "variant must be 0 (tensor cores), 1 (narrow same-spin tiles), 2 (persistent opposite "
+                           "grid) or 3 (tensor-core wait limit)");
     });
 }
 
@@ -513,7 +521,16 @@ int f2g_dav_dots(const double* A, int na, int64_t lda, const double* B, int nb, 
 
 int f2g_dav_dots_noalloc(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n,
                          double* out, void* stream) {
-    return guard([&] { dav_dots_noalloc(A, na, lda, B, nb, ldb, n, out, S(stream)); });
+    return guard([&] {
+        if (na < 0 || nb < 0 || n < 0)
+            throw Error(2, "dots_noalloc: negative size");
+        if (na > 0 && nb > 0) {
+            need(A, "A");
+            need(B, "B");
+            need(out, "out");
+        }
+        dav_dots_noalloc(A, na, lda, B, nb, ldb, n, out, S(stream));
+    });
 }
 
 int f2g_dav_lincomb(const double* X, int nx, int64_t ldx, const double* coef, int ny, double* Y, int64_t ldy,

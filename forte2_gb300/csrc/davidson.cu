@@ -315,6 +315,9 @@ double* g_static_ptr[128] = {};
 // Device address of g_static_partials on the current device. In host code the array's name is only
 // a host-side stand-in, so the address is looked up once per device with that device current; the
 // first call on a device therefore does this set-up (it should come before any stream capture).
+// The address is kept for the life of the process: a cudaDeviceReset (or any reset of the device's
+// primary context) unloads the module that holds the array, so this entry point must not be called
+// again after one.
 static double* static_partials() {
     int dev = 0;
     F2G_CUDA(cudaGetDevice(&dev));

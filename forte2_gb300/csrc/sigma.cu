@@ -19,11 +19,13 @@
 //   shared memory. For each p in Ja (Ka = Ja - p) it stages the integral slice V[p, r, q, s]
 //   (q unoccupied in Ka) and, per beta 1-hole string Kb, gathers D[q][s] = sgn C(Ka+q, Kb+s),
 //   forms E[r] = sum_{q,s} V[p,r,q,s] D[q][s] for the (n - nb + 1) r unoccupied in Kb and adds
-//   sgn E[r] to sigma(Ja, Kb+r) with shared-memory atomics. Only the non-zero rows of the
-//   reference's D([qs],[Ka Kb]) are touched, so the FLOP count is 2 N1a N1b (ma mb)^2 with
-//   ma = n-na+1, mb = n-nb+1 (10x fewer than the dense n^2 x n^2 product). Owner-writes over
-//   Ja rows: no global atomics.
+//   sgn E[r] to sigma(Ja, Kb+r) in one phase per orbital r (a_r^+ is one-to-one on the Kb of a
+//   round, so the adds of a phase never collide). Only the non-zero rows of the reference's
+//   D([qs],[Ka Kb]) are touched, so the FLOP count is 2 N1a N1b (ma mb)^2 with ma = n-na+1,
+//   mb = n-nb+1 (10x fewer than the dense n^2 x n^2 product). Owner-writes over Ja rows and no
+//   atomics: every sigma element is summed in a fixed order (bitwise reproducible).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "sigma.cuh"
@@ -210,7 +212,7 @@ __global__ void k_scale(int64_t n, double a, const double* in, double* out) {
 
 // ---- opposite spin ----------------------------------------------------------------------------
 // One CTA per output alpha string Ja. MB bounds mb = n - nb + 1 (beta holes per 1-hole string).
-// SMROW: sigma(Ja,:) lives in shared memory; otherwise updates go to global memory atomically.
+// SMROW: sigma(Ja,:) lives in shared memory; otherwise the phased updates go to global memory.
 template <typename T, int MB, bool SMROW>
 __global__ void __launch_bounds__(512, 1)
     k_opposite(int64_t N0a, int n, int na, int N0b, int64_t N1b, int ma, int mb, const uint32_t* __restrict__ down_a,
@@ -249,17 +251,20 @@ __global__ void __launch_bounds__(512, 1)
             vs[idx] = V[(((size_t)p * n + r) * n + q) * n + s];
         }
         __syncthreads();
-        for (int64_t Kb = threadIdx.x; Kb < N1b; Kb += blockDim.x) {
+        // every thread runs the same number of Kb rounds: the scatter below has barriers
+        for (int64_t Kb0 = 0; Kb0 < N1b; Kb0 += blockDim.x) {
+            const int64_t Kb = Kb0 + threadIdx.x;
+            const bool active = Kb < N1b;
             uint32_t ub[MB];
             int so[MB];
             T acc[MB];
 #pragma unroll
             for (int si = 0; si < MB; ++si) {
-                ub[si] = si < mb ? __ldg(up_b + Kb * mb + si) : 0u;
-                so[si] = e_orb(ub[si]);
+                ub[si] = (active && si < mb) ? __ldg(up_b + Kb * mb + si) : 0u;
+                so[si] = (active && si < mb) ? e_orb(ub[si]) : -1;
                 acc[si] = T(0);
             }
-            for (int qi = 0; qi < ma; ++qi) {
+            for (int qi = 0; active && qi < ma; ++qi) {
                 const uint32_t eq = ua[qi];
                 const T* crow = C + (int64_t)e_addr(eq) * N0b;
                 const int negq = e_neg(eq);
@@ -287,14 +292,19 @@ __global__ void __launch_bounds__(512, 1)
                     }
                 }
             }
+            // Owner-ordered scatter, one phase per created orbital r: within a phase Kb -> Kb + r is
+            // one-to-one, so plain read-add-writes never collide, and every sigma element receives
+            // its contributions in the fixed order (Kb round, r): the result is bitwise the same
+            // for every launch shape and batch.
+            for (int r = 0; r < n; ++r) {
+                __syncthreads();
 #pragma unroll
-            for (int ri = 0; ri < MB; ++ri) {
-                if (ri < mb) {
-                    const T x = (negp ^ e_neg(ub[ri])) ? -acc[ri] : acc[ri];
-                    if (SMROW)
-                        atomicAdd(row + e_addr(ub[ri]), x);
-                    else
-                        atomicAdd(srow + e_addr(ub[ri]), x);
+                for (int ri = 0; ri < MB; ++ri) {
+                    if (so[ri] == r) {
+                        const T x = (negp ^ e_neg(ub[ri])) ? -acc[ri] : acc[ri];
+                        T* dst = (SMROW ? row : srow) + e_addr(ub[ri]);
+                        *dst += x;
+                    }
                 }
             }
         }
@@ -366,8 +376,17 @@ static int sm_count() {
 size_t opposite_tc_smem(int N0b);
 bool opposite_tc_supported(const CIStrings* s);
 void build_beta_exc(const CIStrings* s, DevBuf<uint32_t>& exc, cudaStream_t st);
-void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, const float* C, float* sig,
-                        int* err, int max_ctas, cudaStream_t st, int nvec);
+int opposite_tc_v_exponent(float vmax);
+void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, int eb, const float* C, float* sig,
+                        unsigned int* cmax, int* err, long long poll_limit, int max_ctas, cudaStream_t st, int nvec);
+
+// scale exponent of the FP32 integrals for the tensor-core kernel's FP16 split (from the host copy)
+static int v_exponent(const std::vector<double>& V) {
+    float m = 0.0f;
+    for (double x : V)
+        m = std::max(m, std::fabs((float)x));
+    return opposite_tc_v_exponent(m);
+}
 
 SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const double* V_, int ll)
     : s(s_), n(s_->norb), log_level(ll) {
@@ -376,8 +395,10 @@ SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const dou
             F2G_CUDA(cudaEventCreate(&e));
     tc_err.reserve(1);
     F2G_CUDA(cudaMemsetAsync(tc_err.get(), 0, sizeof(int), 0));
-    if (opposite_tc_supported(s))
+    if (opposite_tc_supported(s)) {
         build_beta_exc(s, beta_exc, 0); // ordered before set_hamiltonian's wait on the legacy stream
+        tc_cmax.reserve(2 * 65536);      // one word per vector of a batch (grid y <= 65535), two sets
+    }
     set_hamiltonian(E_, H_, V_);
 }
 
@@ -431,6 +452,7 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
     E = E_;
     H.assign(H_, H_ + (size_t)n * n);
     V.assign(V_, V_ + (size_t)n * n * n * n);
+    tc_eb = v_exponent(V);
     dH.reserve(std::max<size_t>(1, H.size()));
     dV.reserve(std::max<size_t>(1, V.size()));
     if (!H.empty())
@@ -458,6 +480,7 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
     E = E_;
     H.assign(H_, H_ + (size_t)n * n);
     V.assign(V_, V_ + (size_t)n * n * n * n);
+    tc_eb = v_exponent(V);
     dH.reserve(std::max<size_t>(1, H.size()));
     dV.reserve(std::max<size_t>(1, V.size()));
     fV.reserve(std::max<size_t>(1, V.size()));
@@ -520,7 +543,7 @@ void SigmaBuilder::apply_f32(const float* C, float* S, cudaStream_t st, int nvec
     }
     if (timed)
         timer_begin();
-    run<float>(C, S, st, 7, timed, nvec, ct, tt);
+    run<float>(C, S, st, 7, timed, nvec, ct, tt, graph);
     if (timed)
         timer_end(nvec);
 }
@@ -669,7 +692,8 @@ void transpose_f64(int64_t rows, int64_t cols, const double* in, double* out, cu
 // Ct_, Tt_: transposition scratch of nvec * ndet elements.
 
 template <typename T>
-void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_) {
+void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_,
+                       bool graph) {
     const int64_t NA = s->a.N0, NB = s->b.N0, nd = NA * NB;
     g_opposite_max_ctas = max_ctas > 0 ? max_ctas : (opposite_persistent ? sm_count() : 0);
     g_spmm_narrow = spmm_narrow;
@@ -706,7 +730,11 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
         bool done = false;
         if constexpr (sizeof(T) == 4) {
             if (use_tc && tensor_cores_available()) {
-                launch_opposite_tc(s, beta_exc.get(), Vt, C, sig, tc_err.get(), max_ctas, st, nvec);
+                // graph launches use their own half of the scale scratch, so a captured solve and a
+                // direct call on the same builder never share it
+                unsigned int* cmax = tc_cmax.get() + (graph ? 65536 : 0);
+                launch_opposite_tc(s, beta_exc.get(), Vt, tc_eb, C, sig, cmax, tc_err.get(), tc_poll_limit, max_ctas,
+                                   st, nvec);
                 done = true;
             }
         }
@@ -812,7 +840,7 @@ void SigmaBuilder::apply_batch(const double* C, double* sigma, cudaStream_t st, 
     if (precision == kFP64) {
         double* ct = graph ? gCt.get() : Ct.reserve(tot);
         double* tt = graph ? gTt.get() : Tt.reserve(tot);
-        run<double>(C, sigma, st, 7, timed, nvec, ct, tt);
+        run<double>(C, sigma, st, 7, timed, nvec, ct, tt, graph);
     } else {
         float* c = graph ? gfC.get() : fC.reserve(tot);
         float* sg = graph ? gfS.get() : fS.reserve(tot);
@@ -820,7 +848,7 @@ void SigmaBuilder::apply_batch(const double* C, double* sigma, cudaStream_t st, 
         float* tt = graph ? gfTt.get() : fTt.reserve(tot);
         k_convert<double, float><<<1024, 256, 0, st>>>((int64_t)tot, C, c);
         F2G_LAUNCH("k_convert C");
-        run<float>(c, sg, st, 7, timed, nvec, ct, tt);
+        run<float>(c, sg, st, 7, timed, nvec, ct, tt, graph);
         k_convert<float, double><<<1024, 256, 0, st>>>((int64_t)tot, sg, sigma);
         F2G_LAUNCH("k_convert sigma");
     }

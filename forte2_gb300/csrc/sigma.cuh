@@ -39,10 +39,14 @@ struct SigmaBuilder {
     // SM looping over the alpha strings; same-spin kernel with half the columns per thread
     bool opposite_persistent = false;
     int spmm_narrow = 0;
-    // FP32 opposite-spin term on the tensor cores (3xTF32, opposite_tc.cu) when the space allows it
+    // FP32 opposite-spin term on the tensor cores (split-FP16 products, opposite_tc.cu) when the
+    // space allows it
     bool use_tc = true;
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
     DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
+    DevBuf<unsigned int> tc_cmax; // per-vector largest |C| of a tensor-core launch (its operand scale)
+    int tc_eb = 0;             // power-of-two scale of the FP32 integrals in the FP16 split
+    long long tc_poll_limit = 0; // polls per bounded wait in the tensor-core kernel (0: the default)
     bool tensor_cores_available() const;
     int tc_error() const;
     int log_level = 3;
@@ -105,7 +109,7 @@ struct SigmaBuilder {
   private:
     void build_string_hamiltonian(int spin, StringHamiltonian& sh, bool with_e0, cudaStream_t st);
     template <typename T>
-    void run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_);
+    void run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_, bool graph);
     void apply_batch(const double* C, double* sigma, cudaStream_t st, int nvec, bool timed, bool graph);
 };
 

@@ -65,14 +65,18 @@ int f2g_sigma_set_precision(void* sigma, int precision);
  * default). A capped build loops over the alpha strings and leaves the other SMs to concurrent
  * work, e.g. small latency-bound solves beside a large one. Same results. No reference counterpart. */
 int f2g_sigma_set_max_blocks(void* sigma, int max_blocks);
-/* FP32 precision only: compute the opposite-spin term on the tensor cores (tcgen05, operands split
- * into two TF32 parts, three products accumulated in FP32: FP32-level accuracy). *available = 1
- * if this space supports it (n <= 16 orbitals, na (n - na + 1) <= 72, one sigma row of beta
- * strings in shared memory); otherwise the CUDA-core kernel is used. No reference counterpart. */
+/* FP32 precision only: compute the opposite-spin term on the tensor cores (tcgen05, operands scaled
+ * by powers of two and split into two FP16 parts, three products accumulated in FP32: FP32-level
+ * accuracy; the sigma row is summed in exact 64-bit fixed point, so results are bitwise
+ * reproducible). *available = 1 if this space supports it (n <= 16 orbitals, na (n - na + 1) <= 72,
+ * nb (n - nb + 1) <= 72, one sigma row of beta strings in shared memory); otherwise the CUDA-core
+ * kernel is used. No reference counterpart. */
 int f2g_sigma_set_tensor_cores(void* sigma, int on, int* available);
 /* Kernel variants with identical results, for the autotuner: which = 0 opposite spin on the tensor
  * cores (FP32 only), 1 same-spin kernel with half the columns per thread, 2 opposite-spin grid of
- * one thread block per SM. No reference counterpart. */
+ * one thread block per SM. which = 3 sets the polls per bounded wait of the tensor-core kernel
+ * (0 = the default, about a second) and clears its error flag; a small value makes the waits give
+ * up, which exercises the error path. No reference counterpart. */
 int f2g_sigma_set_variant(void* sigma, int which, int value);
 /* 1 if a tensor-core build gave up waiting for its matrix operations (results invalid). */
 int f2g_sigma_tc_error(void* sigma, int* out);
@@ -162,7 +166,9 @@ int f2g_dav_dots(const double* dev_A, int na, int64_t lda, const double* dev_B, 
  * Limit: na * nb <= 256 vector pairs per call (status 2 beyond), na, nb <= 64, any n. The first
  * call on each device looks up the array's device address (cudaGetSymbolAddress) with that device
  * current; make that first call before any stream capture. Every call reuses the same array, so
- * calls that overlap on the GPU (other streams, other host threads) race and must be serialised. */
+ * calls that overlap on the GPU (other streams, other host threads) race and must be serialised.
+ * The looked-up address is kept for the process: do not call this again after a cudaDeviceReset.
+ * NULL operands with na * nb > 0 and negative sizes return status 2 before any device work. */
 int f2g_dav_dots_noalloc(const double* dev_A, int na, int64_t lda, const double* dev_B, int nb, int64_t ldb,
                          int64_t n, double* dev_out, void* stream);
 /* Y_j = beta Y_j + sum_i coef[i * ny + j] X_i (Y must not alias X) */

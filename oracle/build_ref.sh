@@ -2,11 +2,15 @@
 # Test infrastructure (oracle only): compile the reference's own hot-path C++ sources, where
 # they lie in the reference checkout, into oracle/_ref/libforte2_ref.so together with the
 # nanobind/sparse shims (oracle/ref_shim), the BLAS bridge and the C-ABI wrapper ref_capi.cc.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (or set FORTE2_REFERENCE_ROOT)
 # Nothing is copied out of the reference tree; outputs go only to oracle/_ref/.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${FORTE2_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+    echo "usage: $0 REFERENCE_ROOT (the forte2 checkout; or set FORTE2_REFERENCE_ROOT)" >&2
+    exit 2
+fi
 SRC="$REF/forte2"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC/ci/ci_sigma_builder.cc" ]; then

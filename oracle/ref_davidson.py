@@ -41,7 +41,7 @@ class _Table:
         return ""
 
 
-def load(reference_root: str = "/root/reference"):
+def load(reference_root: str):
     logger = types.ModuleType("forte2.helpers.logger")
     logger.log = lambda *a, **k: None
     logger.log_warning = lambda *a, **k: None

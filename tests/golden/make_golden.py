@@ -1,8 +1,8 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run where the reference sources are checked out, with their root in FORTE2_REFERENCE_ROOT:
 
-    oracle/build_ref.sh /root/reference
+    oracle/build_ref.sh "$FORTE2_REFERENCE_ROOT"
     python tests/golden/make_golden.py [--big]
 
 Everything here comes from the reference's own code: its C++ CIStrings / CISigmaBuilder
@@ -319,7 +319,9 @@ def gen_davidson(out, ref_root):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("FORTE2_REFERENCE_ROOT"),
+                    required=os.environ.get("FORTE2_REFERENCE_ROOT") is None,
+                    help="root of the forte2 checkout (or set FORTE2_REFERENCE_ROOT)")
     ap.add_argument("--big", action="store_true", help="also the CAS(16,16) sigma checksum")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()

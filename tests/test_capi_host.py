@@ -119,6 +119,10 @@ def test_davidson_and_sigma_entry_points_validate_sizes_without_gpu(libpath):
     L = lib()
     assert L.f2g_dav_dots(None, -1, 8, None, 2, 8, 8, None, None, None) == 2
     assert L.f2g_dav_dots(None, 2, 8, None, 2, 8, 8, None, None, None) == 2  # NULL operands
+    # the allocation-free variant validates the same way, before it touches the device
+    assert L.f2g_dav_dots_noalloc(None, -1, 8, None, 2, 8, 8, None, None) == 2
+    assert L.f2g_dav_dots_noalloc(None, 2, 8, None, 2, 8, 8, None, None) == 2
+    assert b"A is NULL" in L.f2g_last_error()
     assert L.f2g_dav_lincomb(None, 2, 8, None, -3, None, 8, 0.0, 8, None) == 2
     assert L.f2g_dav_lincomb(None, 2, 8, None, 2, None, 8, 0.0, 8, None) == 2
     assert L.f2g_dav_residual(None, None, 2, 8, None, None, -1, None, 8, 1e-8, None, 8, None, None, None) == 2

@@ -265,8 +265,8 @@ def test_capped_opposite_grid_same_sigma(cuda, golden_sigma):
 
 @pytest.mark.parametrize("na,nb,n", [(3, 3, 6), (4, 3, 7), (2, 5, 8), (5, 5, 10), (7, 7, 14)])
 def test_fp32_tensor_core_opposite_spin(cuda, na, nb, n):
-    """FP32 sigma with the opposite-spin term on the tensor cores (3xTF32) agrees with the FP64
-    sigma to FP32 accuracy, and with the CUDA-core FP32 kernel."""
+    """FP32 sigma with the opposite-spin term on the tensor cores (split-FP16 products) agrees with
+    the FP64 sigma to FP32 accuracy, and with the CUDA-core FP32 kernel."""
     torch = cuda
     from forte2_gb300.ci_helpers import CISigmaBuilder
 
@@ -288,3 +288,56 @@ def test_fp32_tensor_core_opposite_spin(cuda, na, nb, n):
         e_tc = rel(tc[i].cpu().numpy(), ref[i].cpu().numpy())
         e_cc = rel(cc[i].cpu().numpy(), ref[i].cpu().numpy())
         assert e_tc < 2e-6 and e_tc < 3 * e_cc + 1e-7
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sigma_is_bitwise_reproducible(cuda, precision):
+    """The same vectors give bitwise-identical sigma across repeated calls, capped grids and batch
+    shapes: the opposite-spin kernels sum every element in a fixed order (FP64: one write phase
+    per created orbital; FP32 tensor cores: exact 64-bit fixed-point row sums)."""
+    torch = cuda
+    s, sb, _ = builder(6, 6, 12, 77)
+    sb.set_precision(precision)
+    if precision == "fp32":
+        assert sb.set_tensor_cores(True) is True
+    X = torch.as_tensor(np.stack([random_ci_vector(s.ndet, 31), random_ci_vector(s.ndet, 32)]), device="cuda")
+    first = torch.empty_like(X)
+    sb.Hamiltonian(X, first)
+    for _ in range(4):
+        again = torch.empty_like(X)
+        sb.Hamiltonian(X, again)
+        assert torch.equal(again, first)
+    for cap in (5, 37, 152, 0):
+        sb.set_max_blocks(cap)
+        capped = torch.empty_like(X)
+        sb.Hamiltonian(X, capped)
+        assert torch.equal(capped, first), cap
+    for i in range(2):
+        single = torch.empty_like(X[i])
+        sb.Hamiltonian(X[i].contiguous(), single)
+        assert torch.equal(single, first[i])
+    if precision == "fp32":
+        assert sb.tensor_core_error() == 0
+
+
+def test_tensor_core_wait_limit_reports_error_and_recovers(cuda):
+    """A bounded wait that gives up sets the tensor-core error flag (the kernel then drains its
+    committed MMAs and releases tensor memory); the context stays usable and the next build with
+    the default limit is correct."""
+    torch = cuda
+    s, sb, _ = builder(5, 5, 10, 1000)
+    dc = torch.as_tensor(random_ci_vector(s.ndet, 110), device="cuda")
+    ref = torch.empty_like(dc)
+    sb.Hamiltonian(dc, ref)
+    sb.set_precision("fp32")
+    assert sb.set_tensor_cores(True) is True
+    sb.set_variant("tc_wait_limit", 1)  # one poll: the first wait gives up
+    out = torch.empty_like(dc)
+    sb.Hamiltonian(dc, out)
+    torch.cuda.synchronize()
+    assert sb.tensor_core_error() == 1
+    sb.set_variant("tc_wait_limit", 0)  # default limit; clears the flag
+    assert sb.tensor_core_error() == 0
+    sb.Hamiltonian(dc, out)
+    assert sb.tensor_core_error() == 0
+    assert rel(out.cpu().numpy(), ref.cpu().numpy()) < 2e-6
