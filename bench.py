@@ -37,7 +37,7 @@ from forte2_gb300.synthetic import cas_dims, hz_flops, make_integrals, random_ci
 
 NORB, NEL = 16, 16
 ISEED, CSEED = 3000, 114
-FP64_PEAK_TFLOPS = 1.098  # measured torch.matmul FP64 8192^3 on this GB300 pool
+FP64_DGEMM_TFLOPS = 1.098  # torch.matmul FP64 8192^3 (cuBLAS DGEMM) on this GB300 pool, for context
 FP32_PEAK_TFLOPS = 69.70  # measured torch.matmul FP32 (no TF32) 8192^3
 METRIC = "CAS(16,16) sigma-builds/s"
 
@@ -65,6 +65,11 @@ def parse():
     ap.add_argument("--e-tol", type=float, default=1e-10)
     ap.add_argument("--precisions", default="fp64,mixed", help="davidson mode: which solves to run")
     ap.add_argument("--maxiter", type=int, default=400, help="davidson mode: iteration limit")
+    ap.add_argument("--basis-per-root", type=int, default=0, help="davidson mode: subspace vectors per root "
+                                                                  "(0: the reference's default, FP64)")
+    ap.add_argument("--collapse-per-root", type=int, default=0)
+    ap.add_argument("--no-davidson", action="store_true",
+                    help="sigma mode: skip the Davidson time-to-solution runs of the default line")
     return ap.parse_args()
 
 
@@ -112,6 +117,31 @@ class Clocks:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_fma_peak(reps=3):
+    """FP64 FMA issue rate of this GPU from the library's own probe (k_probe_dfma: 8 independent
+    DFMA chains per thread, 4 blocks of 256 threads per SM), timed with CUDA events on the
+    launching stream after one warm-up launch; the best of `reps` launches (burst), in TFLOP/s."""
+    import torch
+
+    from forte2_gb300._lib import check, lib, stream_handle
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    blocks, threads, iters = 4 * sms, 256, 1 << 16
+    out = torch.empty(blocks, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    check(lib().f2g_probe_dfma(blocks, threads, iters, out.data_ptr(), stream_handle()))
+    best = 0.0
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        check(lib().f2g_probe_dfma(blocks, threads, iters, out.data_ptr(), stream_handle()))
+        e1.record(st)
+        torch.cuda.synchronize()
+        best = max(best, 16.0 * blocks * threads * iters / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    assert bool(torch.isfinite(out).all())
+    return best
 
 
 def cpu_cores():
@@ -231,6 +261,7 @@ def run_gb300(a):
     sb.reset_build_times()
     clocks = Clocks(local)
     clocks.start()
+    fp64_peak = fp64_fma_peak()  # roofline denominator, measured under the same clock sampling
     barrier(dist)
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -281,6 +312,9 @@ def run_gb300(a):
         mt = sb.avg_build_time()
         mixed_terms = {"total": 1e3 * mt[0], "aabb": 1e3 * mt[1], "aaaa_h1a_h0": 1e3 * mt[2], "bbbb_h1b": 1e3 * mt[3]}
         sb.set_precision("fp64")
+    davidson = None
+    if rank == 0 and world == 1 and not a.no_davidson and a.norb == NORB:
+        davidson = davidson_acceptance()
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         v, sample, cores = cpu_baseline(a.norb, a.cpu_seconds, na, nb, ints, c_host)
@@ -298,17 +332,26 @@ def run_gb300(a):
                     "d2h_bytes_per_step": 8 * ndet},
             "gpu_launches": 5 * a.steps,
             "roofline": {"bound": "compute", "pipe": "fp64", "kernel": "k_opposite (opposite-spin sigma)",
-                         "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                         "frac": achieved / FP64_PEAK_TFLOPS, "traffic": opposite_traffic(a.norb, na, nb),
+                         "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp64_peak, "traffic": opposite_traffic(a.norb, na, nb),
                          "traffic_source": "dram read+write per gathered C element of the ncu capture at "
                                            "CAS(15e,15o) (profiles/k_opposite_fp64_cas15.md: 5.04 GB for "
                                            "2.09e10 elements), times this launch's gathered elements",
-                         "peak_source": "measured FP64 DGEMM, profiles/gb300_gemm_peaks.md",
-                         "flops_per_launch": f_sp["ab"], "launch_ms": 1e3 * t_ab},
+                         "peak_source": "measured in this run: the library's DFMA issue-rate probe "
+                                        "(k_probe_dfma, best of 3 launches, CUDA events)",
+                         "fp64_dgemm_tflops": FP64_DGEMM_TFLOPS, "frac_of_dgemm": achieved / FP64_DGEMM_TFLOPS,
+                         "flops_per_launch": f_sp["ab"], "launch_ms": 1e3 * t_ab,
+                         # the reference's dense HZ product counts n^2 x n^2 blocks whose D rows are
+                         # mostly zero; the kernel skips exactly those (same sigma to 1e-12)
+                         "dense_hz_flops_per_launch": f_hz["ab"],
+                         "dense_hz_equivalent_tflops": f_hz["ab"] / t_ab / 1e12,
+                         "algorithmic_bytes": 24 * ndet,
+                         "traffic_over_algorithmic": opposite_traffic(a.norb, na, nb) / (24 * ndet)},
             "terms_ms": {"total": 1e3 * tot, "aabb": 1e3 * t_ab, "aaaa_h1a_h0": 1e3 * t_aa, "bbbb_h1b": 1e3 * t_bb},
             "hz_dense_flops": f_hz, "sparse_flops": f_sp,
             "autotune": None if tuned is None else {p: {"choice": r["choice"], "ms": r["ms"], "default_ms": r["default_ms"]}
                                                     for p, r in tuned.items()},
+            "davidson": davidson,
             "mixed_fp32_sigma_builds_per_s": mixed,
             "mixed_fp32_terms_ms": mixed_terms,
             "clocks": clk,
@@ -320,8 +363,61 @@ def run_gb300(a):
         dist.destroy_process_group()
 
 
+def cpu_full_build(norb, na, nb, ints, c):
+    """One complete reference-algorithm sigma build (HZ, every K-block chunk) on all host cores,
+    after one small warm-up sample (thread pools, first-touch pages). Returns (seconds, cores)."""
+    from oracle.port import PortCI, build_port, open_blas
+
+    build_port()
+    cores = cpu_cores()
+    os.environ["ORACLE_THREADS"] = str(cores)
+    open_blas(threads=cores)
+    p = PortCI(norb, na, nb)
+    p.set_hamiltonian(ints.E, ints.H, ints.V)
+    p.set_fraction(0.001)
+    p.sigma(c)
+    p.set_fraction(1.0)
+    t = time.perf_counter()
+    p.sigma(c)
+    return time.perf_counter() - t, cores
+
+
+GPU_FP64_FIXTURE = os.path.join(ROOT, "tests", "golden", "davidson_gpu_fp64_cas16.json")
+
+
+def davidson_acceptance():
+    """Time to solution of the metric's Davidson part, run in the default line:
+
+    * CAS(16e,16o), 1 root, mixed precision, e_tol 1e-10: wall time and |E_mixed - E_FP64| against
+      the converged plain FP64 GPU solve of the same integrals (a committed GPU fixture: the CPU
+      oracle would need about a day here; FP64 parity is pinned at smaller sizes), and the FP64 /
+      mixed time ratio against that fixture's measured FP64 times;
+    * CAS(14e,14o), 3 roots, both precisions measured here (plain FP64 with the reference's
+      subspace), their energy differences and time ratio.
+    """
+    out = {}
+    m16 = casci_time_to_solution(16, 1, "mixed", 1e-10, 2000, ISEED)
+    out["cas16_1root_mixed"] = m16
+    if os.path.exists(GPU_FP64_FIXTURE):
+        with open(GPU_FP64_FIXTURE) as f:
+            fx = json.load(f)
+        out["cas16_fp64_fixture"] = {k: fx[k] for k in ("energies", "runs", "command") if k in fx}
+        out["cas16_abs_dE_mixed_vs_fp64"] = [abs(x - y) for x, y in zip(m16["energies"], fx["energies"])]
+        out["cas16_fp64_over_mixed_time"] = {name: r["seconds_total"] / m16["seconds_total"]
+                                             for name, r in fx["runs"].items()}
+    r14 = {prec: casci_time_to_solution(14, 3, prec, 1e-10, 1000, 1014) for prec in ("fp64", "mixed")}
+    out["cas14_3roots"] = r14
+    out["cas14_abs_dE_mixed_vs_fp64"] = [abs(x - y) for x, y in zip(r14["mixed"]["energies"], r14["fp64"]["energies"])]
+    out["cas14_fp64_over_mixed_time"] = r14["fp64"]["seconds_total"] / r14["mixed"]["seconds_total"]
+    return out
+
+
 def run_reference(a):
-    """Reference arm: the reference's HZ algorithm on the host cores (oracle port), rank 0 only."""
+    """Reference arm: the reference's HZ algorithm on the host cores (oracle port), rank 0 only.
+
+    The timed step is ONE complete sigma build (value = 1 / its time). The two-sample model of the
+    GPU arm's cpu_baseline is run beside it and its prediction and error are reported. A complete
+    build that the model puts above 240 s is not run; the model's rate is reported instead."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
@@ -329,23 +425,57 @@ def run_reference(a):
     na, nb, n0a, n0b, ndet = cas_dims(a.norb, a.norb, 0)
     ints = make_integrals(a.norb, ISEED)
     c = random_ci_vector(ndet, CSEED)
-    budget = max(2.0, min(a.cpu_seconds, 150.0 / max(1, a.steps + a.warmup)))
-    vals = []
-    sample = cores = None
-    for i in range(a.warmup + a.steps):
-        v, sample, cores = cpu_baseline(a.norb, budget, na, nb, ints, c)
-        if i >= a.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
+    model_rate, model_sample, cores = cpu_baseline(a.norb, min(a.cpu_seconds, 10.0), na, nb, ints, c)
+    model_s = 1.0 / model_rate
+    full_s = None
+    if model_s <= 240.0:
+        full_s, cores = cpu_full_build(a.norb, na, nb, ints, c)
+    value = 1.0 / full_s if full_s else model_rate
+    sample = (f"one complete CAS({2 * na}e,{a.norb}o) FP64 HZ sigma build ({full_s:.1f} s) on {cores} threads, "
+              f"after a 0.1% warm-up sample" if full_s else
+              f"model only (a complete build is predicted to take {model_s:.0f} s): " + model_sample)
     print(json.dumps({
         "impl": "reference", "metric": METRIC if a.norb == NORB else f"CAS({a.norb},{a.norb}) sigma-builds/s",
-        "value": value, "unit": "sigma-builds/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded integrals, naux=4n; seeded C)",
+        "value": value, "unit": "sigma-builds/s", "n_gpus": world, "steps": 1 if full_s else 0,
+        "requested_steps": a.steps, "warmup": 1, "ms_per_step": 1e3 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded integrals, naux=4n; seeded C)",
         "config": {"workload": f"CAS({a.norb}e,{a.norb}o) Ms=0 FP64 sigma build, {ndet} determinants", "ndet": ndet},
         "cpu_baseline": {"value": value, "unit": "sigma-builds/s", "cores": cores, "kind": "port", "sample": sample},
+        "measured_full_build_s": full_s,
+        "model": {"full_build_s": model_s, "sample": model_sample,
+                  "rel_error_vs_measured": (model_s - full_s) / full_s if full_s else None},
         "e2e": {"value": value, "unit": "sigma-builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def casci_time_to_solution(norb, nroot, prec, e_tol, maxiter, iseed, basis_per_root=None, collapse_per_root=None):
+    """One CASCI(n e, n o) Ms=0 singlet solve on the GPU, wall time from the solver's creation to
+    its energies on the host (strings, CSF set-up, guess, Davidson-Liu)."""
+    import torch
+
+    from forte2_gb300.ci import CASCISolver
+    from forte2_gb300.params import CIParams, DavidsonLiuParams
+
+    na, nb, _, _, _ = cas_dims(norb, norb, 0)
+    ints = make_integrals(norb, iseed)
+    dl = DavidsonLiuParams(e_tol=e_tol, maxiter=maxiter)
+    if basis_per_root:
+        dl = DavidsonLiuParams(e_tol=e_tol, maxiter=maxiter, basis_per_root=basis_per_root,
+                               collapse_per_root=collapse_per_root)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sol = CASCISolver(norb=norb, na=na, nb=nb, multiplicity=1, nroot=nroot, E=ints.E, H=ints.H, V=ints.V,
+                      ci_params=CIParams(precision=prec), davidson_liu_params=dl).run()
+    torch.cuda.synchronize()
+    r = {"seconds_total": time.perf_counter() - t0, "seconds_davidson": sol.timings["davidson"],
+         "seconds_setup": sol.timings.get("startup", 0.0) + sol.timings.get("setup", 0.0),
+         "converged": bool(sol.converged), "phases": sol.phases, "energies": [float(e) for e in sol.evals],
+         "ncsf": sol.basis_size, "subspace": [sol.eigensolver.basis_per_root, sol.eigensolver.collapse_per_root],
+         "iterations": sum(p[1] for p in sol.phases if not p[0].endswith("check"))}
+    r["seconds_per_iteration"] = r["seconds_davidson"] / max(1, r["iterations"])
+    del sol
+    torch.cuda.empty_cache()
+    return r
 
 
 def run_davidson(a):
@@ -353,29 +483,18 @@ def run_davidson(a):
     FP64 refinement), same seeded integrals; energies of the mixed run against the FP64 run."""
     import torch
 
-    from forte2_gb300.ci import CASCISolver
-    from forte2_gb300.params import CIParams, DavidsonLiuParams
-
     torch.cuda.set_device(0)
     na, nb, _, _, ndet = cas_dims(a.norb, a.norb, 0)
-    ints = make_integrals(a.norb, ISEED if a.norb == NORB else 1000 + a.norb)
     out = {"metric": f"CAS({a.norb},{a.norb}) Davidson time to solution", "unit": "s", "higher_is_better": False,
            "config": {"workload": f"CAS({a.norb}e,{a.norb}o) Ms=0 singlet, {a.nroot} root(s), e_tol {a.e_tol}, "
-                                  f"r_tol 1e-6", "ndet": ndet}}
+                                  f"r_tol 1e-6", "ndet": ndet,
+                      "subspace": "reference default" if not a.basis_per_root else
+                                  f"{a.basis_per_root}/{a.collapse_per_root} per root"}}
     res = {}
     for prec in a.precisions.split(","):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        sol = CASCISolver(norb=a.norb, na=na, nb=nb, multiplicity=1, nroot=a.nroot, E=ints.E, H=ints.H, V=ints.V,
-                          ci_params=CIParams(precision=prec),
-                          davidson_liu_params=DavidsonLiuParams(e_tol=a.e_tol, maxiter=a.maxiter)).run()
-        torch.cuda.synchronize()
-        res[prec] = {"seconds_total": time.perf_counter() - t0, "seconds_davidson": sol.timings["davidson"],
-                     "seconds_setup": sol.timings.get("startup", 0.0) + sol.timings.get("setup", 0.0),
-                     "converged": bool(sol.converged), "phases": sol.phases, "energies": [float(e) for e in sol.evals],
-                     "ncsf": sol.basis_size,
-                     "iterations": sum(p[1] for p in sol.phases if not p[0].endswith("check"))}
-        res[prec]["seconds_per_iteration"] = res[prec]["seconds_davidson"] / max(1, res[prec]["iterations"])
+        res[prec] = casci_time_to_solution(a.norb, a.nroot, prec, a.e_tol, a.maxiter,
+                                           ISEED if a.norb == NORB else 1000 + a.norb,
+                                           a.basis_per_root, a.collapse_per_root)
         print(json.dumps({"partial": prec, **res[prec]}), flush=True)  # each precision as soon as it is done
     out.update(res)
     if "fp64" in res and "mixed" in res:
@@ -455,6 +574,7 @@ def run_rdm(a):
         x1.record(st)
         torch.cuda.synchronize()
         ab_ms.append(x0.elapsed_time(x1))
+    fp64_peak = fp64_fma_peak()
     clk = clocks.stop()
     # algorithmic FP64 work of k_rdm_ab with bra = ket: alpha pair entries with u <= x times all
     # beta pair entries, one multiply-add each
@@ -480,9 +600,10 @@ def run_rdm(a):
                    "d2h_bytes_per_step": (n * n + n ** 4) * 8},
            "roofline": {"bound": "compute", "pipe": "fp64", "kernel": "k_rdm_ab (mixed-spin 2-RDM, with its mirror)",
                         "achieved": ab_flop / ab_s / 1e12,
-                        "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": ab_flop / ab_s / 1e12 / FP64_PEAK_TFLOPS,
+                        "peak": fp64_peak, "unit": "TFLOP/s", "frac": ab_flop / ab_s / 1e12 / fp64_peak,
                         "flop_per_launch": ab_flop, "ms": ab_s * 1e3, "traffic": None,
-                        "peak_source": "measured FP64 DGEMM, profiles/gb300_gemm_peaks.md"},
+                        "peak_source": "measured in this run: the library's DFMA issue-rate probe (k_probe_dfma)",
+                        "fp64_dgemm_tflops": FP64_DGEMM_TFLOPS},
            "clocks": clk,
            # per set: k_rdm_hole<1> x2, k_transpose x2, k_rdm_ab, its mirror, k_rdm_hole<2> x2, k_rdm_sf2
            "gpu_launches": 9 * a.steps}

@@ -78,6 +78,7 @@ def _declare(L):
         "f2g_dgraph_ritz": (i32, [vp, P, i64, vp]),
         "f2g_dgraph_history": (i32, [vp, P, i32]),
         "f2g_sigma_set_hamiltonian_async": (i32, [vp, d, P, P, vp]),
+        "f2g_probe_dfma": (i32, [i32, i32, i64, P, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

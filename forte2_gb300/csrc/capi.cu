@@ -24,6 +24,7 @@ void dav_residual(const double* B, const double* S, int m, int64_t ld, const dou
 void dav_eigh(int m, const double* G, double* evals, double* evecs, cudaStream_t st);
 void dav_dots_noalloc(const double* A, int na, int64_t lda, const double* B, int nb, int64_t ldb, int64_t n,
                       double* out, cudaStream_t st);
+void probe_dfma(int blocks, int threads, long long iters, double* out, cudaStream_t st);
 } // namespace f2g
 
 using namespace f2g;
@@ -499,6 +500,13 @@ int f2g_spin_adapter_dump(void* h, int64_t* bounds, int64_t* det_idx, double* co
     return guard([&] {
         need(h, "spin adapter");
         static_cast<SpinAdapter*>(h)->dump(bounds, det_idx, coeff, ranges);
+    });
+}
+
+int f2g_probe_dfma(int blocks, int threads, int64_t iters, double* out, void* stream) {
+    return guard([&] {
+        need(out, "out");
+        probe_dfma(blocks, threads, (long long)iters, out, S(stream));
     });
 }
 

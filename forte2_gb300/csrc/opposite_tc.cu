@@ -25,14 +25,22 @@
 // is bitwise the same for every grid, batch and run. The row is converted back and added to the
 // same-spin terms in FP32 once per alpha string.
 //
-// One CTA per SM (persistent over Ja), 1024 threads: all threads gather the operand tiles into
-// shared memory in the canonical K-major no-swizzle layout (8-row x 16-byte core matrices), one
-// thread issues the MMAs into one of two 128-lane x 128-column FP32 accumulators in tensor memory
-// and commits them to an mbarrier, and while they run all 32 warps read the previous tile's
-// accumulator back (the 8 warps w = q mod 4 share lanes 32 q .. +31 and take one s column block
-// each) for its scatter. Waits are bounded: a wait that gives up sets the error flag, the CTA stops
-// issuing work, waits (bounded again) for the MMAs it has committed and releases its tensor memory.
-// An error flag of 1 means that the sigma of that call is not valid.
+// One CTA per SM (persistent over Ja), 17 warps in three roles that hand tiles to each other
+// through mbarriers (every wait bounded):
+//  * 4 producer warps: thread m owns row m (beta string ib0 + m) of the A tile. It requests the K
+//    gathered values of the next tile into registers while the tensor cores work on the current
+//    one, then (once those MMAs have released the A buffer) scales, splits and stores them in the
+//    canonical K-major no-swizzle layout (8-row x 16-byte core matrices) and arrives on A_full.
+//  * 1 MMA warp: one thread issues the 3 x kp/16 MMAs of a tile (M = 128, N = 256: all 16 s x 16 r
+//    columns in one instruction, so A is gathered once per tile) into one of two 256-column FP32
+//    accumulators in tensor memory and commits them to A_empty and ACC_full.
+//  * 12 scatter warps (three per 32-lane quarter of the accumulator, each taking every third s):
+//    read the finished accumulator with tcgen05.ld, add the fixed-point contributions into the
+//    sigma row and arrive on ACC_empty, so the MMAs of tile t + 1 overlap the scatter of tile t.
+// B = V' for the alpha string is built by all warps between alpha strings. A wait that gives up
+// sets the error flag and the CTA leaves its loops, waits (bounded again) for the MMAs it has
+// committed and releases its tensor memory. An error flag of 1 means that the sigma of that call
+// is not valid.
 #include <cuda_fp16.h>
 
 #include <cmath>
@@ -44,13 +52,15 @@ namespace f2g {
 
 namespace {
 
-constexpr int kTcThreads = 1024;
-constexpr int kQuarterWarps = kTcThreads / 128;      // warps sharing one 32-lane quarter of the accumulator
-constexpr int kChunksPerWarp = 8 / kQuarterWarps;    // s columns (16 accumulator columns each) per warp
+constexpr int kProdWarps = 4;   // producer warps: one thread per row of the A tile
+constexpr int kScatWarps = 12;  // scatter warps: three per lane quarter of the accumulator
+constexpr int kMmaWarp = kProdWarps + kScatWarps;
+constexpr int kTcThreads = (kMmaWarp + 1) * 32;
 constexpr int kTcM = 128;      // beta strings per tile (accumulator lanes)
-constexpr int kTcN = 128;      // 8 values of s x 16 values of r per pass
+constexpr int kTcN = 256;      // 16 values of s x 16 values of r
 constexpr int kTcMaxK = 80;    // padded alpha-excitation count (na * (n - na + 1) <= 72 for n <= 16)
-constexpr int kTcCols = 256;   // tensor-memory columns allocated: two 128-column accumulators
+constexpr int kTcK = 72;       // largest alpha-excitation count
+constexpr int kTcCols = 512;   // tensor-memory columns allocated: two 256-column accumulators
 constexpr int kFixShift = 18;  // fixed-point fraction bits (in units of the scaled product)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -91,15 +101,33 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
 
-// bounded wait for the phase `parity` of an mbarrier; returns false if it gave up after `limit` polls
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long limit) {
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
+// bounded wait for the phase `parity` of an mbarrier; returns false if it gave up after `limit` polls.
+// A poll is a try_wait (which may suspend the thread for a while); limits below kProbeLimit (a test
+// setting) poll with the non-suspending test_wait instead, so that they give up after that many probes.
+// With `abort`, the wait also gives up once another thread of the CTA has set that flag.
+constexpr long long kProbeLimit = 4096;
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long limit,
+                                          const volatile int* abort = nullptr) {
     for (long long it = 0; it < limit; ++it) {
+        if (abort && (it & 63) == 63 && *abort)
+            return false;
         uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}\n"
-                     : "=r"(done)
-                     : "r"(mbar), "r"(parity)
-                     : "memory");
+        if (limit >= kProbeLimit)
+            asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                         "selp.u32 %0, 1, 0, p;\n\t}\n"
+                         : "=r"(done)
+                         : "r"(mbar), "r"(parity)
+                         : "memory");
+        else
+            asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                         "selp.u32 %0, 1, 0, p;\n\t}\n"
+                         : "=r"(done)
+                         : "r"(mbar), "r"(parity)
+                         : "memory");
         if (done)
             return true;
     }
@@ -122,7 +150,7 @@ __device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) 
 
 // scale exponent that maps a largest magnitude m into [2^14, 2^15) (0 for m = 0 or not finite),
 // clamped so that 2^e and 2^-e are normal floats
-__host__ __device__ inline int split_exponent(float m) {
+__device__ __forceinline__ int split_exponent(float m) {
     if (!(m > 0.0f) || !(m <= 3.0e38f))
         return 0;
     int ex = 0;
@@ -149,12 +177,12 @@ struct TcShared {
     alignas(128) __half a_lo[kTcM * kTcMaxK];
     alignas(128) __half b_hi[kTcN * kTcMaxK];
     alignas(128) __half b_lo[kTcN * kTcMaxK];
-    uint32_t ia[kTcMaxK];  // alpha string of excitation k
-    float sgn[kTcMaxK];    // its sign
+    const float* rowp[kTcMaxK]; // row of C of alpha excitation k
+    float sfa[kTcMaxK];         // its sign times the C scale 2^ea
     int pk[kTcMaxK], qk[kTcMaxK];
-    alignas(8) uint64_t mbar;
+    alignas(8) uint64_t a_full, a_empty, acc_full[2], acc_empty[2];
     uint32_t tmem_base;
-    int abort;
+    volatile int abort;
 };
 
 // two FP16 parts of 8 scaled values, stored as one 16-byte row of a core matrix each
@@ -225,31 +253,44 @@ __global__ void k_absmax(int64_t nd, const float* __restrict__ x, unsigned int* 
     }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __maxnreg__(120)
     k_opposite_tc(int n, int na, int nb, int ma, int64_t N0a, int N0b, const uint32_t* __restrict__ down_a,
                   const uint32_t* __restrict__ up_a, const uint64_t* __restrict__ str_b,
-                  const uint32_t* __restrict__ exc_b, const float* __restrict__ V, int eb,
-                  const unsigned int* __restrict__ cmax, const float* __restrict__ C, float* __restrict__ sig,
-                  int* __restrict__ err, long long poll_limit) {
+                  const uint32_t* __restrict__ exc_b, const float* __restrict__ V,
+                  const unsigned int* __restrict__ vmax, const unsigned int* __restrict__ cmax,
+                  const float* __restrict__ C, float* __restrict__ sig, int* __restrict__ err,
+                  long long poll_limit) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TcShared& sh = *reinterpret_cast<TcShared*>(smem_raw);
     // sigma(Ja, :) in 64-bit fixed point, N0b elements
     unsigned long long* row = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(TcShared));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = na * ma, kp = (K + 15) & ~15;
+    const int ntile = (N0b + kTcM - 1) / kTcM;
     C += blockIdx.y * N0a * (int64_t)N0b; // vector blockIdx.y of a batch
     sig += blockIdx.y * N0a * (int64_t)N0b;
-    const uint32_t mbar = smem_u32(&sh.mbar);
-    // operand scales 2^ea (C) and 2^eb (V); the fixed-point row is in units of 2^-(ea + eb + kFixShift)
+    // operand scales 2^ea (C) and 2^eb (V) from the largest magnitudes, read from device memory (so
+    // captured graphs follow new vectors and integrals); the fixed-point row is in units of
+    // 2^-(ea + eb + kFixShift)
     const int ea = split_exponent(__uint_as_float(cmax[blockIdx.y]));
+    const int eb = split_exponent(__uint_as_float(vmax[0]));
     const float fa = pow2f(ea), fb = pow2f(eb);
     const float unscale0 = pow2f(-kFixShift), unscale1 = pow2f(-ea), unscale2 = pow2f(-eb);
+    const uint32_t a_full = smem_u32(&sh.a_full), a_empty = smem_u32(&sh.a_empty);
+    const uint32_t acc_full[2] = {smem_u32(&sh.acc_full[0]), smem_u32(&sh.acc_full[1])};
+    const uint32_t acc_empty[2] = {smem_u32(&sh.acc_empty[0]), smem_u32(&sh.acc_empty[1])};
+    const uint32_t lbo = 128, sbo = (uint32_t)(kp >> 3) * 128;
 
     if (tid == 0) {
-        mbar_init(mbar, 1);
+        mbar_init(a_full, kTcM);
+        mbar_init(a_empty, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(acc_full[b], 1);
+            mbar_init(acc_empty[b], kScatWarps);
+        }
         sh.abort = 0;
     }
-    if (warp == 0) {
+    if (warp == kMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh.tmem_base)),
                      "r"(kTcCols)
                      : "memory");
@@ -260,177 +301,195 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = sh.tmem_base;
-    uint32_t phase = 0;
-    bool in_flight = false; // a commit this thread has not yet seen complete
-    const uint32_t lbo = 128, sbo = (uint32_t)(kp >> 3) * 128;
 
-    // scatter of one finished tile: warp w reads lanes 32 (w % 4) + [0, 32) = beta strings ib0 + that;
-    // the warps sharing a lane quarter take every kQuarterWarps-th s of the pass. The excitation
-    // entries are requested first, then the accumulator columns, then one wait for both, so their
-    // latencies overlap.
-    auto scatter = [&](int ib0, uint32_t acc, int s0) {
-        const int m = (warp & 3) * 32 + lane;
-        const int Ib = ib0 + m;
-        const bool valid = Ib < N0b;
-        const uint64_t mI = valid ? str_b[Ib] : 0;
-        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        uint4 e4[kChunksPerWarp][4];
-        bool has[kChunksPerWarp];
-#pragma unroll
-        for (int i = 0; i < kChunksPerWarp; ++i) {
-            const int s = s0 + (warp >> 2) + kQuarterWarps * i;
-            has[i] = valid && s < n && (mI >> s & 1);
-            if (has[i]) {
-                const int si = popc64(mI & ((uint64_t(1) << s) - 1));
-                const uint4* src = reinterpret_cast<const uint4*>(exc_b + ((int64_t)Ib * nb + si) * 16);
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    e4[i][q] = __ldg(src + q);
-            }
-        }
-        uint32_t v[kChunksPerWarp][16];
-        __syncwarp();
-#pragma unroll
-        for (int i = 0; i < kChunksPerWarp; ++i)
-            tmem_ld16(acc + lane_base + (uint32_t)(((warp >> 2) + kQuarterWarps * i) * 16), v[i]);
-        tmem_wait_ld();
-#pragma unroll
-        for (int i = 0; i < kChunksPerWarp; ++i) {
-            if (!has[i])
-                continue;
-            const uint32_t e[16] = {e4[i][0].x, e4[i][0].y, e4[i][0].z, e4[i][0].w, e4[i][1].x, e4[i][1].y,
-                                    e4[i][1].z, e4[i][1].w, e4[i][2].x, e4[i][2].y, e4[i][2].z, e4[i][2].w,
-                                    e4[i][3].x, e4[i][3].y, e4[i][3].z, e4[i][3].w};
-#pragma unroll
-            for (int r = 0; r < 16; ++r) {
-                const uint32_t jb = e[r] & 0x00FFFFFFu;
-                if (jb != 0x00FFFFFFu) // the sign bit of the entry flips the sign of the value
-                    atomicAdd(row + jb, fixed_point(v[i][r], e[r] >> 31));
-            }
-        }
+    auto give_up = [&]() {
+        atomicExch(err, 1);
+        sh.abort = 1;
     };
 
+    long long g0 = 0;      // tiles of this CTA before the current alpha string
+    long long last_g = -1; // MMA thread: last tile whose MMAs were committed
     for (int64_t Ja = blockIdx.x; Ja < N0a && !sh.abort; Ja += gridDim.x) {
         float* srow = sig + Ja * (int64_t)N0b;
-        for (int c = tid; c < N0b; c += kTcThreads)
-            row[c] = 0ull;
-        // alpha excitations of Ja: k = pi * ma + qi
+        // ---- alpha string set-up (all warps): excitations k = pi * ma + qi, B, zero row
         if (tid < K) {
             const int pi = tid / ma, qi = tid % ma;
             const uint32_t ep = down_a[Ja * na + pi];
             const uint32_t eq = up_a[(int64_t)e_addr(ep) * ma + qi];
-            sh.ia[tid] = e_addr(eq);
-            sh.sgn[tid] = (e_neg(ep) ^ e_neg(eq)) ? -1.0f : 1.0f;
+            sh.rowp[tid] = C + (int64_t)e_addr(eq) * N0b;
+            sh.sfa[tid] = (e_neg(ep) ^ e_neg(eq)) ? -fa : fa; // the alpha sign is folded into A
             sh.pk[tid] = e_orb(ep);
             sh.qk[tid] = e_orb(eq);
         }
+        for (int c = tid; c < N0b; c += kTcThreads)
+            row[c] = 0ull;
         __syncthreads();
-        for (int s0 = 0; s0 < n && !sh.abort; s0 += 8) {
-            // B = V'[(s, r)][k] 2^eb for s in [s0, s0 + 8), r < 16 (zero outside the space); the alpha
-            // sign of excitation k is folded into column k. One 16-byte row of 8 k per task.
-            for (int t = tid; t < kTcN * (kp >> 3); t += kTcThreads) {
-                const int nn = t / (kp >> 3), k0 = (t % (kp >> 3)) * 8;
-                const int s = s0 + (nn >> 4), r = nn & 15;
-                float x[8];
+        // B = V'[(s, r)][k] 2^eb (zero outside the space); one 16-byte row of 8 k per task
+        for (int t = tid; t < kTcN * (kp >> 3); t += kTcThreads) {
+            const int nn = t / (kp >> 3), k0 = (t % (kp >> 3)) * 8;
+            const int s = nn >> 4, r = nn & 15;
+            float x[8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int kk = k0 + j;
-                    x[j] = (kk < K && s < n && r < n)
-                               ? sh.sgn[kk] * fb * V[(((size_t)sh.pk[kk] * n + r) * n + sh.qk[kk]) * n + s]
-                               : 0.0f;
-                }
-                const uint32_t off = kmajor_off(nn, k0, kp) >> 1;
-                split_store(x, sh.b_hi + off, sh.b_lo + off);
+            for (int j = 0; j < 8; ++j) {
+                const int kk = k0 + j;
+                x[j] = (kk < K && s < n && r < n) ? fb * V[(((size_t)sh.pk[kk] * n + r) * n + sh.qk[kk]) * n + s]
+                                                  : 0.0f;
             }
-            int prev_ib0 = -1, tile = 0;
-            uint32_t prev_acc = 0;
-            for (int ib0 = 0; ib0 < N0b && !sh.abort; ib0 += kTcM) {
-                // A = T[Ib][k] 2^ea = C(Ia_k, Ib) 2^ea for Ib in [ib0, ib0 + 128): each thread takes one
-                // Ib and groups of 8 consecutive k (one 16-byte row of a core matrix); for fixed k a
-                // warp reads 32 consecutive floats. All loads of a thread are issued first.
-                {
-                    constexpr int kRowThreads = kTcThreads / kTcM;              // threads per beta string
-                    constexpr int kGroups = (kTcMaxK / 8 + kRowThreads - 1) / kRowThreads;
-                    const int m = tid & (kTcM - 1);
-                    const int Ib = ib0 + m;
-                    const int g0 = tid >> 7;
-                    const bool in = Ib < N0b;
-                    float x[kGroups][8];
-#pragma unroll
-                    for (int j = 0; j < kGroups; ++j)
-#pragma unroll
-                        for (int c = 0; c < 8; ++c) {
-                            const int kk = 8 * (g0 + j * kRowThreads) + c;
-                            x[j][c] = (kk < K && in) ? fa * __ldg(C + (int64_t)sh.ia[kk] * N0b + Ib) : 0.0f;
-                        }
-#pragma unroll
-                    for (int j = 0; j < kGroups; ++j) {
-                        const int g = g0 + j * kRowThreads;
-                        if (8 * g < kp) {
-                            const uint32_t off = kmajor_off(m, 8 * g, kp) >> 1;
-                            split_store(x[j], sh.a_hi + off, sh.a_lo + off);
-                        }
-                    }
-                }
-                // make the generic-proxy shared-memory writes visible to the tensor cores
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                __syncthreads();
-                // two accumulators: the MMAs of this tile run while the previous tile is scattered
-                const uint32_t acc = tmem + (uint32_t)(tile & 1) * kTcN;
-                if (tid == 0) {
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t ahi = smem_u32(sh.a_hi), alo = smem_u32(sh.a_lo);
-                    const uint32_t bhi = smem_u32(sh.b_hi), blo = smem_u32(sh.b_lo);
-                    for (int t = 0; t < kp / 16; ++t) {
-                        const uint32_t adv = (uint32_t)t * 2 * lbo; // 16 FP16 = two core matrices along K
-                        mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), t > 0);
-                        mma_f16(acc, smem_desc(alo + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), 1);
-                        mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(blo + adv, lbo, sbo), 1);
-                    }
-                    mma_commit(mbar);
-                }
-                in_flight = true;
-                if (prev_ib0 >= 0) {
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    scatter(prev_ib0, prev_acc, s0);
-                }
-                const bool ok = mbar_wait(mbar, phase, poll_limit);
-                if (ok) {
-                    in_flight = false;
-                    phase ^= 1;
-                } else {
-                    if (lane == 0)
-                        atomicExch(err, 1);
-                    sh.abort = 1;
-                }
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncthreads();
-                prev_ib0 = ib0;
-                prev_acc = acc;
-                ++tile;
-            }
-            if (prev_ib0 >= 0 && !sh.abort) {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                scatter(prev_ib0, prev_acc, s0);
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            }
-            __syncthreads();
+            const uint32_t off = kmajor_off(nn, k0, kp) >> 1;
+            split_store(x, sh.b_hi + off, sh.b_lo + off);
         }
+        // make the generic-proxy shared-memory writes visible to the tensor cores
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+
+        if (warp < kProdWarps) {
+            // ---- producer: row m of A for every tile of this alpha string
+            const int m = tid;
+            float x[kTcK];
+            auto request = [&](int ib0) {
+                const int Ib = ib0 + m;
+                const bool in = Ib < N0b;
+#pragma unroll
+                for (int k = 0; k < kTcK; ++k)
+                    x[k] = (k < K && in) ? __ldg(sh.rowp[k] + Ib) : 0.0f;
+            };
+            request(0);
+            for (int t = 0; t < ntile; ++t) {
+                const long long g = g0 + t;
+                if (sh.abort)
+                    break;
+                if (g > 0 && !mbar_wait(a_empty, (uint32_t)((g - 1) & 1), poll_limit, &sh.abort)) {
+                    give_up();
+                    break;
+                }
+#pragma unroll
+                for (int j = 0; j < kTcMaxK / 8; ++j) {
+                    if (8 * j < kp) {
+                        float v[8];
+#pragma unroll
+                        for (int c = 0; c < 8; ++c)
+                            v[c] = (8 * j + c < kTcK) ? x[8 * j + c] * sh.sfa[8 * j + c] : 0.0f;
+                        const uint32_t off = kmajor_off(m, 8 * j, kp) >> 1;
+                        split_store(v, sh.a_hi + off, sh.a_lo + off);
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(a_full);
+                if (t + 1 < ntile)
+                    request((t + 1) * kTcM);
+            }
+        } else if (warp < kMmaWarp) {
+            // ---- scatter: lanes 32 q .. +31 of the accumulator (q = warp mod 4, the quarter this warp
+            // may read), every third s from grp on
+            const int q = warp & 3, grp = (warp - kProdWarps) >> 2;
+            const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+            for (int t = 0; t < ntile; ++t) {
+                const long long g = g0 + t;
+                const int buf = (int)(g & 1);
+                // lane 0 waits and decides for the whole warp (the warp-collective operations below
+                // need every lane); __syncwarp orders the other lanes after its acquire
+                int go = 0;
+                if (lane == 0) {
+                    go = !sh.abort;
+                    if (go && !mbar_wait(acc_full[buf], (uint32_t)((g >> 1) & 1), poll_limit, &sh.abort)) {
+                        give_up();
+                        go = 0;
+                    }
+                }
+                go = __shfl_sync(0xffffffffu, go, 0);
+                __syncwarp();
+                if (!go)
+                    break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + (uint32_t)buf * kTcN + lane_base;
+                const int Ib = t * kTcM + q * 32 + lane;
+                const bool valid = Ib < N0b;
+                const uint64_t mI = valid ? str_b[Ib] : 0;
+                // the excitation entries of the next s are requested before the current s is added
+                uint4 en[4];
+                auto request = [&](int s) {
+                    if (valid && s < n && (mI >> s & 1)) {
+                        const int si = popc64(mI & ((uint64_t(1) << s) - 1));
+                        const uint4* src = reinterpret_cast<const uint4*>(exc_b + ((int64_t)Ib * nb + si) * 16);
+#pragma unroll
+                        for (int c = 0; c < 4; ++c)
+                            en[c] = __ldg(src + c);
+                    }
+                };
+                request(grp);
+                for (int s = grp; s < n; s += 3) {
+                    const bool has = valid && (mI >> s & 1);
+                    const uint32_t e[16] = {en[0].x, en[0].y, en[0].z, en[0].w, en[1].x, en[1].y, en[1].z, en[1].w,
+                                            en[2].x, en[2].y, en[2].z, en[2].w, en[3].x, en[3].y, en[3].z, en[3].w};
+                    request(s + 3);
+                    if (!__any_sync(0xffffffffu, has))
+                        continue;
+                    uint32_t v[16];
+                    tmem_ld16(acc + (uint32_t)(s * 16), v);
+                    tmem_wait_ld();
+                    if (has) {
+#pragma unroll
+                        for (int r = 0; r < 16; ++r) {
+                            const uint32_t jb = e[r] & 0x00FFFFFFu;
+                            if (jb != 0x00FFFFFFu) // the sign bit of the entry flips the sign of the value
+                                atomicAdd(row + jb, fixed_point(v[r], e[r] >> 31));
+                        }
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0)
+                    mbar_arrive(acc_empty[buf]);
+            }
+        } else if (lane == 0) {
+            // ---- MMA issue: D[buf] = A B over kp / 16 steps of K = 16, three split products each
+            const uint32_t ahi = smem_u32(sh.a_hi), alo = smem_u32(sh.a_lo);
+            const uint32_t bhi = smem_u32(sh.b_hi), blo = smem_u32(sh.b_lo);
+            for (int t = 0; t < ntile; ++t) {
+                const long long g = g0 + t;
+                const int buf = (int)(g & 1);
+                if (sh.abort)
+                    break;
+                if (!mbar_wait(a_full, (uint32_t)(g & 1), poll_limit, &sh.abort)) {
+                    give_up();
+                    break;
+                }
+                if (g >= 2 && !mbar_wait(acc_empty[buf], (uint32_t)(((g >> 1) - 1) & 1), poll_limit, &sh.abort)) {
+                    give_up();
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + (uint32_t)buf * kTcN;
+                for (int kk = 0; kk < kp / 16; ++kk) {
+                    const uint32_t adv = (uint32_t)kk * 2 * lbo; // 16 FP16 = two core matrices along K
+                    mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), kk > 0);
+                    mma_f16(acc, smem_desc(alo + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), 1);
+                    mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(blo + adv, lbo, sbo), 1);
+                }
+                mma_commit(a_empty);
+                mma_commit(acc_full[buf]);
+                last_g = g;
+            }
+        }
+        __syncwarp();
+        __syncthreads(); // every tile of Ja scattered (so every MMA of it complete), or an abort
         if (!sh.abort)
             for (int c = tid; c < N0b; c += kTcThreads) {
                 const float x = __ll2float_rn((long long)row[c]) * unscale0 * unscale1 * unscale2;
                 srow[c] += x;
             }
+        g0 += ntile;
         __syncthreads();
     }
-    // after a wait that gave up, the MMAs of that commit may still be running: wait for them (bounded)
-    // before the tensor memory they write is released
-    if (in_flight)
-        (void)mbar_wait(mbar, phase, (1ll << 26));
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // after an abort, MMAs may still be running: wait (bounded) for the last commit before the tensor
+    // memory they write is released (a no-op when every tile was scattered)
+    if (warp == kMmaWarp && lane == 0 && last_g >= 0)
+        (void)mbar_wait(acc_full[last_g & 1], (uint32_t)((last_g >> 1) & 1), (1ll << 26));
+    __syncwarp();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0)
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == kMmaWarp)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
 }
 
@@ -453,11 +512,20 @@ void build_beta_exc(const CIStrings* s, DevBuf<uint32_t>& exc, cudaStream_t st) 
     F2G_LAUNCH("k_build_beta_exc");
 }
 
-int opposite_tc_v_exponent(float vmax) { return split_exponent(vmax); }
+// vmax <- the largest |V| of the n^4 FP32 integrals (as FP32 bits), ordered on st
+void opposite_tc_vmax(const float* V, int64_t count, unsigned int* vmax, cudaStream_t st) {
+    F2G_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned int), st));
+    if (count == 0)
+        return;
+    k_absmax<<<dim3(64, 1), 256, 0, st>>>(count, V, vmax);
+    F2G_LAUNCH("k_absmax V");
+}
 
-// cmax: nvec words of scratch (the per-vector largest |C|), written here before the kernel runs.
-void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, int eb, const float* C, float* sig,
-                        unsigned int* cmax, int* err, long long poll_limit, int max_ctas, cudaStream_t st, int nvec) {
+// vmax: the integrals' largest magnitude (opposite_tc_vmax); cmax: nvec words of scratch for the
+// per-vector largest |C|, written here before the kernel runs.
+void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, const unsigned int* vmax,
+                        const float* C, float* sig, unsigned int* cmax, int* err, long long poll_limit, int max_ctas,
+                        cudaStream_t st, int nvec) {
     const int64_t nd = s->a.N0 * s->b.N0;
     F2G_CUDA(cudaMemsetAsync(cmax, 0, (size_t)nvec * sizeof(unsigned int), st));
     k_absmax<<<dim3(256, (unsigned)nvec), 256, 0, st>>>(nd, C, cmax);
@@ -472,7 +540,7 @@ void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V,
         gx = std::min<int64_t>(gx, max_ctas);
     k_opposite_tc<<<dim3((unsigned)gx, (unsigned)nvec), kTcThreads, smem, st>>>(
         s->norb, s->na, s->nb, s->a.m1, s->a.N0, (int)s->b.N0, s->a.down1.get(), s->a.up1.get(), s->b.str.get(), exc,
-        V, eb, cmax, C, sig, err, poll_limit > 0 ? poll_limit : (1ll << 26));
+        V, vmax, cmax, C, sig, err, poll_limit > 0 ? poll_limit : (1ll << 26));
     F2G_LAUNCH("k_opposite_tc");
 }
 

@@ -264,19 +264,24 @@ __global__ void __launch_bounds__(512, 1)
                 so[si] = (active && si < mb) ? e_orb(ub[si]) : -1;
                 acc[si] = T(0);
             }
+            // the gathered C values of excitation qi + 1 are requested before the products of qi,
+            // so every warp hides its own gather latency (warps leave each round's barriers together)
+            T dn[MB];
+#pragma unroll
+            for (int si = 0; si < MB; ++si)
+                dn[si] = (active && si < mb) ? __ldg(C + (int64_t)e_addr(ua[0]) * N0b + e_addr(ub[si])) : T(0);
             for (int qi = 0; active && qi < ma; ++qi) {
-                const uint32_t eq = ua[qi];
-                const T* crow = C + (int64_t)e_addr(eq) * N0b;
-                const int negq = e_neg(eq);
+                const int negq = e_neg(ua[qi]);
                 T d[MB];
 #pragma unroll
-                for (int si = 0; si < MB; ++si) {
-                    if (si < mb) {
-                        const T x = __ldg(crow + e_addr(ub[si]));
-                        d[si] = (negq ^ e_neg(ub[si])) ? -x : x;
-                    } else {
-                        d[si] = T(0);
-                    }
+                for (int si = 0; si < MB; ++si)
+                    d[si] = (negq ^ e_neg(ub[si])) ? -dn[si] : dn[si];
+                if (qi + 1 < ma) {
+                    const T* crow = C + (int64_t)e_addr(ua[qi + 1]) * N0b;
+#pragma unroll
+                    for (int si = 0; si < MB; ++si)
+                        if (si < mb)
+                            dn[si] = __ldg(crow + e_addr(ub[si]));
                 }
                 const T* vq = vs + qi * n;
 #pragma unroll
@@ -376,17 +381,10 @@ static int sm_count() {
 size_t opposite_tc_smem(int N0b);
 bool opposite_tc_supported(const CIStrings* s);
 void build_beta_exc(const CIStrings* s, DevBuf<uint32_t>& exc, cudaStream_t st);
-int opposite_tc_v_exponent(float vmax);
-void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, int eb, const float* C, float* sig,
-                        unsigned int* cmax, int* err, long long poll_limit, int max_ctas, cudaStream_t st, int nvec);
-
-// scale exponent of the FP32 integrals for the tensor-core kernel's FP16 split (from the host copy)
-static int v_exponent(const std::vector<double>& V) {
-    float m = 0.0f;
-    for (double x : V)
-        m = std::max(m, std::fabs((float)x));
-    return opposite_tc_v_exponent(m);
-}
+void opposite_tc_vmax(const float* V, int64_t count, unsigned int* vmax, cudaStream_t st);
+void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, const unsigned int* vmax,
+                        const float* C, float* sig, unsigned int* cmax, int* err, long long poll_limit, int max_ctas,
+                        cudaStream_t st, int nvec);
 
 SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const double* V_, int ll)
     : s(s_), n(s_->norb), log_level(ll) {
@@ -398,6 +396,7 @@ SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const dou
     if (opposite_tc_supported(s)) {
         build_beta_exc(s, beta_exc, 0); // ordered before set_hamiltonian's wait on the legacy stream
         tc_cmax.reserve(2 * 65536);      // one word per vector of a batch (grid y <= 65535), two sets
+        tc_vmax.reserve(1);
     }
     set_hamiltonian(E_, H_, V_);
 }
@@ -452,7 +451,6 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
     E = E_;
     H.assign(H_, H_ + (size_t)n * n);
     V.assign(V_, V_ + (size_t)n * n * n * n);
-    tc_eb = v_exponent(V);
     dH.reserve(std::max<size_t>(1, H.size()));
     dV.reserve(std::max<size_t>(1, V.size()));
     if (!H.empty())
@@ -464,6 +462,8 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
         k_convert<double, float><<<64, 256>>>((int64_t)V.size(), dV.get(), fV.get());
         F2G_LAUNCH("k_convert V");
     }
+    if (tc_vmax.get())
+        opposite_tc_vmax(fV.get(), (int64_t)V.size(), tc_vmax.get(), 0);
     build_string_hamiltonian(0, ha, true, 0);
     build_string_hamiltonian(1, hb, false, 0);
     F2G_CUDA(cudaStreamSynchronize(0)); // set-up ran on the legacy stream: wait for it alone
@@ -480,7 +480,6 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
     E = E_;
     H.assign(H_, H_ + (size_t)n * n);
     V.assign(V_, V_ + (size_t)n * n * n * n);
-    tc_eb = v_exponent(V);
     dH.reserve(std::max<size_t>(1, H.size()));
     dV.reserve(std::max<size_t>(1, V.size()));
     fV.reserve(std::max<size_t>(1, V.size()));
@@ -491,6 +490,8 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
         k_convert<double, float><<<64, 256, 0, st>>>((int64_t)V.size(), dV.get(), fV.get());
         F2G_LAUNCH("k_convert V");
     }
+    if (tc_vmax.get())
+        opposite_tc_vmax(fV.get(), (int64_t)V.size(), tc_vmax.get(), st);
     build_string_hamiltonian(0, ha, true, st);
     build_string_hamiltonian(1, hb, false, st);
     for (StringHamiltonian* sh : {&ha, &hb}) {
@@ -733,8 +734,8 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
                 // graph launches use their own half of the scale scratch, so a captured solve and a
                 // direct call on the same builder never share it
                 unsigned int* cmax = tc_cmax.get() + (graph ? 65536 : 0);
-                launch_opposite_tc(s, beta_exc.get(), Vt, tc_eb, C, sig, cmax, tc_err.get(), tc_poll_limit, max_ctas,
-                                   st, nvec);
+                launch_opposite_tc(s, beta_exc.get(), Vt, tc_vmax.get(), C, sig, cmax, tc_err.get(), tc_poll_limit,
+                                   max_ctas, st, nvec);
                 done = true;
             }
         }

@@ -45,7 +45,7 @@ struct SigmaBuilder {
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
     DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
     DevBuf<unsigned int> tc_cmax; // per-vector largest |C| of a tensor-core launch (its operand scale)
-    int tc_eb = 0;             // power-of-two scale of the FP32 integrals in the FP16 split
+    DevBuf<unsigned int> tc_vmax; // largest |V| of the FP32 integrals (the FP16 split's scale)
     long long tc_poll_limit = 0; // polls per bounded wait in the tensor-core kernel (0: the default)
     bool tensor_cores_available() const;
     int tc_error() const;

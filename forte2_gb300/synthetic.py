@@ -53,6 +53,35 @@ def make_integrals(norb: int, seed: int, naux: int | None = None) -> ActiveSpace
     return ActiveSpaceIntegrals(0.0, np.ascontiguousarray(h), V, eri)
 
 
+def rotate_integrals(ints: ActiveSpaceIntegrals, seed: int, theta: float = 0.05) -> ActiveSpaceIntegrals:
+    """The active-space integrals of the next macro-iteration of an orbital optimiser
+    (forte2/mcopt/mc_optimizer.py:297-328), from ``default_rng(seed)``:
+
+    1. an active-active rotation U = exp(K), K antisymmetric with strict-upper entries N(0, theta)
+       (``np.triu_indices(n, 1)`` order): h -> U^T h U, (pq|rs) -> sum U_ap U_bq U_cr U_ds (ab|cd);
+       alone it leaves the CASCI energies unchanged but changes every determinant matrix element;
+    2. the change an inactive-active rotation makes, modelled as a mix with a fresh draw of the
+       integral recipe: x -> (1 - theta) x + theta x', x' = make_integrals(n, seed + 1) (the energies
+       move by O(theta); the 8-fold symmetry of (pq|rs) is kept).
+    """
+    from scipy.linalg import expm
+
+    n = ints.norb
+    rng = np.random.default_rng(seed)
+    iu = np.triu_indices(n, 1)
+    K = np.zeros((n, n))
+    K[iu] = rng.normal(0.0, theta, len(iu[0]))
+    K = K - K.T
+    U = expm(K)
+    fresh = make_integrals(n, seed + 1)
+    h = (1.0 - theta) * (U.T @ ints.H @ U) + theta * fresh.H
+    h = 0.5 * (h + h.T)
+    eri = np.einsum("ap,bq,cr,ds,abcd->pqrs", U, U, U, U, ints.eri, optimize=True)
+    eri = (1.0 - theta) * eri + theta * fresh.eri
+    V = np.ascontiguousarray(eri.transpose(0, 2, 1, 3))
+    return ActiveSpaceIntegrals(ints.E, np.ascontiguousarray(h), V, eri)
+
+
 def random_ci_vector(ndet: int, seed: int) -> np.ndarray:
     """Normalised N(0,1) determinant vector (as in the reference's tests/ci/test_ci_rdms.py:387)."""
     rng = np.random.default_rng(seed)

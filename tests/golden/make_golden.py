@@ -240,9 +240,11 @@ def gen_sigma_checksums(out, cases, fname):
 
 
 def reference_casci(na, nb, n, mult, twice_ms, nroot, iseed, e_tol, DavidsonLiuSolver, Params,
-                    maxiter=100):
-    """Drive the reference Davidson exactly as forte2/ci/ci.py:_do_iterative_ci does."""
-    ints = make_integrals(n, iseed)
+                    maxiter=100, ints=None, solver=None, return_solver=False):
+    """Drive the reference Davidson exactly as forte2/ci/ci.py:_do_iterative_ci does. With `solver`
+    (a DavidsonLiuSolver that has already solved), it continues from that solver's vectors with the
+    new integrals, as the reference's MCSCF loop does (ci.py:266-290, mc_optimizer.py:297-328)."""
+    ints = make_integrals(n, iseed) if ints is None else ints
     s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
     sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
     sb.set_algorithm("hz")
@@ -250,7 +252,9 @@ def reference_casci(na, nb, n, mult, twice_ms, nroot, iseed, e_tol, DavidsonLiuS
     sa.prepare_couplings(s)
     hdiag = sb.form_Hdiag_csf(sa)
     params = Params(e_tol=e_tol, maxiter=maxiter)
-    solver = DavidsonLiuSolver(size=sa.ncsf, nroot=nroot, davidson_liu_params=params, log_level=0)
+    warm = solver is not None
+    if not warm:
+        solver = DavidsonLiuSolver(size=sa.ncsf, nroot=nroot, davidson_liu_params=params, log_level=0)
     solver.add_h_diag(hdiag)
     # guess vectors (ci.py:411-452)
     nguess = min(params.guess_per_root * nroot, sa.ncsf)
@@ -268,7 +272,8 @@ def reference_casci(na, nb, n, mult, twice_ms, nroot, iseed, e_tol, DavidsonLiuS
     for i in range(nguess):
         for j, d in enumerate(indices):
             guess[d, i] = vecs[j, i]
-    solver.add_guesses(guess)
+    if not warm:
+        solver.add_guesses(guess)
 
     def sigma_builder(B, S):
         for i in range(B.shape[1]):
@@ -296,11 +301,12 @@ def reference_casci(na, nb, n, mult, twice_ms, nroot, iseed, e_tol, DavidsonLiuS
     else:
         op = LinearOperator((sa.ncsf, sa.ncsf), matvec=mv, dtype=np.float64)
         lanczos = np.sort(eigsh(op, k=nroot, which="SA", tol=1e-14, ncv=max(4 * nroot, 40))[0])
-    return dict(evals=[float(x) for x in evals], converged=bool(solver.converged),
-                iterations=int(solver.iter), ncsf=sa.ncsf, ndet=s.ndet, seconds=seconds,
-                hdiag_min=float(hdiag.min()), nguess_dets=int(nguess_dets), maxiter=maxiter,
-                lanczos=[float(x) for x in lanczos],
-                max_dev_vs_lanczos=float(np.max(np.abs(np.sort(evals) - lanczos))))
+    out = dict(evals=[float(x) for x in evals], converged=bool(solver.converged),
+               iterations=int(solver.iter), ncsf=sa.ncsf, ndet=s.ndet, seconds=seconds,
+               hdiag_min=float(hdiag.min()), nguess_dets=int(nguess_dets), maxiter=maxiter,
+               lanczos=[float(x) for x in lanczos],
+               max_dev_vs_lanczos=float(np.max(np.abs(np.sort(evals) - lanczos))))
+    return (out, solver) if return_solver else out
 
 
 def gen_davidson(out, ref_root):
@@ -317,6 +323,40 @@ def gen_davidson(out, ref_root):
         json.dump(meta, f, indent=1)
 
 
+# MCSCF-style sequence: (na, nb, norb, multiplicity, nroot, integral seed, rotation seeds, theta, e_tol)
+MCSCF_CASES = [(4, 4, 8, 1, 2, 4100, (4111, 4122), 0.05, 1e-10),
+               (5, 5, 10, 1, 1, 4200, (4211, 4222), 0.03, 1e-10),
+               (4, 4, 8, 3, 1, 4300, (4311, 4322), 0.05, 1e-10)]
+
+
+def gen_mcscf(out, ref_root):
+    """Energies of successive CI solves with rotated integrals, one reference Davidson solver
+    warm-started from solve to solve, as the reference's orbital optimiser drives its CI solver
+    (mcopt/mc_optimizer.py:297-328: set_ints then run, ci.py:266-290 keeps the eigensolver)."""
+    from forte2_gb300.synthetic import rotate_integrals
+
+    DL, Params = load_davidson(ref_root)
+    meta = {}
+    for na, nb, n, mult, nroot, iseed, rseeds, theta, e_tol in MCSCF_CASES:
+        ints = make_integrals(n, iseed)
+        solver = None
+        steps = []
+        for k in range(len(rseeds) + 1):
+            if k > 0:
+                ints = rotate_integrals(ints, rseeds[k - 1], theta)
+            r, solver = reference_casci(na, nb, n, mult, 0, nroot, iseed, e_tol, DL, Params, 400, ints=ints,
+                                        solver=solver, return_solver=True)
+            steps.append(dict(evals=r["evals"], iterations=r["iterations"], converged=r["converged"],
+                              lanczos=r["lanczos"], max_dev_vs_lanczos=r["max_dev_vs_lanczos"],
+                              H_sha=sha(ints.H)))
+            print("mcscf", (na, nb, n, mult, nroot), k, r["evals"], r["iterations"], flush=True)
+        meta[f"{na}_{nb}_{n}_m{mult}_r{nroot}"] = dict(na=na, nb=nb, norb=n, multiplicity=mult, nroot=nroot,
+                                                      iseed=iseed, rotation_seeds=list(rseeds), theta=theta,
+                                                      e_tol=e_tol, steps=steps)
+    with open(os.path.join(out, "mcscf.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("FORTE2_REFERENCE_ROOT"),
@@ -329,6 +369,7 @@ def main():
     steps = {"lists": lambda: gen_lists(HERE), "sigma": lambda: gen_sigma(HERE),
              "checksums": lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_CASES, "sigma_checksums.json"),
              "davidson": lambda: gen_davidson(HERE, a.reference), "rdm": lambda: gen_rdm(HERE),
+             "mcscf": lambda: gen_mcscf(HERE, a.reference),
              "rdm3": lambda: gen_rdm3(HERE)}
     if a.big:
         steps["big"] = lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_BIG, "sigma_checksums_16.json")

@@ -244,3 +244,36 @@ def test_casci_energy_shift_and_warm_start(cuda, golden_davidson):
     sol2.run()  # MCSCF-style second run with the same integrals: warm start from the last vectors
     assert sol2.eigensolver.iter <= min(3, it_first)
     np.testing.assert_allclose(sol2.evals, g["evals"][:2], atol=1e-10)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("key", ["4_4_8_m1_r2", "5_5_10_m1_r1", "4_4_8_m3_r1"])
+def test_mcscf_loop_with_new_integrals(cuda, key, graph):
+    """The orbital optimiser's use of the CI solver (mcopt/mc_optimizer.py:297-328): set_ints with
+    the next macro-iteration's integrals, then run(), warm-started from the last vectors. Each
+    solve matches the energies of the reference's own Davidson, driven the same way on the
+    reference's compiled sigma (tests/golden/mcscf.json), to 1e-10 Eh; warm starts take fewer
+    iterations than the cold first solve."""
+    import json
+    import os
+
+    from forte2_gb300.ci import CASCISolver
+    from forte2_gb300.params import DavidsonLiuParams
+    from forte2_gb300.synthetic import rotate_integrals
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "mcscf.json")) as f:
+        g = json.load(f)[key]
+    ints = make_integrals(g["norb"], g["iseed"])
+    sol = CASCISolver(norb=g["norb"], na=g["na"], nb=g["nb"], multiplicity=g["multiplicity"], nroot=g["nroot"],
+                      E=ints.E, H=ints.H, V=ints.V, use_graph=graph,
+                      davidson_liu_params=DavidsonLiuParams(e_tol=g["e_tol"], maxiter=400))
+    iters = []
+    for k, step in enumerate(g["steps"]):
+        if k > 0:
+            ints = rotate_integrals(ints, g["rotation_seeds"][k - 1], g["theta"])
+            sol.set_ints(ints.E, ints.H, ints.V)
+        sol.run()
+        assert sol.converged, (key, k)
+        np.testing.assert_allclose(np.sort(sol.evals), np.sort(step["evals"]), rtol=0, atol=1e-10)
+        iters.append(sol.eigensolver.iter)
+    assert max(iters[1:]) < iters[0], iters
