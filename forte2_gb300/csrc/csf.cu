@@ -226,6 +226,31 @@ __device__ inline int64_t find_bucket(const int64_t* off, int64_t n, int64_t x) 
     return lo;
 }
 
+// largest c in [lo, hi] with off[c] <= x, given off[lo] <= x (a search inside one thread block's
+// bracket of configurations: a few steps on one or two cache lines)
+__device__ inline int64_t find_in(const int64_t* off, int64_t lo, int64_t hi, int64_t x) {
+    ++hi;
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (off[mid] <= x)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// bracket[b] = the configuration holding element b * kBracket of the offsets `off` (nconf + 1
+// entries, total = off[nconf]); bracket[nb] = the configuration of the last element
+constexpr int kBracket = 256;
+__global__ void k_brackets(const int64_t* off, int64_t nconf, int64_t total, int64_t nb, int64_t* bracket) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b > nb)
+        return;
+    const int64_t x = b < nb ? b * kBracket : total - 1;
+    bracket[b] = find_bucket(off, nconf, x);
+}
+
 struct CsfView {
     int64_t nconf;
     const uint64_t* conf_s;
@@ -236,12 +261,19 @@ struct CsfView {
     const int64_t* offN;
     const int* ncsfN;
     const int* ndetN;
-    const float* Of; // FP32 copy of the overlap tables (the FP32 transforms of the mixed mode)
+    const float* Of;  // FP32 copy of the overlap tables (the FP32 transforms of the mixed mode)
+    const double* OT; // the tables transposed, [ndetN][ncsfN] (det -> CSF reads them along the CSFs)
+    const float* OTf;
+    const int64_t* slot_brk; // configuration brackets of the slot blocks (k_brackets)
+    const int64_t* csf_brk;  // and of the CSF blocks
 };
 
 template <typename T> __device__ __forceinline__ const T* overlaps(const CsfView& v);
 template <> __device__ __forceinline__ const double* overlaps<double>(const CsfView& v) { return v.O; }
 template <> __device__ __forceinline__ const float* overlaps<float>(const CsfView& v) { return v.Of; }
+template <typename T> __device__ __forceinline__ const T* overlaps_t(const CsfView& v);
+template <> __device__ __forceinline__ const double* overlaps_t<double>(const CsfView& v) { return v.OT; }
+template <> __device__ __forceinline__ const float* overlaps_t<float>(const CsfView& v) { return v.OTf; }
 
 // Vector blockIdx.y of a batch: csf + y * ncsf_stride, det + y * ndet_stride. T = double, or float
 // for the FP32 sigma of the mixed mode.
@@ -253,7 +285,7 @@ __global__ void k_csf_to_det(int64_t nslot, CsfView v, const T* __restrict__ csf
         return;
     csf += blockIdx.y * ncsf_stride;
     det += blockIdx.y * ndet_stride;
-    const int64_t c = find_bucket(v.conf_slot, v.nconf, t);
+    const int64_t c = find_in(v.conf_slot, v.slot_brk[blockIdx.x], v.slot_brk[blockIdx.x + 1], t);
     const int N = popc64(v.conf_s[c]);
     const int nd = v.ndetN[N], nc = v.ncsfN[N];
     const int64_t j = t - v.conf_slot[c];
@@ -274,15 +306,16 @@ __global__ void k_det_to_csf(int64_t ncsf, CsfView v, const T* __restrict__ det,
         return;
     det += blockIdx.y * ndet_stride;
     csf += blockIdx.y * ncsf_stride;
-    const int64_t c = find_bucket(v.conf_csf, v.nconf, u);
+    const int64_t c = find_in(v.conf_csf, v.csf_brk[blockIdx.x], v.csf_brk[blockIdx.x + 1], u);
     const int N = popc64(v.conf_s[c]);
-    const int nd = v.ndetN[N];
+    const int nd = v.ndetN[N], nc = v.ncsfN[N];
     const int64_t i = u - v.conf_csf[c];
-    const T* O = overlaps<T>(v) + v.offN[N] + i * nd;
+    // transposed table: the threads of a configuration (consecutive i) read consecutive entries
+    const T* O = overlaps_t<T>(v) + v.offN[N] + i;
     const uint32_t* pm = v.perm + v.conf_slot[c];
     T acc = 0;
     for (int j = 0; j < nd; ++j) {
-        const T o = O[j];
+        const T o = O[(int64_t)j * nc];
         if (o == T(0))
             continue;
         const uint32_t e = pm[j];
@@ -470,6 +503,18 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
     O.reserve(std::max<size_t>(1, Ohost.size()));
     if (!Ohost.empty())
         F2G_CUDA(cudaMemcpy(O.get(), Ohost.data(), Ohost.size() * sizeof(double), cudaMemcpyHostToDevice));
+    {
+        std::vector<double> T_(Ohost.size());
+        for (int N = 0; N <= n; ++N) {
+            const int64_t nc = ncsfN[N], nd = ndetN[N], b = offN[N];
+            for (int64_t i = 0; i < nc; ++i)
+                for (int64_t j = 0; j < nd; ++j)
+                    T_[b + j * nc + i] = Ohost[b + i * nd + j];
+        }
+        OT.reserve(std::max<size_t>(1, T_.size()));
+        if (!T_.empty())
+            F2G_CUDA(cudaMemcpy(OT.get(), T_.data(), T_.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
     dOff.reserve(n + 2);
     dNcsf.reserve(n + 1);
     dNdet.reserve(n + 1);
@@ -537,6 +582,18 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
                                                    first.get(), cidx.get(), conf_slot.get(), perm.get());
         F2G_LAUNCH("k_conf_perm");
     }
+    // configuration brackets of the 256-element blocks of the transform kernels
+    for (int which = 0; which < 2; ++which) {
+        const int64_t total = which == 0 ? nslot : ncsf;
+        const int64_t nb = (total + kBracket - 1) / kBracket;
+        DevBuf<int64_t>& brk = which == 0 ? slot_brk : csf_brk;
+        brk.reserve(nb + 1);
+        if (total > 0) {
+            k_brackets<<<ceil_div(nb + 1, T), T, 0, st>>>(which == 0 ? conf_slot.get() : conf_csf.get(), nconf, total,
+                                                          nb, brk.get());
+            F2G_LAUNCH("k_brackets");
+        }
+    }
     // coupling count (non-zero overlaps), as the reference logs it
     TmpBuf<unsigned long long> hist(65, st);
     F2G_CUDA(cudaMemsetAsync(hist.get(), 0, 65 * 8, st));
@@ -554,8 +611,9 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
 }
 
 static CsfView view_of(const SpinAdapter& a) {
-    return CsfView{a.nconf, a.conf_s.get(), a.conf_csf.get(), a.conf_slot.get(), a.perm.get(),
-                   a.O.get(), a.dOff.get(), a.dNcsf.get(), a.dNdet.get(), a.O32.get()};
+    return CsfView{a.nconf,       a.conf_s.get(), a.conf_csf.get(), a.conf_slot.get(), a.perm.get(),
+                   a.O.get(),     a.dOff.get(),   a.dNcsf.get(),    a.dNdet.get(),     a.O32.get(),
+                   a.OT.get(),    a.OT32.get(),   a.slot_brk.get(), a.csf_brk.get()};
 }
 
 void SpinAdapter::csf_to_det(const double* csf, double* det, cudaStream_t st, int nvec) const {
@@ -590,6 +648,9 @@ void SpinAdapter::ensure_fp32_tables(cudaStream_t st) const {
     O32.reserve((size_t)nO);
     k_convert_d2f<<<ceil_div(nO, 256), 256, 0, st>>>(nO, O.get(), O32.get());
     F2G_LAUNCH("k_convert_d2f overlaps");
+    OT32.reserve((size_t)nO);
+    k_convert_d2f<<<ceil_div(nO, 256), 256, 0, st>>>(nO, OT.get(), OT32.get());
+    F2G_LAUNCH("k_convert_d2f transposed overlaps");
 }
 
 void SpinAdapter::csf_to_det(const float* csf, float* det, cudaStream_t st, int nvec) const {

@@ -17,11 +17,13 @@ struct SpinAdapter {
     std::vector<int> ncsfN, ndetN;
     std::vector<int64_t> offN;             // offset of table N in O
     DevBuf<double> O;                      // concatenated [ncsfN][ndetN] tables
+    DevBuf<double> OT;                     // the same tables transposed, [ndetN][ncsfN]
     DevBuf<int64_t> dOff;                  // offN on the device
     DevBuf<int> dNcsf, dNdet;
     DevBuf<uint64_t> conf_d, conf_s;       // [nconf] doubly / singly occupied masks (insertion order)
     DevBuf<int64_t> conf_csf, conf_slot;   // [nconf + 1] exclusive offsets
     DevBuf<uint32_t> perm;                 // [nslot] determinant address | negative sign << 31
+    DevBuf<int64_t> slot_brk, csf_brk;     // configuration of every 256th slot / CSF (and of the last)
 
     SpinAdapter(const CIStrings* s, int twoS, int twoMs);
     // nvec vectors back to back (strides ncsf and ndet), one launch
@@ -31,7 +33,7 @@ struct SpinAdapter {
     void csf_to_det(const float* csf, float* det, cudaStream_t st, int nvec = 1) const;
     void det_to_csf(const float* det, float* csf, cudaStream_t st, int nvec = 1) const;
     void ensure_fp32_tables(cudaStream_t st) const;
-    mutable DevBuf<float> O32;
+    mutable DevBuf<float> O32, OT32;
     mutable std::unique_ptr<struct CsfSigmaScratch> host_scratch; // for host calls of sigma_csf
     void hdiag(const double* det_energy, double* out, cudaStream_t st) const;
     // dense <I|H|J> over CSFs idx[0..m) (slater_rules_csf, ci_sigma_builder.cc:278-297)

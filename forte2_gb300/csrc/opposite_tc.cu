@@ -25,15 +25,15 @@
 // is bitwise the same for every grid, batch and run. The row is converted back and added to the
 // same-spin terms in FP32 once per alpha string.
 //
-// One CTA per SM (persistent over Ja), 17 warps in three roles that hand tiles to each other
+// One CTA per SM (persistent over Ja), 16 warps in three roles that hand tiles to each other
 // through mbarriers (every wait bounded):
 //  * 4 producer warps: thread m owns row m (beta string ib0 + m) of the A tile. It requests the K
 //    gathered values of the next tile into registers while the tensor cores work on the current
 //    one, then (once those MMAs have released the A buffer) scales, splits and stores them in the
 //    canonical K-major no-swizzle layout (8-row x 16-byte core matrices) and arrives on A_full.
-//  * 1 MMA warp: one thread issues the 3 x kp/16 MMAs of a tile (M = 128, N = 256: all 16 s x 16 r
-//    columns in one instruction, so A is gathered once per tile) into one of two 256-column FP32
-//    accumulators in tensor memory and commits them to A_empty and ACC_full.
+//  * MMA issue (thread 0, after its own row): the 3 x kp/16 MMAs of a tile (M = 128, N = 256: all
+//    16 s x 16 r columns in one instruction, so A is gathered once per tile) into one of two
+//    256-column FP32 accumulators in tensor memory, committed to A_empty and ACC_full.
 //  * 12 scatter warps (three per 32-lane quarter of the accumulator, each taking every third s):
 //    read the finished accumulator with tcgen05.ld, add the fixed-point contributions into the
 //    sigma row and arrive on ACC_empty, so the MMAs of tile t + 1 overlap the scatter of tile t.
@@ -52,10 +52,9 @@ namespace f2g {
 
 namespace {
 
-constexpr int kProdWarps = 4;   // producer warps: one thread per row of the A tile
+constexpr int kProdWarps = 4;   // producer warps: one thread per row of the A tile (thread 0 issues the MMAs)
 constexpr int kScatWarps = 12;  // scatter warps: three per lane quarter of the accumulator
-constexpr int kMmaWarp = kProdWarps + kScatWarps;
-constexpr int kTcThreads = (kMmaWarp + 1) * 32;
+constexpr int kTcThreads = (kProdWarps + kScatWarps) * 32; // 16 warps: 4 per SM sub-partition, 128 registers
 constexpr int kTcM = 128;      // beta strings per tile (accumulator lanes)
 constexpr int kTcN = 256;      // 16 values of s x 16 values of r
 constexpr int kTcMaxK = 80;    // padded alpha-excitation count (na * (n - na + 1) <= 72 for n <= 16)
@@ -253,7 +252,7 @@ __global__ void k_absmax(int64_t nd, const float* __restrict__ x, unsigned int* 
     }
 }
 
-__global__ void __maxnreg__(120)
+__global__ void __launch_bounds__(kTcThreads, 1)
     k_opposite_tc(int n, int na, int nb, int ma, int64_t N0a, int N0b, const uint32_t* __restrict__ down_a,
                   const uint32_t* __restrict__ up_a, const uint64_t* __restrict__ str_b,
                   const uint32_t* __restrict__ exc_b, const float* __restrict__ V,
@@ -290,7 +289,7 @@ __global__ void __maxnreg__(120)
         }
         sh.abort = 0;
     }
-    if (warp == kMmaWarp) {
+    if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh.tmem_base)),
                      "r"(kTcCols)
                      : "memory");
@@ -375,10 +374,32 @@ __global__ void __maxnreg__(120)
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(a_full);
+                if (tid == 0) {
+                    // ---- MMA issue: D[buf] = A B over kp / 16 steps of K = 16, three split products
+                    const int buf = (int)(g & 1);
+                    if (!mbar_wait(a_full, (uint32_t)(g & 1), poll_limit, &sh.abort) ||
+                        (g >= 2 && !mbar_wait(acc_empty[buf], (uint32_t)(((g >> 1) - 1) & 1), poll_limit, &sh.abort))) {
+                        give_up();
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t ahi = smem_u32(sh.a_hi), alo = smem_u32(sh.a_lo);
+                    const uint32_t bhi = smem_u32(sh.b_hi), blo = smem_u32(sh.b_lo);
+                    const uint32_t acc = tmem + (uint32_t)buf * kTcN;
+                    for (int kk = 0; kk < kp / 16; ++kk) {
+                        const uint32_t adv = (uint32_t)kk * 2 * lbo; // 16 FP16 = two core matrices along K
+                        mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), kk > 0);
+                        mma_f16(acc, smem_desc(alo + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), 1);
+                        mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(blo + adv, lbo, sbo), 1);
+                    }
+                    mma_commit(a_empty);
+                    mma_commit(acc_full[buf]);
+                    last_g = g;
+                }
                 if (t + 1 < ntile)
                     request((t + 1) * kTcM);
             }
-        } else if (warp < kMmaWarp) {
+        } else {
             // ---- scatter: lanes 32 q .. +31 of the accumulator (q = warp mod 4, the quarter this warp
             // may read), every third s from grp on
             const int q = warp & 3, grp = (warp - kProdWarps) >> 2;
@@ -441,35 +462,6 @@ __global__ void __maxnreg__(120)
                 if (lane == 0)
                     mbar_arrive(acc_empty[buf]);
             }
-        } else if (lane == 0) {
-            // ---- MMA issue: D[buf] = A B over kp / 16 steps of K = 16, three split products each
-            const uint32_t ahi = smem_u32(sh.a_hi), alo = smem_u32(sh.a_lo);
-            const uint32_t bhi = smem_u32(sh.b_hi), blo = smem_u32(sh.b_lo);
-            for (int t = 0; t < ntile; ++t) {
-                const long long g = g0 + t;
-                const int buf = (int)(g & 1);
-                if (sh.abort)
-                    break;
-                if (!mbar_wait(a_full, (uint32_t)(g & 1), poll_limit, &sh.abort)) {
-                    give_up();
-                    break;
-                }
-                if (g >= 2 && !mbar_wait(acc_empty[buf], (uint32_t)(((g >> 1) - 1) & 1), poll_limit, &sh.abort)) {
-                    give_up();
-                    break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t acc = tmem + (uint32_t)buf * kTcN;
-                for (int kk = 0; kk < kp / 16; ++kk) {
-                    const uint32_t adv = (uint32_t)kk * 2 * lbo; // 16 FP16 = two core matrices along K
-                    mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), kk > 0);
-                    mma_f16(acc, smem_desc(alo + adv, lbo, sbo), smem_desc(bhi + adv, lbo, sbo), 1);
-                    mma_f16(acc, smem_desc(ahi + adv, lbo, sbo), smem_desc(blo + adv, lbo, sbo), 1);
-                }
-                mma_commit(a_empty);
-                mma_commit(acc_full[buf]);
-                last_g = g;
-            }
         }
         __syncwarp();
         __syncthreads(); // every tile of Ja scattered (so every MMA of it complete), or an abort
@@ -483,13 +475,13 @@ __global__ void __maxnreg__(120)
     }
     // after an abort, MMAs may still be running: wait (bounded) for the last commit before the tensor
     // memory they write is released (a no-op when every tile was scattered)
-    if (warp == kMmaWarp && lane == 0 && last_g >= 0)
+    if (tid == 0 && last_g >= 0)
         (void)mbar_wait(acc_full[last_g & 1], (uint32_t)((last_g >> 1) & 1), (1ll << 26));
     __syncwarp();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (warp == kMmaWarp)
+    if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
 }
 
