@@ -319,6 +319,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             sh.sfa[tid] = (e_neg(ep) ^ e_neg(eq)) ? -fa : fa; // the alpha sign is folded into A
             sh.pk[tid] = e_orb(ep);
             sh.qk[tid] = e_orb(eq);
+        } else if (tid < kTcMaxK) { // padding columns of K: zero factors (never uninitialised memory)
+            sh.rowp[tid] = C;
+            sh.sfa[tid] = 0.0f;
+            sh.pk[tid] = 0;
+            sh.qk[tid] = 0;
         }
         for (int c = tid; c < N0b; c += kTcThreads)
             row[c] = 0ull;

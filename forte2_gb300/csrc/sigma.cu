@@ -211,6 +211,15 @@ __global__ void k_scale(int64_t n, double a, const double* in, double* out) {
 }
 
 // ---- opposite spin ----------------------------------------------------------------------------
+// x with its sign flipped when neg is 1, by an integer XOR of the sign bit: the FP64 pipe (the
+// bound of the FP64 kernel) is left to the multiply-adds
+__device__ __forceinline__ double flip(double x, int neg) {
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)neg << 63));
+}
+__device__ __forceinline__ float flip(float x, int neg) {
+    return __uint_as_float(__float_as_uint(x) ^ ((unsigned)neg << 31));
+}
+
 // One CTA per output alpha string Ja. MB bounds mb = n - nb + 1 (beta holes per 1-hole string).
 // SMROW: sigma(Ja,:) lives in shared memory; otherwise the phased updates go to global memory.
 template <typename T, int MB, bool SMROW>
@@ -275,7 +284,7 @@ __global__ void __launch_bounds__(512, 1)
                 T d[MB];
 #pragma unroll
                 for (int si = 0; si < MB; ++si)
-                    d[si] = (negq ^ e_neg(ub[si])) ? -dn[si] : dn[si];
+                    d[si] = flip(dn[si], negq ^ e_neg(ub[si]));
                 if (qi + 1 < ma) {
                     const T* crow = C + (int64_t)e_addr(ua[qi + 1]) * N0b;
 #pragma unroll
@@ -297,19 +306,17 @@ __global__ void __launch_bounds__(512, 1)
                     }
                 }
             }
-            // Owner-ordered scatter, one phase per created orbital r: within a phase Kb -> Kb + r is
-            // one-to-one, so plain read-add-writes never collide, and every sigma element receives
-            // its contributions in the fixed order (Kb round, r): the result is bitwise the same
-            // for every launch shape and batch.
+            // Ordered scatter, one phase per created orbital r: within a phase Kb -> Kb + r is
+            // one-to-one, so no two adds of a phase reach the same element, and every sigma
+            // element receives its contributions in the fixed order (Kb round, r): the result is
+            // bitwise the same for every launch shape and batch. The adds are shared-memory atomics
+            // only because those run in the memory unit, not on the FP64 pipe that bounds this kernel.
             for (int r = 0; r < n; ++r) {
                 __syncthreads();
 #pragma unroll
                 for (int ri = 0; ri < MB; ++ri) {
-                    if (so[ri] == r) {
-                        const T x = (negp ^ e_neg(ub[ri])) ? -acc[ri] : acc[ri];
-                        T* dst = (SMROW ? row : srow) + e_addr(ub[ri]);
-                        *dst += x;
-                    }
+                    if (so[ri] == r)
+                        atomicAdd((SMROW ? row : srow) + e_addr(ub[ri]), flip(acc[ri], negp ^ e_neg(ub[ri])));
                 }
             }
         }

