@@ -120,15 +120,15 @@ class Clocks:
 
 
 def fp64_fma_peak(reps=3):
-    """FP64 FMA issue rate of this GPU from the library's own probe (k_probe_dfma: 8 independent
-    DFMA chains per thread, 4 blocks of 256 threads per SM), timed with CUDA events on the
+    """FP64 FMA issue rate of this GPU from the library's own probe (k_probe_dfma: 16 independent
+    DFMA chains per thread, 8 blocks of 256 threads per SM), timed with CUDA events on the
     launching stream after one warm-up launch; the best of `reps` launches (burst), in TFLOP/s."""
     import torch
 
     from forte2_gb300._lib import check, lib, stream_handle
 
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    blocks, threads, iters = 4 * sms, 256, 1 << 16
+    blocks, threads, iters = 8 * sms, 256, 1 << 14
     out = torch.empty(blocks, dtype=torch.float64, device="cuda")
     st = torch.cuda.current_stream()
     check(lib().f2g_probe_dfma(blocks, threads, iters, out.data_ptr(), stream_handle()))
@@ -139,7 +139,7 @@ def fp64_fma_peak(reps=3):
         check(lib().f2g_probe_dfma(blocks, threads, iters, out.data_ptr(), stream_handle()))
         e1.record(st)
         torch.cuda.synchronize()
-        best = max(best, 16.0 * blocks * threads * iters / (e0.elapsed_time(e1) / 1e3) / 1e12)
+        best = max(best, 32.0 * blocks * threads * iters / (e0.elapsed_time(e1) / 1e3) / 1e12)
     assert bool(torch.isfinite(out).all())
     return best
 

@@ -238,8 +238,8 @@ int f2g_sigma_set_hamiltonian_async(void* sigma, double E, const double* host_H,
                                     void* stream);
 
 /* ---- measurement ---------------------------------------------------------------------------- */
-/* FP64 FMA issue-rate probe: blocks x threads threads each run 8 independent DFMA chains of
- * `iters` steps (16 blocks threads iters FLOP); dev_out[blocks] receives the chains' sums. The
+/* FP64 FMA issue-rate probe: blocks x threads threads each run 16 independent DFMA chains of
+ * `iters` steps (32 blocks threads iters FLOP); dev_out[blocks] receives the chains' sums. The
  * roofline denominator of the FP64 sigma kernels, timed by the caller. No reference counterpart. */
 int f2g_probe_dfma(int blocks, int threads, int64_t iters, double* dev_out, void* stream);
 
