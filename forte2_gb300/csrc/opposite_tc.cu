@@ -25,18 +25,21 @@
 // is bitwise the same for every grid, batch and run. The row is converted back and added to the
 // same-spin terms in FP32 once per alpha string.
 //
-// One CTA per SM (persistent over Ja), 16 warps in three roles that hand tiles to each other
+// One CTA per SM (persistent over Ja), 24 warps in three roles that hand tiles to each other
 // through mbarriers (every wait bounded):
-//  * 4 producer warps: thread m owns row m (beta string ib0 + m) of the A tile. It requests the K
-//    gathered values of the next tile into registers while the tensor cores work on the current
-//    one, then (once those MMAs have released the A buffer) scales, splits and stores them in the
-//    canonical K-major no-swizzle layout (8-row x 16-byte core matrices) and arrives on A_full.
+//  * 8 producer warps: threads m and m + 128 own the two halves (k < 40, k >= 40) of row m (beta
+//    string ib0 + m) of the A tile. They request the gathered values of the next tile into
+//    registers while the tensor cores work on the current one, then (once those MMAs have released
+//    the A buffer) scale, split and store them in the canonical K-major no-swizzle layout (8-row x
+//    16-byte core matrices) and arrive on A_full.
 //  * MMA issue (thread 0, after its own row): the 3 x kp/16 MMAs of a tile (M = 128, N = 256: all
 //    16 s x 16 r columns in one instruction, so A is gathered once per tile) into one of two
 //    256-column FP32 accumulators in tensor memory, committed to A_empty and ACC_full.
-//  * 12 scatter warps (three per 32-lane quarter of the accumulator, each taking every third s):
+//  * 16 scatter warps (four per 32-lane quarter of the accumulator, each taking every fourth s):
 //    read the finished accumulator with tcgen05.ld, add the fixed-point contributions into the
 //    sigma row and arrive on ACC_empty, so the MMAs of tile t + 1 overlap the scatter of tile t.
+//    An r slot runs only if some lane of the warp has it (uniform branch: neighbouring strings
+//    mostly agree on the low orbitals).
 // B = V' for the alpha string is built by all warps between alpha strings. A wait that gives up
 // sets the error flag and the CTA leaves its loops, waits (bounded again) for the MMAs it has
 // committed and releases its tensor memory. An error flag of 1 means that the sigma of that call
@@ -52,13 +55,13 @@ namespace f2g {
 
 namespace {
 
-constexpr int kProdWarps = 4;   // producer warps: one thread per row of the A tile (thread 0 issues the MMAs)
-constexpr int kScatWarps = 12;  // scatter warps: three per lane quarter of the accumulator
-constexpr int kTcThreads = (kProdWarps + kScatWarps) * 32; // 16 warps: 4 per SM sub-partition, 128 registers
+constexpr int kProdWarps = 8;   // producer warps: two threads per row of the A tile (thread 0 issues the MMAs)
+constexpr int kScatWarps = 16;  // scatter warps: four per lane quarter of the accumulator
+constexpr int kTcThreads = (kProdWarps + kScatWarps) * 32; // 24 warps: 6 per SM sub-partition, 80 registers
+constexpr int kProdHalf = 40;   // k values per producer thread (half of the padded K)
 constexpr int kTcM = 128;      // beta strings per tile (accumulator lanes)
 constexpr int kTcN = 256;      // 16 values of s x 16 values of r
 constexpr int kTcMaxK = 80;    // padded alpha-excitation count (na * (n - na + 1) <= 72 for n <= 16)
-constexpr int kTcK = 72;       // largest alpha-excitation count
 constexpr int kTcCols = 512;   // tensor-memory columns allocated: two 256-column accumulators
 constexpr int kFixShift = 18;  // fixed-point fraction bits (in units of the scaled product)
 
@@ -161,12 +164,16 @@ __device__ __forceinline__ int split_exponent(float m) {
 // x (FP32 bits, |x| < 2^37) times 2^kFixShift, truncated toward zero, as a two's-complement 64-bit
 // integer, negated when `neg` is set. Integer operations only: the same bits on every run.
 __device__ __forceinline__ unsigned long long fixed_point(uint32_t b, uint32_t neg) {
-    const uint32_t e = (b >> 23) & 0xFFu;
     const uint32_t m = (b & 0x7FFFFFu) | 0x800000u;
-    int sh = (int)e - (127 + 23 - kFixShift); // x 2^kFixShift = m 2^sh
-    sh = sh > 40 ? 40 : sh;                    // only for values outside the bound (not finite)
-    unsigned long long q = sh >= 0 ? ((unsigned long long)m << sh) : (sh > -24 ? (unsigned long long)(m >> -sh) : 0ull);
-    q = e ? q : 0ull; // zero or subnormal: below the resolution
+    const int sh = (int)((b >> 23) & 0xFFu) - (127 + 23 - kFixShift); // x 2^kFixShift = m 2^sh
+    // m 2^sh as (hi, lo) words with clamped 32-bit shifts: a left shift by sh (<= 31 inside the
+    // bound), a right shift by -sh (a shift by 32 or more gives 0, which also covers zero and
+    // subnormal inputs)
+    uint32_t lo_l, lo_r, hi;
+    asm("shl.b32 %0, %1, %2;" : "=r"(lo_l) : "r"(m), "r"(sh));
+    asm("shr.b32 %0, %1, %2;" : "=r"(lo_r) : "r"(m), "r"(-sh));
+    asm("shf.l.clamp.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(m), "r"(0u), "r"(sh > 0 ? sh : 0));
+    const unsigned long long q = ((unsigned long long)hi << 32) | (lo_l | lo_r);
     return (((b >> 31) ^ neg) & 1u) ? (0ull - q) : q;
 }
 
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t lbo = 128, sbo = (uint32_t)(kp >> 3) * 128;
 
     if (tid == 0) {
-        mbar_init(a_full, kTcM);
+        mbar_init(a_full, kProdWarps * 32);
         mbar_init(a_empty, 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(acc_full[b], 1);
@@ -347,15 +354,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         __syncthreads();
 
         if (warp < kProdWarps) {
-            // ---- producer: row m of A for every tile of this alpha string
-            const int m = tid;
-            float x[kTcK];
+            // ---- producer: half h of row m of A (k in [40 h, 40 h + 40)) for every tile of Ja
+            const int m = tid & (kTcM - 1), h = tid >> 7, kb = h * kProdHalf;
+            float x[kProdHalf];
             auto request = [&](int ib0) {
                 const int Ib = ib0 + m;
                 const bool in = Ib < N0b;
 #pragma unroll
-                for (int k = 0; k < kTcK; ++k)
-                    x[k] = (k < K && in) ? __ldg(sh.rowp[k] + Ib) : 0.0f;
+                for (int i = 0; i < kProdHalf; ++i)
+                    x[i] = (kb + i < K && in) ? __ldg(sh.rowp[kb + i] + Ib) : 0.0f;
             };
             request(0);
             for (int t = 0; t < ntile; ++t) {
@@ -367,13 +374,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     break;
                 }
 #pragma unroll
-                for (int j = 0; j < kTcMaxK / 8; ++j) {
-                    if (8 * j < kp) {
+                for (int j = 0; j < kProdHalf / 8; ++j) {
+                    if (kb + 8 * j < kp) {
                         float v[8];
 #pragma unroll
                         for (int c = 0; c < 8; ++c)
-                            v[c] = (8 * j + c < kTcK) ? x[8 * j + c] * sh.sfa[8 * j + c] : 0.0f;
-                        const uint32_t off = kmajor_off(m, 8 * j, kp) >> 1;
+                            v[c] = x[8 * j + c] * sh.sfa[kb + 8 * j + c];
+                        const uint32_t off = kmajor_off(m, kb + 8 * j, kp) >> 1;
                         split_store(v, sh.a_hi + off, sh.a_lo + off);
                     }
                 }
@@ -406,8 +413,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
         } else {
             // ---- scatter: lanes 32 q .. +31 of the accumulator (q = warp mod 4, the quarter this warp
-            // may read), every third s from grp on
+            // may read), every fourth s from grp on
             const int q = warp & 3, grp = (warp - kProdWarps) >> 2;
+            const uint32_t nmask = (1u << n) - 1u;
             const uint32_t lane_base = (uint32_t)(q * 32) << 16;
             for (int t = 0; t < ntile; ++t) {
                 const long long g = g0 + t;
@@ -443,22 +451,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     }
                 };
                 request(grp);
-                for (int s = grp; s < n; s += 3) {
+                for (int s = grp; s < n; s += kScatWarps / 4) {
                     const bool has = valid && (mI >> s & 1);
                     const uint32_t e[16] = {en[0].x, en[0].y, en[0].z, en[0].w, en[1].x, en[1].y, en[1].z, en[1].w,
                                             en[2].x, en[2].y, en[2].z, en[2].w, en[3].x, en[3].y, en[3].z, en[3].w};
-                    request(s + 3);
-                    if (!__any_sync(0xffffffffu, has))
+                    request(s + kScatWarps / 4);
+                    // r valid: r not in Ib - s (and r < n); the union over the warp decides which r
+                    // slots the warp runs at all (uniform branches: the low orbitals of neighbouring
+                    // strings mostly agree)
+                    const uint32_t vm = has ? (~(uint32_t)(mI & ~(uint64_t(1) << s)) & nmask) : 0u;
+                    const uint32_t U = __reduce_or_sync(0xffffffffu, vm);
+                    if (!U)
                         continue;
                     uint32_t v[16];
                     tmem_ld16(acc + (uint32_t)(s * 16), v);
                     tmem_wait_ld();
-                    if (has) {
 #pragma unroll
-                        for (int r = 0; r < 16; ++r) {
-                            const uint32_t jb = e[r] & 0x00FFFFFFu;
-                            if (jb != 0x00FFFFFFu) // the sign bit of the entry flips the sign of the value
-                                atomicAdd(row + jb, fixed_point(v[r], e[r] >> 31));
+                    for (int r = 0; r < 16; ++r) {
+                        if (U >> r & 1) {
+                            if (vm >> r & 1) // the sign bit of the entry flips the sign of the value
+                                atomicAdd(row + (e[r] & 0x00FFFFFFu), fixed_point(v[r], e[r] >> 31));
                         }
                     }
                 }
