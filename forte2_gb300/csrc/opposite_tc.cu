@@ -17,10 +17,11 @@
 // the dropped lo*lo term is below FP32 rounding). The error against the FP64 sigma is that of an
 // FP32 evaluation (1e-7 relative).
 //
-// Determinism: sigma(Ja, :) is accumulated in shared memory as 64-bit fixed point. Every product
-// sum is bounded by construction (|A|, |B| < 2^15, K <= 72, so |U| < 2^37 in scaled units), is
-// truncated to a multiple of 2^-18 of the scaled unit by integer arithmetic, and at most
-// nb (n - nb + 1) <= 72 of them reach one element, so the sum stays below 2^62 and is exact.
+// Determinism: sigma(Ja, :) is accumulated in shared memory in fixed point, as two 32-bit integer
+// rows. Every product sum is bounded by construction (|A|, |B| < 2^15, K <= 72, so |U| < 2^37 in
+// scaled units) and is rounded to a multiple of 2^-7 scaled units, split exactly into a high part
+// (units of 2^15) and a low part (units of 2^-7), each below 2^21.2 in magnitude; at most
+// nb (n - nb + 1) <= 72 of them reach one element, so both sums stay below 2^28 and are exact.
 // Integer addition does not depend on the order of the shared-memory atomics: the sigma of a vector
 // is bitwise the same for every grid, batch and run. The row is converted back and added to the
 // same-spin terms in FP32 once per alpha string.
@@ -63,7 +64,6 @@ constexpr int kTcM = 128;      // beta strings per tile (accumulator lanes)
 constexpr int kTcN = 256;      // 16 values of s x 16 values of r
 constexpr int kTcMaxK = 80;    // padded alpha-excitation count (na * (n - na + 1) <= 72 for n <= 16)
 constexpr int kTcCols = 512;   // tensor-memory columns allocated: two 256-column accumulators
-constexpr int kFixShift = 18;  // fixed-point fraction bits (in units of the scaled product)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -161,20 +161,19 @@ __device__ __forceinline__ int split_exponent(float m) {
     return e < -120 ? -120 : (e > 120 ? 120 : e);
 }
 
-// x (FP32 bits, |x| < 2^37) times 2^kFixShift, truncated toward zero, as a two's-complement 64-bit
-// integer, negated when `neg` is set. Integer operations only: the same bits on every run.
-__device__ __forceinline__ unsigned long long fixed_point(uint32_t b, uint32_t neg) {
-    const uint32_t m = (b & 0x7FFFFFu) | 0x800000u;
-    const int sh = (int)((b >> 23) & 0xFFu) - (127 + 23 - kFixShift); // x 2^kFixShift = m 2^sh
-    // m 2^sh as (hi, lo) words with clamped 32-bit shifts: a left shift by sh (<= 31 inside the
-    // bound), a right shift by -sh (a shift by 32 or more gives 0, which also covers zero and
-    // subnormal inputs)
-    uint32_t lo_l, lo_r, hi;
-    asm("shl.b32 %0, %1, %2;" : "=r"(lo_l) : "r"(m), "r"(sh));
-    asm("shr.b32 %0, %1, %2;" : "=r"(lo_r) : "r"(m), "r"(-sh));
-    asm("shf.l.clamp.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(m), "r"(0u), "r"(sh > 0 ? sh : 0));
-    const unsigned long long q = ((unsigned long long)hi << 32) | (lo_l | lo_r);
-    return (((b >> 31) ^ neg) & 1u) ? (0ull - q) : q;
+// Adds x (FP32 bits, |x| < 2^37 in scaled units; sign flipped when neg is 1) to the fixed-point
+// element jb as two exact integers: hi = round(x / 2^15) into row_hi and lo = round((x - hi 2^15)
+// 2^7) into row_lo, so the element holds (hi 2^22 + lo) 2^-7. Both parts come from FP32
+// multiply-adds on a 1.5 2^23 offset (the float bits of C + y are C's bits + y for an integer
+// |y| < 2^22); |hi|, |lo| < 2^21.2, so up to 72 of them sum exactly in 32 bits.
+__device__ __forceinline__ void add_fixed(int* row_hi, int* row_lo, uint32_t jb, uint32_t b, uint32_t neg) {
+    const float C = 12582912.0f; // 1.5 2^23
+    const float x = __uint_as_float(b ^ (neg << 31));
+    const float t = fmaf(x, 0x1p-15f, C);                  // C + round(x / 2^15)
+    const float rem = fmaf(-(t - C), 32768.0f, x);          // x - hi 2^15, exact, |rem| <= 2^14
+    const float u = fmaf(rem, 128.0f, C);                    // C + round(rem 2^7)
+    atomicAdd(row_hi + jb, __float_as_int(t) - __float_as_int(C));
+    atomicAdd(row_lo + jb, __float_as_int(u) - __float_as_int(C));
 }
 
 struct TcShared {
@@ -268,8 +267,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                   long long poll_limit) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TcShared& sh = *reinterpret_cast<TcShared*>(smem_raw);
-    // sigma(Ja, :) in 64-bit fixed point, N0b elements
-    unsigned long long* row = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(TcShared));
+    // sigma(Ja, :) in fixed point: high and low 32-bit parts, N0b elements each
+    int* row_hi = reinterpret_cast<int*>(smem_raw + sizeof(TcShared));
+    int* row_lo = row_hi + N0b;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = na * ma, kp = (K + 15) & ~15;
     const int ntile = (N0b + kTcM - 1) / kTcM;
@@ -277,11 +277,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     sig += blockIdx.y * N0a * (int64_t)N0b;
     // operand scales 2^ea (C) and 2^eb (V) from the largest magnitudes, read from device memory (so
     // captured graphs follow new vectors and integrals); the fixed-point row is in units of
-    // 2^-(ea + eb + kFixShift)
+    // 2^-(ea + eb + 7)
     const int ea = split_exponent(__uint_as_float(cmax[blockIdx.y]));
     const int eb = split_exponent(__uint_as_float(vmax[0]));
     const float fa = pow2f(ea), fb = pow2f(eb);
-    const float unscale0 = pow2f(-kFixShift), unscale1 = pow2f(-ea), unscale2 = pow2f(-eb);
+    const float unscale0 = pow2f(-7), unscale1 = pow2f(-ea), unscale2 = pow2f(-eb);
     const uint32_t a_full = smem_u32(&sh.a_full), a_empty = smem_u32(&sh.a_empty);
     const uint32_t acc_full[2] = {smem_u32(&sh.acc_full[0]), smem_u32(&sh.acc_full[1])};
     const uint32_t acc_empty[2] = {smem_u32(&sh.acc_empty[0]), smem_u32(&sh.acc_empty[1])};
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             sh.qk[tid] = 0;
         }
         for (int c = tid; c < N0b; c += kTcThreads)
-            row[c] = 0ull;
+            row_hi[c] = row_lo[c] = 0;
         __syncthreads();
         // B = V'[(s, r)][k] 2^eb (zero outside the space); one 16-byte row of 8 k per task
         for (int t = tid; t < kTcN * (kp >> 3); t += kTcThreads) {
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     for (int r = 0; r < 16; ++r) {
                         if (U >> r & 1) {
                             if (vm >> r & 1) // the sign bit of the entry flips the sign of the value
-                                atomicAdd(row + (e[r] & 0x00FFFFFFu), fixed_point(v[r], e[r] >> 31));
+                                add_fixed(row_hi, row_lo, e[r] & 0x00FFFFFFu, v[r], e[r] >> 31);
                         }
                     }
                 }
@@ -484,7 +484,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         __syncthreads(); // every tile of Ja scattered (so every MMA of it complete), or an abort
         if (!sh.abort)
             for (int c = tid; c < N0b; c += kTcThreads) {
-                const float x = __ll2float_rn((long long)row[c]) * unscale0 * unscale1 * unscale2;
+                const long long q = ((long long)row_hi[c] << 22) + row_lo[c]; // units of 2^-7
+                const float x = __ll2float_rn(q) * unscale0 * unscale1 * unscale2;
                 srow[c] += x;
             }
         g0 += ntile;
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
 }
 
-size_t opposite_tc_smem(int N0b) { return sizeof(TcShared) + (size_t)N0b * sizeof(unsigned long long); }
+size_t opposite_tc_smem(int N0b) { return sizeof(TcShared) + (size_t)N0b * 2 * sizeof(int); }
 
 bool opposite_tc_supported(const CIStrings* s) {
     const int n = s->norb;

@@ -11,6 +11,9 @@ namespace f2g {
 constexpr int kChains = 16;
 
 __global__ void k_probe_dfma(long long iters, double x, double y, double* __restrict__ out) {
+    // x and y in registers (opaque to the optimiser), as the sigma kernels' operands are: a DFMA
+    // with a constant-bank operand is not what the pipe runs there
+    asm volatile("" : "+d"(x), "+d"(y));
     double a[kChains];
 #pragma unroll
     for (int c = 0; c < kChains; ++c)
