@@ -144,6 +144,25 @@ def fp64_fma_peak(reps=3):
     return best
 
 
+def _measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def fp64_nominal_peak(sm_mhz):
+    """GB300's FP64 rate, 4 FLOP (2 DFMA) per clock per SM, at the median SM clock sampled during
+    the run (1.26 TFLOP/s at 2070 MHz; the nominal 1.25 TFLOP/s). The library's own issue-rate
+    probe is reported beside it: it stays below what the opposite-spin kernel itself sustains, so it
+    cannot serve as the ceiling."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    return 4.0 * sms * (sm_mhz or 2070.0) * 1e6 / 1e12
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -272,6 +291,7 @@ def run_gb300(a):
     torch.cuda.synchronize()
     barrier(dist)
     clk = clocks.stop()
+    peak64 = fp64_nominal_peak(clk.get("sm_mhz"))
     t_local = ev0.elapsed_time(ev1) / 1e3
     t = max_over_ranks(t_local, dist)
     value = replica_rate(a.steps, t_local, dist)
@@ -297,6 +317,7 @@ def run_gb300(a):
     # mixed mode (FP32 sigma) throughput, same workload
     mixed = None
     mixed_terms = None
+    tc_roof = None
     if not a.no_mixed:
         sb.set_precision("fp32")
         for _ in range(2):
@@ -311,6 +332,20 @@ def run_gb300(a):
         mixed = world * a.steps / max_over_ranks(e0.elapsed_time(e1) / 1e3, dist)
         mt = sb.avg_build_time()
         mixed_terms = {"total": 1e3 * mt[0], "aabb": 1e3 * mt[1], "aaaa_h1a_h0": 1e3 * mt[2], "bbbb_h1b": 1e3 * mt[3]}
+        if sb.set_tensor_cores(True):
+            # k_opposite_tc: 3 split-FP16 products of M = 128, N = 256, K padded to 16, per tile of
+            # 128 beta strings, per alpha string; against the measured dense BF16/FP16 GEMM peak
+            from math import comb
+
+            kp = (na * (a.norb - na + 1) + 15) // 16 * 16
+            tiles = comb(a.norb, na) * ((comb(a.norb, nb) + 127) // 128)
+            tc_flop = 3 * 2 * 128 * 256 * kp * tiles
+            bf16 = _measured_peaks().get("bf16_tflops", 1900.0)
+            tc_roof = {"bound": "tensor", "kernel": "k_opposite_tc (FP32 opposite-spin sigma, split FP16)",
+                       "flop_per_launch": tc_flop, "launch_ms": mt[1] * 1e3,
+                       "achieved": tc_flop / mt[1] / 1e12, "peak": bf16, "unit": "TFLOP/s",
+                       "frac": tc_flop / mt[1] / 1e12 / bf16,
+                       "peak_source": "MEASURED_PEAKS.json bf16_tflops (dense FP16 runs at the BF16 rate)"}
         sb.set_precision("fp64")
     davidson = None
     if rank == 0 and world == 1 and not a.no_davidson and a.norb == NORB:
@@ -332,13 +367,16 @@ def run_gb300(a):
                     "d2h_bytes_per_step": 8 * ndet},
             "gpu_launches": 5 * a.steps,
             "roofline": {"bound": "compute", "pipe": "fp64", "kernel": "k_opposite (opposite-spin sigma)",
-                         "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp64_peak, "traffic": opposite_traffic(a.norb, na, nb),
+                         "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                         "frac": achieved / peak64, "traffic": opposite_traffic(a.norb, na, nb),
                          "traffic_source": "dram read+write per gathered C element of the ncu capture at "
                                            "CAS(15e,15o) (profiles/k_opposite_fp64_cas15.md: 5.04 GB for "
                                            "2.09e10 elements), times this launch's gathered elements",
-                         "peak_source": "measured in this run: the library's DFMA issue-rate probe "
-                                        "(k_probe_dfma, best of 3 launches, CUDA events)",
+                         "peak_source": "FP64 rate 4 FLOP/clk/SM x SMs x median SM clock sampled in this run "
+                                        "(no FP64 entry in MEASURED_PEAKS.json)",
+                         "probe_tflops": fp64_peak, "frac_of_probe": achieved / fp64_peak,
+                         "probe_source": "the library's DFMA issue-rate probe (k_probe_dfma, 16 chains per thread, "
+                                         "best of 3 launches, CUDA events), measured in this run",
                          "fp64_dgemm_tflops": FP64_DGEMM_TFLOPS, "frac_of_dgemm": achieved / FP64_DGEMM_TFLOPS,
                          "flops_per_launch": f_sp["ab"], "launch_ms": 1e3 * t_ab,
                          # the reference's dense HZ product counts n^2 x n^2 blocks whose D rows are
@@ -353,6 +391,7 @@ def run_gb300(a):
                                                     for p, r in tuned.items()},
             "davidson": davidson,
             "mixed_fp32_sigma_builds_per_s": mixed,
+            "tensor_core_roofline": tc_roof,
             "mixed_fp32_terms_ms": mixed_terms,
             "clocks": clk,
             "cpu_baseline": cpu,
@@ -600,10 +639,11 @@ def run_rdm(a):
                    "d2h_bytes_per_step": (n * n + n ** 4) * 8},
            "roofline": {"bound": "compute", "pipe": "fp64", "kernel": "k_rdm_ab (mixed-spin 2-RDM, with its mirror)",
                         "achieved": ab_flop / ab_s / 1e12,
-                        "peak": fp64_peak, "unit": "TFLOP/s", "frac": ab_flop / ab_s / 1e12 / fp64_peak,
+                        "peak": fp64_nominal_peak(clk.get("sm_mhz")), "unit": "TFLOP/s",
+                        "frac": ab_flop / ab_s / 1e12 / fp64_nominal_peak(clk.get("sm_mhz")),
                         "flop_per_launch": ab_flop, "ms": ab_s * 1e3, "traffic": None,
-                        "peak_source": "measured in this run: the library's DFMA issue-rate probe (k_probe_dfma)",
-                        "fp64_dgemm_tflops": FP64_DGEMM_TFLOPS},
+                        "peak_source": "FP64 rate 4 FLOP/clk/SM x SMs x median SM clock sampled in this run",
+                        "probe_tflops": fp64_peak, "fp64_dgemm_tflops": FP64_DGEMM_TFLOPS},
            "clocks": clk,
            # per set: k_rdm_hole<1> x2, k_transpose x2, k_rdm_ab, its mirror, k_rdm_hole<2> x2, k_rdm_sf2
            "gpu_launches": 9 * a.steps}
