@@ -180,6 +180,134 @@ __global__ void __launch_bounds__(128) k_spmm_rows(int64_t nrows, int ncols, int
     }
 }
 
+// ---- grouped FP32 same-spin SpMM -------------------------------------------------------------
+// Output rows are taken kSsGroup at a time: consecutive strings share most of the strings within
+// two replacements of them (at CAS(16,16) the union of 8 rows' 849 inputs is ~42% of 8 x 849), so
+// the group reads each input row once and applies it to all its rows. The same-spin term is bound
+// by these row reads (L2), not by arithmetic.
+
+// Build pass (one block per group): the group's (input row, slot) keys sorted in shared memory
+// (bitonic), slot = j * nnz + k for entry k of row g*G + j. fill = 0 counts the distinct input
+// rows into count[g]; fill = 1 writes gcol and gval from goff.
+__global__ void k_group_build(int64_t nrows, int nnz, const int32_t* __restrict__ col, const float* __restrict__ valf,
+                              int S, int fill, int64_t* __restrict__ count, const int64_t* __restrict__ goff,
+                              int32_t* __restrict__ gcol, float* __restrict__ gval) {
+    extern __shared__ unsigned long long keys[]; // S keys, then S floats
+    float* vals = reinterpret_cast<float*>(keys + S);
+    __shared__ int part[1024];
+    const int64_t g = blockIdx.x, J0 = g * kSsGroup;
+    const int tid = threadIdx.x, T = blockDim.x;
+    for (int i = tid; i < S; i += T) {
+        const int j = i / nnz, k = i - j * nnz;
+        if (j < kSsGroup && J0 + j < nrows) {
+            keys[i] = ((unsigned long long)(uint32_t)col[(J0 + j) * nnz + k] << 32) | (unsigned)i;
+            vals[i] = valf[(J0 + j) * nnz + k];
+        } else {
+            keys[i] = ~0ull;
+        }
+    }
+    __syncthreads();
+    for (int k = 2; k <= S; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < S; i += T) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = keys[i], b = keys[ixj];
+                    if ((a > b) == ((i & k) == 0)) {
+                        keys[i] = b;
+                        keys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    // a new input row starts where the row index changes; each thread scans a contiguous segment
+    const int seg = (S + T - 1) / T, i0 = tid * seg;
+    int n_new = 0;
+    for (int i = i0; i < i0 + seg && i < S; ++i)
+        n_new += keys[i] != ~0ull && (i == 0 || (keys[i] >> 32) != (keys[i - 1] >> 32));
+    part[tid] = n_new;
+    __syncthreads();
+    if (!fill) {
+        if (tid == 0) {
+            int64_t c = 0;
+            for (int t = 0; t < T; ++t)
+                c += part[t];
+            count[g] = c;
+        }
+        return;
+    }
+    int before = 0; // exclusive prefix over the threads before this one
+    for (int t = 0; t < tid; ++t)
+        before += part[t];
+    const int64_t base = goff[g], nu = goff[g + 1] - base;
+    for (int64_t e = tid; e < nu * kSsGroup; e += T)
+        gval[base * kSsGroup + e] = 0.0f;
+    __syncthreads();
+    int u = before - 1;
+    for (int i = i0; i < i0 + seg && i < S; ++i) {
+        const unsigned long long key = keys[i];
+        if (key == ~0ull)
+            break;
+        if (i == 0 || (key >> 32) != (keys[i - 1] >> 32)) { // else: continues the row started before
+            ++u;
+            gcol[base + u] = (int32_t)(key >> 32);
+        }
+        const int slot = (int)(key & 0xffffffffu);
+        gval[(base + u) * kSsGroup + slot / nnz] = vals[slot];
+    }
+}
+
+// Y[J, :] = (accumulate ? Y[J, :] : 0) + sum_u gval[u][J - g G] X[gcol[u], :] for the rows J of
+// group g = blockIdx.x; the input rows in ascending order (a fixed summation order).
+template <int VEC>
+__global__ void __launch_bounds__(128) k_spmm_group(int64_t nrows, int ncols, const int64_t* __restrict__ goff,
+                                                    const int32_t* __restrict__ gcol, const float* __restrict__ gval,
+                                                    const float* __restrict__ X, float* __restrict__ Y, int accumulate,
+                                                    int64_t vstride) {
+    X += blockIdx.z * vstride;
+    Y += blockIdx.z * vstride;
+    const int64_t g = blockIdx.x, u0 = goff[g], u1 = goff[g + 1];
+    const int c0 = blockIdx.y * (blockDim.x * VEC) + threadIdx.x;
+    float acc[kSsGroup][VEC];
+#pragma unroll
+    for (int j = 0; j < kSsGroup; ++j)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v)
+            acc[j][v] = 0.0f;
+#pragma unroll 2
+    for (int64_t u = u0; u < u1; ++u) {
+        const float* xr = X + (int64_t)__ldg(gcol + u) * ncols;
+        float x[VEC];
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) {
+            const int c = c0 + v * blockDim.x;
+            x[v] = c < ncols ? __ldg(xr + c) : 0.0f;
+        }
+        const float4 wa = __ldg(reinterpret_cast<const float4*>(gval + u * kSsGroup));
+        const float4 wb = __ldg(reinterpret_cast<const float4*>(gval + u * kSsGroup) + 1);
+        const float w[kSsGroup] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+        for (int j = 0; j < kSsGroup; ++j)
+#pragma unroll
+            for (int v = 0; v < VEC; ++v)
+                acc[j][v] = fmaf(w[j], x[v], acc[j][v]);
+    }
+#pragma unroll
+    for (int j = 0; j < kSsGroup; ++j) {
+        const int64_t J = g * kSsGroup + j;
+        if (J >= nrows)
+            break;
+        float* y = Y + J * (int64_t)ncols;
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) {
+            const int c = c0 + v * blockDim.x;
+            if (c < ncols)
+                y[c] = accumulate ? y[c] + acc[j][v] : acc[j][v];
+        }
+    }
+}
+
 // out (cols x rows) = in (rows x cols)^T, 32x32 tiles
 template <typename T>
 __global__ void k_transpose(int64_t rows, int64_t cols, const T* __restrict__ in, T* __restrict__ out) {
@@ -449,9 +577,47 @@ void SigmaBuilder::ensure_fp32() {
         sh->valf.reserve(total);
         k_convert<double, float><<<1024, 256>>>((int64_t)total, sh->val.get(), sh->valf.get());
         F2G_LAUNCH("k_convert string Hamiltonian");
+        build_groups(s_, *sh, 0);
     }
     F2G_CUDA(cudaStreamSynchronize(0)); // the conversions ran on the legacy stream: wait for them alone
     fp32_ready = true;
+}
+
+// The grouped layout of one spin's FP32 string Hamiltonian, for spaces of kSsGroupMinRows strings
+// or more. The first call sizes it (one host read of the total); later calls (new integrals, same
+// strings) refill it in place on stream st.
+void SigmaBuilder::build_groups(int spin, StringHamiltonian& sh, cudaStream_t st) {
+    const int64_t N0 = s->spin(spin).N0;
+    int S = 1;
+    while (S < kSsGroup * sh.nnz)
+        S <<= 1;
+    if (N0 < kSsGroupMinRows || sh.nnz == 0 || S > kSsGroupMaxSort)
+        return;
+    const size_t smem = (size_t)S * (sizeof(unsigned long long) + sizeof(float));
+    F2G_CUDA(cudaFuncSetAttribute(k_group_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t ng = (N0 + kSsGroup - 1) / kSsGroup;
+    if (sh.ngroups == 0) {
+        DevBuf<int64_t> cnt;
+        cnt.reserve(ng + 1);
+        F2G_CUDA(cudaMemsetAsync(cnt.get(), 0, (ng + 1) * sizeof(int64_t), st));
+        k_group_build<<<(unsigned)ng, 1024, smem, st>>>(N0, sh.nnz, sh.col.get(), sh.valf.get(), S, 0, cnt.get(),
+                                                        nullptr, nullptr, nullptr);
+        F2G_LAUNCH("k_group_build count");
+        std::vector<int64_t> c(ng + 1, 0), off(ng + 1, 0);
+        F2G_CUDA(cudaMemcpyAsync(c.data(), cnt.get(), ng * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        F2G_CUDA(cudaStreamSynchronize(st));
+        for (int64_t g = 0; g < ng; ++g)
+            off[g + 1] = off[g] + c[g];
+        sh.goff.reserve(ng + 1);
+        sh.gcol.reserve((size_t)std::max<int64_t>(1, off[ng]));
+        sh.gval.reserve((size_t)std::max<int64_t>(1, off[ng]) * kSsGroup);
+        F2G_CUDA(cudaMemcpyAsync(sh.goff.get(), off.data(), (ng + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        F2G_CUDA(cudaStreamSynchronize(st));
+        sh.ngroups = ng;
+    }
+    k_group_build<<<(unsigned)ng, 1024, smem, st>>>(N0, sh.nnz, sh.col.get(), sh.valf.get(), S, 1, nullptr,
+                                                    sh.goff.get(), sh.gcol.get(), sh.gval.get());
+    F2G_LAUNCH("k_group_build fill");
 }
 
 void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_) {
@@ -509,6 +675,7 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
         sh->valf.reserve(total);
         k_convert<double, float><<<1024, 256, 0, st>>>((int64_t)total, sh->val.get(), sh->valf.get());
         F2G_LAUNCH("k_convert string Hamiltonian");
+        build_groups(s_, *sh, st);
     }
     fp32_ready = true;
 }
@@ -676,6 +843,16 @@ static void launch_spmm(const StringHamiltonian& sh, const T* val, int64_t nrows
                         bool accumulate, cudaStream_t st, int nvec = 1) {
     if (nrows == 0 || ncols == 0 || sh.nnz == 0)
         return;
+    if constexpr (sizeof(T) == 4) {
+        if (sh.ngroups > 0) {
+            constexpr int VEC = 4;
+            dim3 grid((unsigned)sh.ngroups, (unsigned)ceil_div(ncols, 128 * VEC), (unsigned)nvec);
+            k_spmm_group<VEC><<<grid, 128, 0, st>>>(nrows, ncols, sh.goff.get(), sh.gcol.get(), sh.gval.get(), X, Y,
+                                                    accumulate ? 1 : 0, nrows * (int64_t)ncols);
+            F2G_LAUNCH("k_spmm_group");
+            return;
+        }
+    }
     constexpr int VEC = sizeof(T) == 8 ? 4 : 8;
     if (g_spmm_narrow)
         launch_spmm_v<T, VEC / 2>(sh, val, nrows, ncols, X, Y, accumulate, st, nvec);

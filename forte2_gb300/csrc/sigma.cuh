@@ -20,7 +20,19 @@ struct StringHamiltonian {
     DevBuf<int32_t> col;
     DevBuf<double> val;
     DevBuf<float> valf;
+    // FP32 row groups (large spaces): rows g*kSsGroup .. +kSsGroup read the union of their input
+    // rows once; gcol[goff[g] .. goff[g+1]) is that union in ascending order and gval holds, per
+    // union row, the kSsGroup values of the group's rows (0 where a row has no entry). The layout
+    // depends on the strings only: later integrals refill gval in place.
+    int64_t ngroups = 0;
+    DevBuf<int64_t> goff;
+    DevBuf<int32_t> gcol;
+    DevBuf<float> gval;
 };
+
+constexpr int kSsGroup = 8;            // rows per group of the grouped FP32 same-spin kernel
+constexpr int64_t kSsGroupMinRows = 2048; // strings per spin from which the FP32 build uses groups
+constexpr int kSsGroupMaxSort = 16384; // kSsGroup * entries per row must fit one block's sort
 
 struct SigmaBuilder {
     CIStrings* s;
@@ -108,6 +120,7 @@ struct SigmaBuilder {
 
   private:
     void build_string_hamiltonian(int spin, StringHamiltonian& sh, bool with_e0, cudaStream_t st);
+    void build_groups(int spin, StringHamiltonian& sh, cudaStream_t st);
     template <typename T>
     void run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_, bool graph);
     void apply_batch(const double* C, double* sigma, cudaStream_t st, int nvec, bool timed, bool graph);

@@ -290,13 +290,14 @@ def test_fp32_tensor_core_opposite_spin(cuda, na, nb, n):
         assert e_tc < 2e-6 and e_tc < 3 * e_cc + 1e-7
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_sigma_is_bitwise_reproducible(cuda, precision):
+@pytest.mark.parametrize("precision,n", [("fp64", 12), ("fp32", 12), ("fp32", 14)])
+def test_sigma_is_bitwise_reproducible(cuda, precision, n):
     """The same vectors give bitwise-identical sigma across repeated calls, capped grids and batch
-    shapes: the opposite-spin kernels sum every element in a fixed order (FP64: one write phase
-    per created orbital; FP32 tensor cores: exact 64-bit fixed-point row sums)."""
+    shapes: every kernel sums each element in a fixed order (FP64 opposite spin: one write phase
+    per created orbital; FP32 tensor cores: exact fixed-point row sums; CAS(14,14) FP32 also runs
+    the grouped same-spin kernel, input rows in ascending order)."""
     torch = cuda
-    s, sb, _ = builder(6, 6, 12, 77)
+    s, sb, _ = builder(n // 2, n // 2, n, 77)
     sb.set_precision(precision)
     if precision == "fp32":
         assert sb.set_tensor_cores(True) is True
@@ -307,7 +308,7 @@ def test_sigma_is_bitwise_reproducible(cuda, precision):
         again = torch.empty_like(X)
         sb.Hamiltonian(X, again)
         assert torch.equal(again, first)
-    for cap in (5, 37, 152, 0):
+    for cap in ((5, 37, 152, 0) if n <= 12 else (37, 0)):
         sb.set_max_blocks(cap)
         capped = torch.empty_like(X)
         sb.Hamiltonian(X, capped)
