@@ -133,6 +133,8 @@ class DavidsonLiuSolver:
         self._graphs = {}
         self._tmp2 = None
         self.used_graph = False
+        self._G = None  # subspace matrix B S^T, valid for the first _g_size rows and columns
+        self._g_size = 0
 
     # ---- configuration (davidsonliu.py:116-182) ----
     def add_sigma_builder(self, sigma_builder):
@@ -293,9 +295,24 @@ class DavidsonLiuSolver:
         self.sigma_builds += hi - lo
 
     def _eigh_dev(self, m):
-        """Enqueue the subspace matrix B S^T and its Jacobi eigendecomposition; returns (evals, evecs)."""
+        """Enqueue the subspace matrix B S^T and its Jacobi eigendecomposition; returns (evals, evecs).
+
+        Entries of rows and columns that were already in the previous subspace matrix are kept:
+        only the pairs with a new basis or sigma row are computed (each pair's dot product is the
+        same number however many pairs share a launch, so the matrix is bitwise the one a full
+        recomputation gives). Anything that changes existing rows (collapse, a new solve, a
+        projection) starts it afresh."""
         torch = _torch()
-        G = self._dots_dev(self.b[:m], self.sigma[:m]).contiguous()
+        k0 = self._g_size if (self._g_size <= m and not hasattr(self, "_proj_out")) else 0
+        if self._G is None:
+            self._G = torch.zeros((self.max_subspace_size, self.max_subspace_size), dtype=torch.float64,
+                                  device="cuda")
+        if k0 < m:
+            self._G[:m, k0:m] = self._dots_dev(self.b[:m], self.sigma[k0:m])
+            if k0 > 0:
+                self._G[k0:m, :k0] = self._dots_dev(self.b[k0:m], self.sigma[:k0])
+        self._g_size = m
+        G = self._G[:m, :m].contiguous()
         ev = torch.empty(m, dtype=torch.float64, device="cuda")
         vec = torch.empty((m, m), dtype=torch.float64, device="cuda")
         check(lib().f2g_dav_eigh(m, _ptr(G), _ptr(ev), _ptr(vec), stream_handle()))
@@ -311,6 +328,7 @@ class DavidsonLiuSolver:
         self.sigma[:k].copy_(self.tmp[:k])
         self.basis_size = k
         self.sigma_size = k
+        self._g_size = 0
         yield from self._orthonormality_steps(self.b[:k], f"After collapse: Checking orthonormality of newB with size {k}")
 
     def restart(self):
@@ -466,6 +484,7 @@ class DavidsonLiuSolver:
         if spec is not None:
             return (yield from self._solve_graph_steps(spec))
         self.used_graph = False
+        self._g_size = 0  # rows may have been written since the last solve
         torch = _torch()
         if not self._executed:
             G = self._guesses.clone() if hasattr(self, "_guesses") else self._random_rows(self.nroot)
