@@ -249,18 +249,19 @@ class DavidsonLiuSolver:
             if A.shape[0]:
                 d = self._dots_dev(A, vr)
                 self._lincomb(A, -d, vr, 1.0)
-            (nrm2,) = yield [self._dots_dev(vr, vr)]
+                # the norm and the overlaps of the projected vector in one host read; the overlaps
+                # of the normalised vector are these over the norm
+                nrm2, ov = yield [self._dots_dev(vr, vr), self._dots_dev(A, vr)]
+            else:
+                (nrm2,) = yield [self._dots_dev(vr, vr)]
+                ov = np.zeros(1)
             nrm = float(np.sqrt(max(nrm2[0, 0], 0.0)))
             if nrm < self.schmidt_discard_threshold:
                 return False, v
             v.mul_(1.0 / nrm)
-            if A.shape[0]:
-                ov, n2 = yield [self._dots_dev(A, vr), self._dots_dev(vr, vr)]
-                max_overlap = float(np.abs(ov).max())
-            else:
-                (n2,) = yield [self._dots_dev(vr, vr)]
-                max_overlap = 0.0
-            if max_overlap < self.schmidt_orthogonality_threshold and abs(float(n2[0, 0]) - 1.0) < self.schmidt_orthogonality_threshold:
+            max_overlap = float(np.abs(ov).max()) / nrm
+            n2 = float(nrm2[0, 0]) / (nrm * nrm)
+            if max_overlap < self.schmidt_orthogonality_threshold and abs(n2 - 1.0) < self.schmidt_orthogonality_threshold:
                 return True, v
         return False, v
 
@@ -517,21 +518,28 @@ class DavidsonLiuSolver:
             if hasattr(self, "_proj_out"):
                 self.do_project_out(self.sigma[:m])
             ev, vec = self._eigh_dev(m)
-            lam, alpha = yield [ev, vec]
-            if self.energy_shift is not None:
+            norms2 = torch.empty(nroot, dtype=torch.float64, device="cuda")
+
+            def residual(d_alpha, d_lam):
+                check(lib().f2g_dav_residual(_ptr(self.b), _ptr(self.sigma), m, self.b.stride(0), _ptr(d_alpha),
+                                             _ptr(d_lam), nroot, _ptr(self.h_diag), self.size,
+                                             self.preconditioner_denom_threshold, _ptr(self.r), self.r.stride(0),
+                                             _ptr(norms2), _ptr(self.scratch), stream_handle()))
+
+            if self.energy_shift is None:
+                # the roots are the lowest eigenpairs, in the eigensolver's order: the residuals are
+                # enqueued straight from its device output, one host read for both
+                residual(vec[:, :nroot].contiguous(), ev[:nroot])
+                lam, alpha, n2 = yield [ev, vec, norms2]
+            else:
+                lam, alpha = yield [ev, vec]
                 idx = np.argsort(np.abs(lam - self.energy_shift))
                 lam, alpha = lam[idx], alpha[:, idx]
+                residual(to_device(alpha[:, :nroot]), to_device(lam[:nroot].copy()))
+                (n2,) = yield [norms2]
             self.lam[:m] = lam
             self.alpha[:m, :m] = alpha
             lamr = lam[:nroot].copy()
-            d_alpha = to_device(alpha[:, :nroot])
-            d_lam = to_device(lamr)
-            norms2 = torch.empty(nroot, dtype=torch.float64, device="cuda")
-            check(lib().f2g_dav_residual(_ptr(self.b), _ptr(self.sigma), m, self.b.stride(0), _ptr(d_alpha),
-                                         _ptr(d_lam), nroot, _ptr(self.h_diag), self.size,
-                                         self.preconditioner_denom_threshold, _ptr(self.r), self.r.stride(0),
-                                         _ptr(norms2), _ptr(self.scratch), stream_handle()))
-            (n2,) = yield [norms2]
             rnorms = np.sqrt(np.maximum(n2, 0.0))
             max_de = float(np.max(np.abs(lamr - self.lam_old[:nroot])))
             max_r = float(rnorms.max())
