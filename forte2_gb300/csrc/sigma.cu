@@ -259,12 +259,17 @@ __global__ void k_group_build(int64_t nrows, int nnz, const int32_t* __restrict_
 }
 
 // Y[J, :] = (accumulate ? Y[J, :] : 0) + sum_u gval[u][J - g G] X[gcol[u], :] for the rows J of
-// group g = blockIdx.x; the input rows in ascending order (a fixed summation order).
+// group g = blockIdx.x; the input rows in ascending order (a fixed summation order). The group's
+// (row, values) list is staged in shared memory chunk by chunk, and the loads of kSsUnroll input
+// rows are issued before their multiply-adds (the kernel is bound by load latency, not bandwidth).
+constexpr int kSsChunk = 512, kSsUnroll = 4;
 template <int VEC>
 __global__ void __launch_bounds__(128) k_spmm_group(int64_t nrows, int ncols, const int64_t* __restrict__ goff,
                                                     const int32_t* __restrict__ gcol, const float* __restrict__ gval,
                                                     const float* __restrict__ X, float* __restrict__ Y, int accumulate,
                                                     int64_t vstride) {
+    __shared__ int32_t scol[kSsChunk];
+    __shared__ __align__(16) float sval[kSsChunk * kSsGroup];
     X += blockIdx.z * vstride;
     Y += blockIdx.z * vstride;
     const int64_t g = blockIdx.x, u0 = goff[g], u1 = goff[g + 1];
@@ -275,23 +280,44 @@ __global__ void __launch_bounds__(128) k_spmm_group(int64_t nrows, int ncols, co
 #pragma unroll
         for (int v = 0; v < VEC; ++v)
             acc[j][v] = 0.0f;
-#pragma unroll 2
-    for (int64_t u = u0; u < u1; ++u) {
-        const float* xr = X + (int64_t)__ldg(gcol + u) * ncols;
-        float x[VEC];
+    for (int64_t base = u0; base < u1; base += kSsChunk) {
+        const int cnt = (int)(u1 - base < kSsChunk ? u1 - base : kSsChunk);
+        __syncthreads(); // the previous chunk is consumed
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x)
+            scol[t] = gcol[base + t];
+        for (int t = threadIdx.x; t < cnt * kSsGroup / 4; t += blockDim.x)
+            reinterpret_cast<float4*>(sval)[t] = __ldg(reinterpret_cast<const float4*>(gval + base * kSsGroup) + t);
+        // rows past the chunk's end: read row 0 with zero weights (no branch in the unrolled loop)
+        for (int t = cnt + threadIdx.x; t < ((cnt + kSsUnroll - 1) / kSsUnroll) * kSsUnroll; t += blockDim.x) {
+            scol[t] = 0;
 #pragma unroll
-        for (int v = 0; v < VEC; ++v) {
-            const int c = c0 + v * blockDim.x;
-            x[v] = c < ncols ? __ldg(xr + c) : 0.0f;
+            for (int j = 0; j < kSsGroup; ++j)
+                sval[t * kSsGroup + j] = 0.0f;
         }
-        const float4 wa = __ldg(reinterpret_cast<const float4*>(gval + u * kSsGroup));
-        const float4 wb = __ldg(reinterpret_cast<const float4*>(gval + u * kSsGroup) + 1);
-        const float w[kSsGroup] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+        __syncthreads();
+        for (int u = 0; u < cnt; u += kSsUnroll) {
+            float x[kSsUnroll][VEC];
 #pragma unroll
-        for (int j = 0; j < kSsGroup; ++j)
+            for (int q = 0; q < kSsUnroll; ++q) {
+                const float* xr = X + (int64_t)scol[u + q] * ncols;
 #pragma unroll
-            for (int v = 0; v < VEC; ++v)
-                acc[j][v] = fmaf(w[j], x[v], acc[j][v]);
+                for (int v = 0; v < VEC; ++v) {
+                    const int c = c0 + v * blockDim.x;
+                    x[q][v] = c < ncols ? __ldg(xr + c) : 0.0f;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kSsUnroll; ++q) {
+                const float4 wa = reinterpret_cast<const float4*>(sval)[(u + q) * 2];
+                const float4 wb = reinterpret_cast<const float4*>(sval)[(u + q) * 2 + 1];
+                const float w[kSsGroup] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+                for (int j = 0; j < kSsGroup; ++j)
+#pragma unroll
+                    for (int v = 0; v < VEC; ++v)
+                        acc[j][v] = fmaf(w[j], x[q][v], acc[j][v]);
+            }
+        }
     }
 #pragma unroll
     for (int j = 0; j < kSsGroup; ++j) {
