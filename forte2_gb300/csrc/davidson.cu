@@ -662,6 +662,88 @@ __global__ void __launch_bounds__(256) k_dg_dots(const DGState* st, int which, c
     }
 }
 
+// Long vectors: every block takes a strided share of the elements for 8 pairs at a time; partial
+// sums per block, added in block order by k_dg_dots_reduce (the same pair selection as k_dg_dots).
+__device__ __forceinline__ void dg_pair_limits(const DGState* st, int which, int ni, int nj, int& li, int& lj) {
+    li = ni;
+    lj = nj;
+    if (which == 0 || which == 1)
+        li = lj = st->m;
+    else if (which == 3)
+        li = st->m;
+}
+
+__global__ void __launch_bounds__(256) k_dg_dots_partial(const DGState* st, int which, const double* __restrict__ A,
+                                                         int64_t lda, const double* __restrict__ B, int64_t ldb,
+                                                         int64_t n, int ni, int nj, double* __restrict__ partial) {
+    if (st->status != kDGRunning)
+        return;
+    if ((which == 1 || which == 2) && !st->collapse)
+        return;
+    int li, lj;
+    dg_pair_limits(st, which, ni, nj, li, lj);
+    const int np = li * lj;
+    const int64_t e0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, step = (int64_t)gridDim.x * blockDim.x;
+    __shared__ double red[8][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int p0 = 0; p0 < np; p0 += 8) {
+        double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int cnt = min(8, np - p0);
+        for (int64_t e = e0; e < n; e += step)
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q < cnt) {
+                    const int pr = p0 + q, i = pr / lj, j = pr % lj;
+                    a[q] += A[(int64_t)i * lda + e] * B[(int64_t)j * ldb + e];
+                }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            double x = a[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0)
+                red[w][q] = x;
+        }
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            double t = 0.0;
+            for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww)
+                t += red[ww][threadIdx.x];
+            partial[(int64_t)blockIdx.x * 4096 + p0 + threadIdx.x] = t;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_dg_dots_reduce(const DGState* st, int which, int ni, int nj, int nblocks,
+                                 const double* __restrict__ partial, double* __restrict__ out, int ldo) {
+    if (st->status != kDGRunning)
+        return;
+    if ((which == 1 || which == 2) && !st->collapse)
+        return;
+    int li, lj;
+    dg_pair_limits(st, which, ni, nj, li, lj);
+    const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pr >= li * lj)
+        return;
+    double t = 0.0;
+    for (int bk = 0; bk < nblocks; ++bk)
+        t += partial[(int64_t)bk * 4096 + pr];
+    out[(pr / lj) * ldo + pr % lj] = t;
+}
+
+void dg_dots_long(const DGState* st, int which, const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n,
+                  int ni, int nj, double* out, int ldo, double* partial, cudaStream_t s) {
+    if (ni <= 0 || nj <= 0 || ni > 64 || nj > 64)
+        throw Error(2, "dg_dots: 1 to 64 vectors per operand");
+    const int blocks = dg_gsm_blocks(n);
+    k_dg_dots_partial<<<blocks, 256, 0, s>>>(st, which, A, lda, B, ldb, n, ni, nj, partial);
+    F2G_LAUNCH("k_dg_dots_partial");
+    k_dg_dots_reduce<<<ceil_div(ni * nj, 128), 128, 0, s>>>(st, which, ni, nj, blocks, partial, out, ldo);
+    F2G_LAUNCH("k_dg_dots_reduce");
+}
+
 void dg_dots(const DGState* st, int which, const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n,
              int ni, int nj, double* out, int ldo, cudaStream_t s) {
     if (ni <= 0 || nj <= 0 || ni > 64 || nj > 64)
@@ -1018,6 +1100,208 @@ __global__ void __launch_bounds__(kGsThreads) k_dg_gs(DGState* st, DGParams P, d
 void dg_gs(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr, cudaStream_t s) {
     k_dg_gs<<<1, gs_threads(P.n), 0, s>>>(st, P, b, ld, r, ldr);
     F2G_LAUNCH("k_dg_gs");
+}
+
+// ---- multi-block Gram-Schmidt (graph-captured iterations on long vectors) ----------------------
+// Partial sums use a fixed element order per block and are added over blocks in block order, so
+// every decision is the same on every run.
+constexpr int kGsmCycles = 10;  // the reference's cycle limit per vector
+constexpr int kGsmStride = 65;  // partial slots per block: 64 overlaps and the squared norm
+
+int dg_gsm_blocks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 1023) / 1024, 152 * 4)); }
+
+__global__ void k_gsm_init(DGState* st, DGParams P, GsmState* g) {
+    g->active = 0;
+    g->kind = 0;
+    if (st->status != kDGRunning) {
+        g->to_add = 0;
+        return;
+    }
+    g->m0 = st->m;
+    g->to_add = min(P.nroot, P.maxm - st->m);
+    g->nadd = g->cand = g->refill_tried = 0;
+    g->refill_total = -1;
+    if (g->to_add <= 0)
+        st->status = kDGConverged;
+}
+
+// next slot: the next candidate residual, then (once the candidates are done) as many random vectors
+// as candidates were rejected, each tried once
+__global__ void k_gsm_pick(const DGState* st, GsmState* g) {
+    g->active = 0;
+    g->kind = 0;
+    if (st->status != kDGRunning || g->to_add <= 0)
+        return;
+    if (g->cand < g->to_add) {
+        g->kind = 1;
+        g->src = g->cand++;
+    } else {
+        if (g->refill_total < 0)
+            g->refill_total = g->to_add - g->nadd;
+        if (g->refill_tried >= g->refill_total)
+            return;
+        g->kind = 2;
+        g->src = g->refill_tried++;
+    }
+    g->s = g->m0 + g->nadd;
+    g->active = 1;
+}
+
+__global__ void k_gsm_load(const DGState* st, DGParams P, const GsmState* g, double* b, int64_t ld,
+                           const double* __restrict__ r, int64_t ldr) {
+    if (!g->active)
+        return;
+    double* v = b + (int64_t)g->s * ld;
+    const int kind = g->kind, src = g->src;
+    const uint64_t stream = (uint64_t)st->iter * 64 + src;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P.n; e += (int64_t)gridDim.x * blockDim.x)
+        v[e] = kind == 1 ? r[(int64_t)src * ldr + e] : gs_uniform(P.seed, stream, e);
+}
+
+// block sums of 8 values per thread into partial[blockIdx.x * kGsmStride + slot0 + i], fixed order
+__device__ void gsm_block_sum8(const double (&a)[8], int cnt, double* partial, int slot0) {
+    __shared__ double red[8][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        double x = a[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0)
+            red[w][i] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+        double t = 0.0;
+        for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww)
+            t += red[ww][threadIdx.x];
+        partial[(int64_t)blockIdx.x * kGsmStride + slot0 + threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+// mode 0: overlaps of v with rows 0..s-1; mode 1: v -= sum dv_i b_i, then |v|^2;
+// mode 2: v *= inv, then overlaps and |v|^2
+__global__ void __launch_bounds__(256) k_gsm_pass(DGParams P, const GsmState* g, double* b, int64_t ld, int mode,
+                                                  double* __restrict__ partial) {
+    if (!g->active)
+        return;
+    __shared__ double dv[64];
+    const int s = g->s;
+    double* v = b + (int64_t)s * ld;
+    const int64_t e0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, step = (int64_t)gridDim.x * blockDim.x;
+    if (mode == 1) {
+        for (int i = threadIdx.x; i < s; i += blockDim.x)
+            dv[i] = g->dv[i];
+        __syncthreads();
+        double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int64_t e = e0; e < P.n; e += step) {
+            double x = v[e];
+            for (int i = 0; i < s; ++i)
+                x -= dv[i] * b[(int64_t)i * ld + e];
+            v[e] = x;
+            a[0] += x * x;
+        }
+        gsm_block_sum8(a, 1, partial, 64);
+        return;
+    }
+    if (mode == 2) {
+        const double inv = g->inv;
+        for (int64_t e = e0; e < P.n; e += step)
+            v[e] *= inv;
+    }
+    for (int i0 = 0; i0 < s; i0 += 8) {
+        double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int cnt = min(8, s - i0);
+        for (int64_t e = e0; e < P.n; e += step) {
+            const double x = v[e];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (i < cnt)
+                    a[i] += b[(int64_t)(i0 + i) * ld + e] * x;
+        }
+        gsm_block_sum8(a, cnt, partial, i0);
+    }
+    if (mode == 2) {
+        double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int64_t e = e0; e < P.n; e += step)
+            a[0] += v[e] * v[e];
+        gsm_block_sum8(a, 1, partial, 64);
+    }
+}
+
+// Sums the block partials in block order and decides (one block of 64 threads).
+// mode 0: overlaps -> dv; mode 1: norm -> reject (below the discard threshold) or inv;
+// mode 2: overlaps and norm of the normalised vector -> accept, or another cycle
+__global__ void k_gsm_decide(DGParams P, GsmState* g, int nblocks, int mode, const double* __restrict__ partial) {
+    if (!g->active)
+        return;
+    __shared__ double tot[kGsmStride];
+    const int s = g->s;
+    for (int i = threadIdx.x; i < kGsmStride; i += blockDim.x) {
+        const bool used = (i < s && mode != 1) || (i == 64 && mode != 0);
+        double t = 0.0;
+        if (used)
+            for (int bk = 0; bk < nblocks; ++bk)
+                t += partial[(int64_t)bk * kGsmStride + i];
+        tot[i] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    if (mode == 0) {
+        for (int i = 0; i < s; ++i)
+            g->dv[i] = tot[i];
+    } else if (mode == 1) {
+        const double nrm = sqrt(fmax(tot[64], 0.0));
+        if (nrm < P.discard)
+            g->active = 0; // rejected
+        else
+            g->inv = 1.0 / nrm;
+    } else {
+        double mo = 0.0;
+        for (int i = 0; i < s; ++i)
+            mo = fmax(mo, fabs(tot[i]));
+        if (mo < P.ortho && fabs(tot[64] - 1.0) < P.ortho) {
+            g->active = 0; // accepted
+            g->nadd += 1;
+        }
+    }
+}
+
+__global__ void k_gsm_end_slot(GsmState* g) { g->active = 0; } // cycles exhausted: rejected
+
+__global__ void k_gsm_end(DGState* st, const GsmState* g) {
+    if (st->status != kDGRunning || g->to_add <= 0)
+        return;
+    st->m = g->m0 + g->nadd;
+    st->added = g->nadd;
+}
+
+void dg_gs_multi(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr, GsmState* g,
+                 double* partial, cudaStream_t s) {
+    const int blocks = dg_gsm_blocks(P.n);
+    k_gsm_init<<<1, 1, 0, s>>>(st, P, g);
+    F2G_LAUNCH("k_gsm_init");
+    for (int slot = 0; slot < 2 * P.nroot; ++slot) {
+        k_gsm_pick<<<1, 1, 0, s>>>(st, g);
+        F2G_LAUNCH("k_gsm_pick");
+        k_gsm_load<<<dg_grid(P.n), 256, 0, s>>>(st, P, g, b, ld, r, ldr);
+        F2G_LAUNCH("k_gsm_load");
+        for (int cycle = 0; cycle < kGsmCycles; ++cycle) {
+            for (int mode = 0; mode < 3; ++mode) {
+                k_gsm_pass<<<blocks, 256, 0, s>>>(P, g, b, ld, mode, partial);
+                F2G_LAUNCH("k_gsm_pass");
+                k_gsm_decide<<<1, 64, 0, s>>>(P, g, blocks, mode, partial);
+                F2G_LAUNCH("k_gsm_decide");
+            }
+        }
+        k_gsm_end_slot<<<1, 1, 0, s>>>(g);
+        F2G_LAUNCH("k_gsm_end_slot");
+    }
+    k_gsm_end<<<1, 1, 0, s>>>(st, g);
+    F2G_LAUNCH("k_gsm_end");
 }
 
 // Everything of one iteration after the sigma build, in one block: for short vectors the

@@ -84,6 +84,24 @@ void dg_collapse(const DGState* st, const DGParams& P, double* b, double* sigma,
 void dg_project(const DGState* st, const DGParams& P, const double* b, int64_t ld, const double* D, double* r,
                 int64_t ldr, cudaStream_t s);
 void dg_gs(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr, cudaStream_t s);
+// The same Gram-Schmidt step (the reference's acceptance rule, davidsonliu.py:338-366 and 438-484)
+// with every pass over the vectors spread over the whole GPU: a fixed sequence of kernels whose
+// decisions (accept, reject, next candidate, random refill) live in a GsmState on the device, so it
+// can be captured in a graph. For long vectors, where one block would stream them alone.
+struct GsmState {
+    int32_t m0, to_add, nadd;       // basis size before the step, candidates, vectors added so far
+    int32_t cand, refill_total, refill_tried;
+    int32_t kind, src, s, active;   // current slot: 1 candidate src / 2 random refill src; its row s
+    double inv;                      // 1 / norm of the projected vector
+    double dv[64];                   // its overlaps with the basis rows
+};
+constexpr int64_t kGsOneBlockMaxN = 1 << 15; // longer vectors use the multi-block Gram-Schmidt
+int dg_gsm_blocks(int64_t n);
+// dg_dots for long vectors: all SMs share every pair (partial: dg_gsm_blocks(n) x 4096 doubles)
+void dg_dots_long(const DGState* st, int which, const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n,
+                  int ni, int nj, double* out, int ldo, double* partial, cudaStream_t s);
+void dg_gs_multi(DGState* st, const DGParams& P, double* b, int64_t ld, const double* r, int64_t ldr, GsmState* g,
+                 double* partial, cudaStream_t s);
 void dg_correct(const DGState* st, const double* X, const double* D, int64_t ldx, const double* Mxd, const double* A,
                 const double* Bd, int k, int R, int64_t n, double* S, cudaStream_t s);
 // One-block iteration after the sigma build, for vectors up to kDGSmallN and bases up to 32.

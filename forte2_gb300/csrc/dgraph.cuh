@@ -78,6 +78,9 @@ struct DavGraph {
 
     DevBuf<DGState> st;
     DevBuf<double> G, G2, evals, V, norms2, partial, Dp, hist, stage_c, stage_s, cA, cB;
+    bool long_vectors = false;    // multi-block dot products and Gram-Schmidt
+    DevBuf<GsmState> gsm;
+    DevBuf<double> gsm_partial, dots_partial;
     CsfSigmaScratch scr; // determinant-space scratch of the captured sigma (reserved at capture)
     DGState* host_state = nullptr;
 
@@ -115,6 +118,12 @@ struct DavGraph {
         hist.reserve((size_t)4 * P.maxiter_cap);
         stage_c.reserve((size_t)R * n);
         stage_s.reserve((size_t)R * n);
+        long_vectors = n > kGsOneBlockMaxN;
+        if (long_vectors) {
+            gsm.reserve(1);
+            gsm_partial.reserve((size_t)dg_gsm_blocks(n) * 65);
+            dots_partial.reserve((size_t)dg_gsm_blocks(n) * 4096);
+        }
         host_state = PinnedStateSlots::get().take();
     }
 
@@ -152,11 +161,19 @@ struct DavGraph {
         const int64_t n = P.n, nd = sa->s->ndet;
         const int mm = P.maxm;
         DGState* S = st.get();
+        // dot products: one block per pair for short vectors, all SMs on every pair for long ones
+        auto dots = [&](int which, const double* A, int64_t lda, const double* B, int64_t ldb, int ni, int nj,
+                        double* out, int ldo) {
+            if (long_vectors)
+                dg_dots_long(S, which, A, lda, B, ldb, n, ni, nj, out, ldo, dots_partial.get(), s);
+            else
+                dg_dots(S, which, A, lda, B, ldb, n, ni, nj, out, ldo, s);
+        };
         dg_stage(S, b, ld, R, n, stage_c.get(), s);
         sigma_csf(*sb, *sa, stage_c.get(), stage_s.get(), R, s, scr, true);
         if (kc) {
-            dg_dots(S, 4, X, ldx, stage_c.get(), n, n, kc, R, cA.get(), R, s);
-            dg_dots(S, 4, D, ldx, stage_c.get(), n, n, kc, R, cB.get(), R, s);
+            dots(4, X, ldx, stage_c.get(), n, kc, R, cA.get(), R);
+            dots(4, D, ldx, stage_c.get(), n, kc, R, cB.get(), R);
             dg_correct(S, X, D, ldx, Mxd, cA.get(), cB.get(), kc, R, n, stage_s.get(), s);
         }
         if (dg_small_ok(P)) {
@@ -165,18 +182,21 @@ struct DavGraph {
             return;
         }
         dg_unstage(S, stage_s.get(), R, n, sigma, ld, s);
-        dg_dots(S, 0, b, ld, sigma, ld, n, mm, mm, G.get(), mm, s);
+        dots(0, b, ld, sigma, ld, mm, mm, G.get(), mm);
         dg_eigh(S, G.get(), mm, evals.get(), V.get(), mm, s);
         dg_residual(S, P, b, sigma, ld, V.get(), mm, evals.get(), hdiag, r, ldr, norms2.get(), partial.get(), s);
         dg_check(S, P, norms2.get(), evals.get(), hist.get(), s);
-        dg_dots(S, 1, b, ld, b, ld, n, mm, mm, G2.get(), mm, s);
+        dots(1, b, ld, b, ld, mm, mm, G2.get(), mm);
         dg_orthocheck(S, P, G2.get(), mm, 0, s);
         dg_collapse(S, P, b, sigma, ld, V.get(), mm, tmp, ldt, s);
-        dg_dots(S, 2, b, ld, b, ld, n, P.collapse_k, P.collapse_k, G2.get(), mm, s);
+        dots(2, b, ld, b, ld, P.collapse_k, P.collapse_k, G2.get(), mm);
         dg_orthocheck(S, P, G2.get(), mm, 1, s);
-        dg_dots(S, 3, b, ld, r, ldr, n, mm, P.nroot, Dp.get(), P.nroot, s);
+        dots(3, b, ld, r, ldr, mm, P.nroot, Dp.get(), P.nroot);
         dg_project(S, P, b, ld, Dp.get(), r, ldr, s);
-        dg_gs(S, P, b, ld, r, ldr, s);
+        if (long_vectors)
+            dg_gs_multi(S, P, b, ld, r, ldr, gsm.get(), gsm_partial.get(), s);
+        else
+            dg_gs(S, P, b, ld, r, ldr, s);
     }
 
     void capture() {

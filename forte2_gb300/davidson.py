@@ -84,7 +84,7 @@ class DavidsonLiuSolver:
     # Graph-captured iterations (f2g_dgraph_*): None = whenever the sigma builder supports it and
     # size <= graph_max_size; True/False force it on/off.
     use_graph: bool = None
-    graph_max_size: int = 1 << 15
+    graph_max_size: int = 1 << 40
     iters_per_launch: int = 8
 
     def __post_init__(self):

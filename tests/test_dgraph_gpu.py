@@ -57,6 +57,20 @@ def test_graph_iteration_limit(cuda):
     assert len(hist) == 3 and all(h[3] > 0 for h in hist)
 
 
+@pytest.mark.parametrize("mult,nroot,precision", [(1, 2, "fp64"), (3, 1, "mixed")])
+def test_graph_iterations_on_long_vectors(cuda, mult, nroot, precision):
+    """CAS(12,12) (226,512 singlet / 382,239 triplet CSFs): graph-captured iterations with the
+    multi-block dot products and Gram-Schmidt give the host-driven energies."""
+    host = _solver(12, mult, nroot, 1212, False, precision=precision).run()
+    gr = _solver(12, mult, nroot, 1212, True, precision=precision).run()
+    assert gr.eigensolver.used_graph and not host.eigensolver.used_graph
+    assert gr.eigensolver.size > 1 << 15
+    assert gr.converged and host.converged
+    np.testing.assert_allclose(gr.evals, host.evals, rtol=0, atol=1e-10 if precision == "fp64" else 1e-8)
+    if precision == "fp64":
+        assert abs(gr.eigensolver.iter - host.eigensolver.iter) <= 3
+
+
 def test_pooled_solver_reuses_graphs(cuda):
     s = _solver(8, 3, 2, 41, True).run()
     graphs = dict(s.eigensolver._graphs)
