@@ -26,6 +26,12 @@ def _declare(L):
         "f2g_last_error": (C.c_char_p, []),
         "f2g_version": (C.c_char_p, []),
         "f2g_strings_create": (i32, [i32, i32, i32, pp]),
+        "f2g_strings_create_general": (i32, [i32, i32, i32, i32, P, P, i32, P, i32, P, pp]),
+        "f2g_strings_blocks_info": (i32, [vp, P]),
+        "f2g_blocks_enumerate": (i32, [i32, i32, i32, i32, P, P, i32, P, i32, P, P, P, P, P, P, P]),
+        "f2g_strings_class_strings": (i32, [vp, i32, P, P]),
+        "f2g_strings_block_table": (i32, [vp, P]),
+        "f2g_strings_occupations": (i32, [vp, P, P, P]),
         "f2g_strings_destroy": (i32, [vp]),
         "f2g_strings_info": (i32, [vp, P]),
         "f2g_strings_masks": (i32, [vp, i32, P]),

@@ -54,6 +54,13 @@ class CASCISolver:
     mixed_basis_per_root: int = 12
     mixed_collapse_per_root: int = 6
     seed: int = 12345
+    # the determinant space (CIStrings(na, nb, symmetry, orbital_symmetry, gas_min, gas_max),
+    # ci.py:120-137): state irrep, orbital irreps per GAS space (None: one space of norb orbitals
+    # in irrep 0) and the GAS electron bounds
+    symmetry: int = 0
+    orbital_symmetry: list = None
+    gas_min: list = field(default_factory=list)
+    gas_max: list = field(default_factory=list)
     # graph-captured Davidson iterations: None = automatic (small CSF spaces), True/False = force
     use_graph: bool = None
     # cap on the opposite-spin kernel's thread blocks (0 = none); see CISigmaBuilder.set_max_blocks
@@ -76,7 +83,10 @@ class CASCISolver:
 
     def _startup(self):
         t0 = time.perf_counter()
-        self.ci_strings = CIStrings(self.na, self.nb, 0, [[0] * self.norb], [], [])
+        orbsym = self.orbital_symmetry if self.orbital_symmetry is not None else [[0] * self.norb]
+        if sum(len(g) for g in orbsym) != self.norb:
+            raise ValueError("orbital_symmetry must list the irreps of all norb active orbitals")
+        self.ci_strings = CIStrings(self.na, self.nb, self.symmetry, orbsym, self.gas_min, self.gas_max)
         if self.ci_strings.ndet == 0:
             raise ValueError("No determinants could be generated for the given state and orbitals.")
         self.spin_adapter = CISpinAdapter(self.multiplicity - 1, self.twice_ms, self.norb)

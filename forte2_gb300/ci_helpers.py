@@ -59,22 +59,44 @@ class Determinants:
         return self.strings.ndet
 
     def masks(self) -> np.ndarray:
-        a = self.strings.alpha_masks()
-        b = self.strings.beta_masks()
-        out = np.empty((len(a) * len(b), 2), dtype=np.uint64)
-        out[:, 0] = np.repeat(a, len(b))
-        out[:, 1] = np.tile(b, len(a))
-        return out
+        return self.strings.determinant_masks()
 
     def __getitem__(self, i):
         return self.strings.determinant(i)
 
 
-class CIStrings:
-    """CI strings of a CAS active space (forte2/ci/ci_strings.cc:26-184), built on the device.
+def enumerate_blocks(na, nb, symmetry, orbital_symmetry, gas_min, gas_max):
+    """The determinant blocks of a space on the host alone (no device call): a dict with the
+    class strings and classes of both spins ('alpha', 'alpha_class', 'beta', 'beta_class'), the
+    block table ('blocks': alpha class, beta class, size, offset, alpha strings, beta strings),
+    'ndet', 'nirrep' and 'trivial'."""
+    sizes = np.array([len(g) for g in orbital_symmetry] or [0], dtype=np.int32)
+    flat = np.array([int(x) for g in orbital_symmetry for x in g] or [0], dtype=np.int32)
+    gmin = np.array(list(gas_min) or [0], dtype=np.int32)
+    gmax = np.array(list(gas_max) or [0], dtype=np.int32)
+    args = (int(na), int(nb), int(symmetry), len(orbital_symmetry), sizes.ctypes.data, flat.ctypes.data,
+            len(gas_min), gmin.ctypes.data, len(gas_max), gmax.ctypes.data)
+    info = np.zeros(16, dtype=np.int64)
+    check(lib().f2g_blocks_enumerate(*args, info.ctypes.data, None, None, None, None, None))
+    out = {"alpha": np.zeros(info[6], np.uint64), "alpha_class": np.zeros(info[6], np.int32),
+           "beta": np.zeros(info[7], np.uint64), "beta_class": np.zeros(info[7], np.int32),
+           "blocks": np.zeros((info[5], 6), np.int64)}
+    check(lib().f2g_blocks_enumerate(*args, info.ctypes.data, out["alpha"].ctypes.data,
+                                     out["alpha_class"].ctypes.data, out["beta"].ctypes.data,
+                                     out["beta_class"].ctypes.data, out["blocks"].ctypes.data))
+    out.update(ndet=int(info[13]), nirrep=int(info[1]), trivial=bool(info[0]))
+    return out
 
-    Supported: one GAS space, all orbital irreps 0 and state symmetry 0 (C1). Point-group
-    blocks and multiple GAS spaces raise NotImplementedError.
+
+class CIStrings:
+    """CI strings of an active space (forte2/ci/ci_strings.cc:26-184), built on the device.
+
+    Any number (up to six) of GAS spaces with their electron bounds, orbital irreps 0..7 and a
+    state irrep: the determinants are the reference's blocks in its order
+    (ci_occupation.cc:35-142, ci_string_class.cc:7-66, ci_strings_makers.cc:13-73). The sigma,
+    RDM and CSF kernels run on the C1 CAS space of all orbitals; a blocked space's vectors are
+    embedded into it (zero elsewhere) and read back, which is P H P, the reference's blocked
+    operator, at the cost of the C1 space.
     """
 
     def __init__(self, na, nb, symmetry, orbital_symmetry, gas_min, gas_max):
@@ -88,29 +110,43 @@ class CIStrings:
                 f"CIStrings: The number of GAS spaces specified by gas_min ({len(gas_min)}) and gas_max "
                 f"({len(gas_max)}) must be less than or equal to the number of orbital symmetries "
                 f"({len(orbital_symmetry)})")
-        nonempty = [g for g in orbital_symmetry if len(g) > 0]
-        if len(nonempty) > 1:
-            raise NotImplementedError("CIStrings: several GAS spaces are not supported by the GPU path")
-        if any(x != 0 for g in orbital_symmetry for x in g) or symmetry != 0:
-            raise NotImplementedError("CIStrings: point-group symmetry blocks are not supported by the GPU path")
         norb = sum(len(g) for g in orbital_symmetry)
         self._na, self._nb, self._norb = int(na), int(nb), int(norb)
         self.symmetry = int(symmetry)
-        self.orbital_symmetry = [list(g) for g in orbital_symmetry]
-        self.gas_min, self.gas_max = list(gas_min), list(gas_max)
+        self.orbital_symmetry = [[int(x) for x in g] for g in orbital_symmetry]
+        self.gas_min, self.gas_max = [int(x) for x in gas_min], [int(x) for x in gas_max]
+        nonempty = [g for g in self.orbital_symmetry if len(g) > 0]
+        plain = (len(nonempty) <= 1 and all(x == 0 for g in nonempty for x in g) and self.symmetry == 0
+                 and not self.gas_min and not self.gas_max)
         if self._na > norb or self._nb > norb:
             # the reference produces an empty determinant space
             self._empty = True
             self.h = None
             self._info = [norb, self._na, self._nb, 0, 0, 0, 0, 0, 0, 0]
+            self._binfo = [1, 1, len(self.orbital_symmetry), 1, 1, 1, 0, 0, 0, 1, 1, 1, self.symmetry, 0, 0, 0]
+            self._det_cache = np.zeros((0, 2), dtype=np.uint64)
             return
         self._empty = False
         h = C.c_void_p()
-        check(lib().f2g_strings_create(self._na, self._nb, self._norb, C.byref(h)))
+        if plain:
+            check(lib().f2g_strings_create(self._na, self._nb, self._norb, C.byref(h)))
+        else:
+            sizes = np.array([len(g) for g in self.orbital_symmetry] or [0], dtype=np.int32)
+            flat = np.array([x for g in self.orbital_symmetry for x in g] or [0], dtype=np.int32)
+            gmin = np.array(self.gas_min or [0], dtype=np.int32)
+            gmax = np.array(self.gas_max or [0], dtype=np.int32)
+            check(lib().f2g_strings_create_general(self._na, self._nb, self.symmetry, len(self.orbital_symmetry),
+                                                   sizes.ctypes.data, flat.ctypes.data, len(self.gas_min),
+                                                   gmin.ctypes.data, len(self.gas_max), gmax.ctypes.data,
+                                                   C.byref(h)))
         self.h = h
         info = np.zeros(10, dtype=np.int64)
         check(lib().f2g_strings_info(self.h, info.ctypes.data))
         self._info = [int(x) for x in info]
+        binfo = np.zeros(16, dtype=np.int64)
+        check(lib().f2g_strings_blocks_info(self.h, binfo.ctypes.data))
+        self._binfo = [int(x) for x in binfo]
+        self._det_cache = None
 
     def __del__(self):
         h = getattr(self, "h", None)
@@ -122,17 +158,64 @@ class CIStrings:
     na = property(lambda self: self._na)
     nb = property(lambda self: self._nb)
     norb = property(lambda self: self._norb)
-    nas = property(lambda self: self._info[3])
-    nbs = property(lambda self: self._info[4])
+    nas = property(lambda self: self._binfo[6])
+    nbs = property(lambda self: self._binfo[7])
     ndet = property(lambda self: self._info[5])
     ngas_spaces = property(lambda self: len(self.orbital_symmetry))
     gas_size = property(lambda self: [len(g) for g in self.orbital_symmetry])
+    nirrep = property(lambda self: self._binfo[1])
+    # True when the space is a set of blocks of the C1 CAS space (irreps or GAS restrictions)
+    blocked = property(lambda self: not self._empty and self._binfo[0] == 0)
+    # determinants of the C1 CAS space the kernels run on
+    nfull = property(lambda self: self._info[3] * self._info[4])
+
+    def _occupations(self):
+        if self._empty:
+            return np.zeros((0, 6), np.int32), np.zeros((0, 6), np.int32), np.zeros((0, 2), np.int32)
+        na_, nb_, npair = self._binfo[9], self._binfo[10], self._binfo[11]
+        a = np.zeros((na_, 6), np.int32)
+        b = np.zeros((nb_, 6), np.int32)
+        pr = np.zeros((npair, 2), np.int32)
+        check(lib().f2g_strings_occupations(self.h, a.ctypes.data, b.ctypes.data, pr.ctypes.data))
+        return a, b, pr
+
+    @property
+    def gas_alpha_occupations(self):
+        return [list(map(int, r)) for r in self._occupations()[0]]
+
+    @property
+    def gas_beta_occupations(self):
+        return [list(map(int, r)) for r in self._occupations()[1]]
+
+    @property
+    def gas_occupations(self):
+        return [tuple(map(int, r)) for r in self._occupations()[2]]
+
+    def class_strings(self, spin):
+        """Strings of one spin in (class, address) order and their class indices."""
+        n = self._binfo[6 + spin]
+        masks = np.zeros(n, dtype=np.uint64)
+        classes = np.zeros(n, dtype=np.int32)
+        if n:
+            check(lib().f2g_strings_class_strings(self.h, spin, masks.ctypes.data, classes.ctypes.data))
+        return masks, classes
+
+    def block_table(self):
+        """Per block: alpha class, beta class, size, offset, alpha strings, beta strings."""
+        nblk = 0 if self._empty else self._binfo[5]
+        out = np.zeros((nblk, 6), dtype=np.int64)
+        if nblk:
+            check(lib().f2g_strings_block_table(self.h, out.ctypes.data))
+        return out
 
     def _masks(self, spin):
         n = self.nas if spin == 0 else self.nbs
         out = np.zeros(n, dtype=np.uint64)
         if n and not self._empty:
-            check(lib().f2g_strings_masks(self.h, spin, out.ctypes.data))
+            if self.blocked:
+                out = self.class_strings(spin)[0]
+            else:
+                check(lib().f2g_strings_masks(self.h, spin, out.ctypes.data))
         return out
 
     def alpha_masks(self):
@@ -141,23 +224,62 @@ class CIStrings:
     def beta_masks(self):
         return self._masks(1)
 
+    def determinant_masks(self):
+        """(ndet, 2) alpha and beta masks of every determinant in address order."""
+        if self._det_cache is None:
+            a, b = self.alpha_masks(), self.beta_masks()
+            if not self.blocked:
+                out = np.empty((len(a) * len(b), 2), dtype=np.uint64)
+                out[:, 0] = np.repeat(a, len(b))
+                out[:, 1] = np.tile(b, len(a))
+            else:
+                aoff = np.zeros(self._binfo[3] + 1, np.int64)
+                boff = np.zeros(self._binfo[4] + 1, np.int64)
+                _, ac = self.class_strings(0)
+                _, bc = self.class_strings(1)
+                aoff[1:] = np.cumsum(np.bincount(ac, minlength=self._binfo[3]))
+                boff[1:] = np.cumsum(np.bincount(bc, minlength=self._binfo[4]))
+                out = np.empty((self.ndet, 2), dtype=np.uint64)
+                for ca, cb, size, off, nia, nib in self.block_table():
+                    if size == 0:
+                        continue
+                    out[off:off + size, 0] = np.repeat(a[aoff[ca]:aoff[ca] + nia], nib)
+                    out[off:off + size, 1] = np.tile(b[boff[cb]:boff[cb] + nib], nia)
+            self._det_cache = out
+        return self._det_cache
+
     def determinant(self, address):
-        a = self.alpha_masks()
-        b = self.beta_masks()
-        return int(a[address // len(b)]), int(b[address % len(b)])
+        if not self.blocked:
+            a = self.alpha_masks()
+            b = self.beta_masks()
+            return int(a[address // len(b)]), int(b[address % len(b)])
+        m = self.determinant_masks()[address]
+        return int(m[0]), int(m[1])
 
     def determinant_index(self, det):
         a, b = det
-        am, bm = self.alpha_masks(), self.beta_masks()
-        ia = int(np.nonzero(am == np.uint64(a))[0][0])
-        ib = int(np.nonzero(bm == np.uint64(b))[0][0])
-        return ia * len(bm) + ib
+        if not self.blocked:
+            am, bm = self.alpha_masks(), self.beta_masks()
+            ia = int(np.nonzero(am == np.uint64(a))[0][0])
+            ib = int(np.nonzero(bm == np.uint64(b))[0][0])
+            return ia * len(bm) + ib
+        m = self.determinant_masks()
+        hit = np.nonzero((m[:, 0] == np.uint64(a)) & (m[:, 1] == np.uint64(b)))[0]
+        if len(hit) == 0:
+            raise KeyError("determinant not in this space")
+        return int(hit[0])
 
     def make_determinants(self):
         return Determinants(self)
 
+    def _c1_only(self):
+        if self.blocked:
+            raise NotImplementedError("CIStrings: the coupling lists are those of the C1 CAS space; a blocked "
+                                      "space keeps no lists of its own")
+
     def list_1h(self, spin):
         """1-hole list rows (class_K, K, class_I, sign, p, I) in the reference's order."""
+        self._c1_only()
         cnt = C.c_int64(0)
         check(lib().f2g_strings_list1h(self.h, spin, None, C.byref(cnt)))
         out = np.zeros((cnt.value, 6), dtype=np.int32)
@@ -167,6 +289,7 @@ class CIStrings:
 
     def list_2h(self, spin):
         """2-hole list rows (class_K, K, class_I, sign, p, q, I) in the reference's order."""
+        self._c1_only()
         cnt = C.c_int64(0)
         check(lib().f2g_strings_list2h(self.h, spin, None, C.byref(cnt)))
         out = np.zeros((cnt.value, 7), dtype=np.int32)

@@ -73,6 +73,149 @@ int f2g_strings_create(int na, int nb, int norb, void** out) {
     });
 }
 
+// the reference's (orbital_symmetry, gas_min, gas_max) arguments from flat arrays
+struct SpaceArgs {
+    std::vector<std::vector<int>> spaces;
+    std::vector<int> mn, mx;
+    int norb = 0;
+};
+static SpaceArgs space_args(int na, int nb, int nspace, const int* gas_size, const int* orbsym, int nmin,
+                            const int* gas_min, int nmax, const int* gas_max) {
+    if (na < 0 || nb < 0)
+        throw Error(2, "CIStrings: the number of electrons must be non-negative");
+    if (nspace < 0 || nmin < 0 || nmax < 0)
+        throw Error(2, "CIStrings: negative list length");
+    if ((nspace && !gas_size) || (nmin && !gas_min) || (nmax && !gas_max))
+        throw Error(2, "CIStrings: NULL list");
+    SpaceArgs a;
+    a.spaces.resize(nspace);
+    for (int g = 0; g < nspace; ++g) {
+        if (gas_size[g] < 0)
+            throw Error(2, "CIStrings: negative GAS space size");
+        if (gas_size[g] && !orbsym)
+            throw Error(2, "CIStrings: NULL orbital irreps");
+        for (int i = 0; i < gas_size[g]; ++i)
+            a.spaces[g].push_back(orbsym[a.norb++]);
+    }
+    if (na > a.norb || nb > a.norb)
+        throw Error(2, "CIStrings: more electrons than orbitals");
+    a.mn.assign(gas_min, gas_min + nmin);
+    a.mx.assign(gas_max, gas_max + nmax);
+    return a;
+}
+
+static void blocks_info(const DetBlocks& B, int64_t nfull, int64_t* out) {
+    const int64_t v[16] = {B.trivial ? 1 : 0,
+                           B.nirrep,
+                           B.nspace,
+                           B.nclass(0),
+                           B.nclass(1),
+                           B.nblk(),
+                           B.cls_off[0].back(),
+                           B.cls_off[1].back(),
+                           nfull,
+                           (int64_t)B.aocc.size(),
+                           (int64_t)B.bocc.size(),
+                           (int64_t)B.occ_pairs.size(),
+                           B.symmetry,
+                           B.ndet,
+                           0,
+                           0};
+    std::memcpy(out, v, sizeof(v));
+}
+
+int f2g_strings_create_general(int na, int nb, int symmetry, int nspace, const int* gas_size, const int* orbsym,
+                               int nmin, const int* gas_min, int nmax, const int* gas_max, void** out) {
+    return guard([&] {
+        need(out, "out");
+        const SpaceArgs a = space_args(na, nb, nspace, gas_size, orbsym, nmin, gas_min, nmax, gas_max);
+        *out = new CIStrings(na, nb, symmetry, a.spaces, a.mn, a.mx);
+    });
+}
+
+int f2g_strings_blocks_info(void* h, int64_t* out) {
+    return guard([&] {
+        need(h, "strings");
+        need(out, "out");
+        const auto* s = static_cast<CIStrings*>(h);
+        blocks_info(s->blocks, s->nfull, out);
+    });
+}
+
+int f2g_blocks_enumerate(int na, int nb, int symmetry, int nspace, const int* gas_size, const int* orbsym, int nmin,
+                         const int* gas_min, int nmax, const int* gas_max, int64_t* info, uint64_t* amasks,
+                         int32_t* aclasses, uint64_t* bmasks, int32_t* bclasses, int64_t* blocks) {
+    return guard([&] {
+        need(info, "info");
+        const SpaceArgs a = space_args(na, nb, nspace, gas_size, orbsym, nmin, gas_min, nmax, gas_max);
+        DetBlocks B;
+        B.enumerate(na, nb, symmetry, a.spaces, a.mn, a.mx);
+        blocks_info(B, (int64_t)(host_binom(a.norb, na) * host_binom(a.norb, nb)), info);
+        for (int spin = 0; spin < 2; ++spin) {
+            uint64_t* m = spin == 0 ? amasks : bmasks;
+            int32_t* c = spin == 0 ? aclasses : bclasses;
+            if (m)
+                std::copy(B.str[spin].begin(), B.str[spin].end(), m);
+            if (c)
+                for (int k = 0; k < B.nclass(spin); ++k)
+                    for (int64_t j = B.cls_off[spin][k]; j < B.cls_off[spin][k + 1]; ++j)
+                        c[j] = k;
+        }
+        if (blocks)
+            std::copy(B.hblk.begin(), B.hblk.end(), blocks);
+    });
+}
+
+int f2g_strings_class_strings(void* h, int spin, uint64_t* host_masks, int32_t* host_classes) {
+    return guard([&] {
+        need(h, "strings");
+        if (spin != 0 && spin != 1)
+            throw Error(2, "spin must be 0 or 1");
+        const auto* s = static_cast<CIStrings*>(h);
+        const DetBlocks& B = s->blocks;
+        const int64_t n = B.cls_off[spin].back();
+        if (n == 0)
+            return;
+        need(host_masks, "masks");
+        need(host_classes, "classes");
+        if (B.str[spin].empty()) // C1 space built without enumeration: the C1 strings, one class
+            F2G_CUDA(cudaMemcpy(host_masks, s->spin(spin).str.get(), n * 8, cudaMemcpyDeviceToHost));
+        else
+            std::memcpy(host_masks, B.str[spin].data(), n * 8);
+        for (int c = 0; c < B.nclass(spin); ++c)
+            for (int64_t j = B.cls_off[spin][c]; j < B.cls_off[spin][c + 1]; ++j)
+                host_classes[j] = c;
+    });
+}
+
+int f2g_strings_block_table(void* h, int64_t* host_out) {
+    return guard([&] {
+        need(h, "strings");
+        const DetBlocks& B = static_cast<CIStrings*>(h)->blocks;
+        if (B.hblk.empty())
+            return;
+        need(host_out, "out");
+        std::memcpy(host_out, B.hblk.data(), B.hblk.size() * sizeof(int64_t));
+    });
+}
+
+int f2g_strings_occupations(void* h, int32_t* host_aocc, int32_t* host_bocc, int32_t* host_pairs) {
+    return guard([&] {
+        need(h, "strings");
+        const DetBlocks& B = static_cast<CIStrings*>(h)->blocks;
+        for (size_t i = 0; host_aocc && i < B.aocc.size(); ++i)
+            for (int g = 0; g < kMaxGasSpaces; ++g)
+                host_aocc[i * kMaxGasSpaces + g] = B.aocc[i][g];
+        for (size_t i = 0; host_bocc && i < B.bocc.size(); ++i)
+            for (int g = 0; g < kMaxGasSpaces; ++g)
+                host_bocc[i * kMaxGasSpaces + g] = B.bocc[i][g];
+        for (size_t i = 0; host_pairs && i < B.occ_pairs.size(); ++i) {
+            host_pairs[2 * i] = B.occ_pairs[i].first;
+            host_pairs[2 * i + 1] = B.occ_pairs[i].second;
+        }
+    });
+}
+
 int f2g_strings_destroy(void* s) {
     return guard([&] { delete static_cast<CIStrings*>(s); });
 }

@@ -150,24 +150,26 @@ __device__ inline void pattern_and_sign(uint64_t a, uint64_t b, int twoMs, const
     neg = ng;
 }
 
-__global__ void k_conf_first(int64_t N0a, int64_t N0b, const uint64_t* sa, const uint64_t* sb, int twoS,
-                             ConfSpace cs, uint32_t* first) {
+// Determinant i of the space comes from the enumerator (blocks of a point-group / GAS space, or
+// the C1 strings); configurations are ranked over all configurations of the active orbitals.
+__global__ void k_conf_first(DetEnum de, int twoS, ConfSpace cs, uint32_t* first) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= N0a * N0b)
+    if (i >= de.ndet)
         return;
-    const uint64_t a = sa[i / N0b], b = sb[i % N0b];
+    uint64_t a, b;
+    de.at(i, a, b);
     const uint64_t d = a & b, s = a ^ b;
     if (popc64(s) < twoS)
         return;
     atomicMin(first + conf_rank(d, s, cs), (uint32_t)i);
 }
 
-__global__ void k_conf_flag(int64_t N0a, int64_t N0b, const uint64_t* sa, const uint64_t* sb, int twoS,
-                            ConfSpace cs, const uint32_t* first, uint32_t* flag) {
+__global__ void k_conf_flag(DetEnum de, int twoS, ConfSpace cs, const uint32_t* first, uint32_t* flag) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= N0a * N0b)
+    if (i >= de.ndet)
         return;
-    const uint64_t a = sa[i / N0b], b = sb[i % N0b];
+    uint64_t a, b;
+    de.at(i, a, b);
     const uint64_t d = a & b, s = a ^ b;
     uint32_t f = 0;
     if (popc64(s) >= twoS)
@@ -175,13 +177,14 @@ __global__ void k_conf_flag(int64_t N0a, int64_t N0b, const uint64_t* sa, const 
     flag[i] = f;
 }
 
-__global__ void k_conf_fill(int64_t N0a, int64_t N0b, const uint64_t* sa, const uint64_t* sb, const uint32_t* flag,
-                            const uint32_t* cidx, const int* ncsfN, const int* ndetN, uint64_t* conf_d,
-                            uint64_t* conf_s, int64_t* conf_ncsf, int64_t* conf_nslot) {
+__global__ void k_conf_fill(DetEnum de, const uint32_t* flag, const uint32_t* cidx, const int* ncsfN,
+                            const int* ndetN, uint64_t* conf_d, uint64_t* conf_s, int64_t* conf_ncsf,
+                            int64_t* conf_nslot) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= N0a * N0b || !flag[i])
+    if (i >= de.ndet || !flag[i])
         return;
-    const uint64_t a = sa[i / N0b], b = sb[i % N0b];
+    uint64_t a, b;
+    de.at(i, a, b);
     const uint32_t c = cidx[i];
     const uint64_t s = a ^ b;
     conf_d[c] = a & b;
@@ -190,13 +193,13 @@ __global__ void k_conf_fill(int64_t N0a, int64_t N0b, const uint64_t* sa, const 
     conf_nslot[c] = ndetN[popc64(s)];
 }
 
-__global__ void k_conf_perm(int64_t N0a, int64_t N0b, const uint64_t* sa, const uint64_t* sb, int twoS, int twoMs,
-                            ConfSpace cs, const uint32_t* first, const uint32_t* cidx, const int64_t* conf_slot,
-                            uint32_t* perm) {
+__global__ void k_conf_perm(DetEnum de, int twoS, int twoMs, ConfSpace cs, const uint32_t* first,
+                            const uint32_t* cidx, const int64_t* conf_slot, uint32_t* perm) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= N0a * N0b)
+    if (i >= de.ndet)
         return;
-    const uint64_t a = sa[i / N0b], b = sb[i % N0b];
+    uint64_t a, b;
+    de.at(i, a, b);
     const uint64_t d = a & b, s = a ^ b;
     if (popc64(s) < twoS)
         return;
@@ -313,8 +316,34 @@ __global__ void k_det_to_csf(int64_t ncsf, CsfView v, const T* __restrict__ det,
     // transposed table: the threads of a configuration (consecutive i) read consecutive entries
     const T* O = overlaps_t<T>(v) + v.offN[N] + i;
     const uint32_t* pm = v.perm + v.conf_slot[c];
+    // eight determinants per step: their table entries and addresses, then their values, are
+    // requested together (the value loads depend on the addresses); zero entries skip the load.
+    // The sum runs over j in order, as one determinant per step would.
+    constexpr int U = 8;
     T acc = 0;
-    for (int j = 0; j < nd; ++j) {
+    int j = 0;
+    for (; j + U <= nd; j += U) {
+        T o[U], x[U];
+        uint32_t e[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            o[k] = O[(int64_t)(j + k) * nc];
+            e[k] = pm[j + k];
+        }
+#pragma unroll
+        for (int k = 0; k < U; ++k)
+            x[k] = o[k] != T(0) ? det[e[k] & 0x7fffffffu] : T(0);
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            if (o[k] == T(0))
+                continue;
+            if (SQUARE)
+                acc += o[k] * o[k] * x[k];
+            else
+                acc += ((e[k] >> 31) ? -o[k] : o[k]) * x[k];
+        }
+    }
+    for (; j < nd; ++j) {
         const T o = O[(int64_t)j * nc];
         if (o == T(0))
             continue;
@@ -413,8 +442,8 @@ __device__ double slater_rules(uint64_t la, uint64_t lb, uint64_t ra, uint64_t r
     return det_energy(la, lb, n, E0, h, V);
 }
 
-__global__ void k_csf_matrix(int m, const int64_t* idx, CsfView v, int64_t N0b, const uint64_t* sa,
-                             const uint64_t* sb, int n, double E0, const double* h, const double* V, double* out) {
+__global__ void k_csf_matrix(int m, const int64_t* idx, CsfView v, DetEnum de, int n, double E0, const double* h,
+                             const double* V, double* out) {
     const int A = blockIdx.x, B = blockIdx.y;
     if (B > A)
         return;
@@ -436,7 +465,10 @@ __global__ void k_csf_matrix(int m, const int64_t* idx, CsfView v, int64_t N0b, 
         const uint32_t ea = pa[ja], eb = pb[jb];
         const int64_t da = ea & 0x7fffffffu, db = eb & 0x7fffffffu;
         const double c = ((ea >> 31) ? -oa : oa) * ((eb >> 31) ? -ob : ob);
-        acc += c * slater_rules(sa[da / N0b], sb[da % N0b], sa[db / N0b], sb[db % N0b], n, E0, h, V);
+        uint64_t la, lb, ra, rb;
+        de.at(da, la, lb);
+        de.at(db, ra, rb);
+        acc += c * slater_rules(la, lb, ra, rb, n, E0, h, V);
     }
     red[threadIdx.x] = acc;
     __syncthreads();
@@ -537,7 +569,8 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
     F2G_CUDA(cudaMemcpyAsync(dbase.get(), base.data(), (n + 2) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
     ConfSpace cs{n, nel, dbase.get(), s->binom.get()};
 
-    const int64_t NA = s->a.N0, NB = s->b.N0, nd_ = NA * NB;
+    const DetEnum de = s->dets();
+    const int64_t nd_ = s->ndet;
     if (nd_ > 0x7fffffffLL)
         throw Error(1, "CISpinAdapter: more than 2^31 determinants");
     TmpBuf<uint32_t> first(std::max<int64_t>(1, total), st), flag(std::max<int64_t>(1, nd_), st),
@@ -545,10 +578,9 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
     F2G_CUDA(cudaMemsetAsync(first.get(), 0xff, std::max<int64_t>(1, total) * sizeof(uint32_t), st));
     const int T = 256;
     if (nd_ > 0) {
-        k_conf_first<<<ceil_div(nd_, T), T, 0, st>>>(NA, NB, s->a.str.get(), s->b.str.get(), twoS, cs, first.get());
+        k_conf_first<<<ceil_div(nd_, T), T, 0, st>>>(de, twoS, cs, first.get());
         F2G_LAUNCH("k_conf_first");
-        k_conf_flag<<<ceil_div(nd_, T), T, 0, st>>>(NA, NB, s->a.str.get(), s->b.str.get(), twoS, cs, first.get(),
-                                                   flag.get());
+        k_conf_flag<<<ceil_div(nd_, T), T, 0, st>>>(de, twoS, cs, first.get(), flag.get());
         F2G_LAUNCH("k_conf_flag");
         exclusive_scan<uint32_t>(flag.get(), cidx.get(), nd_, st);
         uint32_t last_flag = 0, last_idx = 0;
@@ -565,9 +597,8 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
     F2G_CUDA(cudaMemsetAsync(cnc.get(), 0, (nconf + 1) * sizeof(int64_t), st));
     F2G_CUDA(cudaMemsetAsync(cns.get(), 0, (nconf + 1) * sizeof(int64_t), st));
     if (nconf > 0) {
-        k_conf_fill<<<ceil_div(nd_, T), T, 0, st>>>(NA, NB, s->a.str.get(), s->b.str.get(), flag.get(), cidx.get(),
-                                                   dNcsf.get(), dNdet.get(), conf_d.get(), conf_s.get(), cnc.get(),
-                                                   cns.get());
+        k_conf_fill<<<ceil_div(nd_, T), T, 0, st>>>(de, flag.get(), cidx.get(), dNcsf.get(), dNdet.get(),
+                                                   conf_d.get(), conf_s.get(), cnc.get(), cns.get());
         F2G_LAUNCH("k_conf_fill");
     }
     exclusive_scan<int64_t>(cnc.get(), conf_csf.get(), nconf + 1, st);
@@ -578,8 +609,8 @@ SpinAdapter::SpinAdapter(const CIStrings* s_, int twoS_, int twoMs_)
     covers_all_dets = nslot == nd_;
     perm.reserve(std::max<int64_t>(1, nslot));
     if (nslot > 0) {
-        k_conf_perm<<<ceil_div(nd_, T), T, 0, st>>>(NA, NB, s->a.str.get(), s->b.str.get(), twoS, twoMs, cs,
-                                                   first.get(), cidx.get(), conf_slot.get(), perm.get());
+        k_conf_perm<<<ceil_div(nd_, T), T, 0, st>>>(de, twoS, twoMs, cs, first.get(), cidx.get(), conf_slot.get(),
+                                                   perm.get());
         F2G_LAUNCH("k_conf_perm");
     }
     // configuration brackets of the 256-element blocks of the transform kernels
@@ -761,8 +792,8 @@ void SpinAdapter::csf_matrix_dev(const SigmaBuilder& sb, const int64_t* idx, int
         return;
     if (m > 65535)
         throw Error(2, "csf_matrix: at most 65535 CSFs per call");
-    k_csf_matrix<<<dim3(m, m), 256, 0, st>>>(m, idx, view_of(*this), s->b.N0, s->a.str.get(), s->b.str.get(), norb,
-                                             sb.E, sb.dH.get(), sb.dV.get(), out);
+    k_csf_matrix<<<dim3(m, m), 256, 0, st>>>(m, idx, view_of(*this), s->dets(), norb, sb.E, sb.dH.get(), sb.dV.get(),
+                                             out);
     F2G_LAUNCH("k_csf_matrix");
 }
 

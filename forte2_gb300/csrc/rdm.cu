@@ -584,6 +584,21 @@ void compute_rdm(SigmaBuilder& sb, int kind, const double* CL, const double* CR,
         return;
     if (!CL || !CR || !out)
         throw Error(2, "RDM: NULL vector or output");
+    if (sb.s->blocked()) {
+        // a blocked space's vectors embedded into C1 vectors: the RDMs are those of the embedding
+        const DetEnum de = sb.s->dets();
+        const int64_t nf = sb.s->nfull;
+        double* xl = sb.xC.reserve(nf);
+        blocks_embed<double>(de, nf, CL, xl, 1, st);
+        const double* xr = xl;
+        if (CR != CL) {
+            double* t = sb.xS.reserve(nf);
+            blocks_embed<double>(de, nf, CR, t, 1, st);
+            xr = t;
+        }
+        CL = xl;
+        CR = xr;
+    }
     F2G_CUDA(cudaMemsetAsync(out, 0, (size_t)size * sizeof(double), st));
     switch (kind) {
     case kRdmA1:

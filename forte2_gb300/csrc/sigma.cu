@@ -715,23 +715,45 @@ void SigmaBuilder::prepare_untimed(int nvec) {
     if (*graph_users > 0)
         throw Error(2, "sigma builder: captured graphs use its graph scratch for " + std::to_string(untimed_nvec) +
                            " vectors; a graph of " + std::to_string(nvec) + " vectors needs a new builder");
-    const size_t tot = (size_t)nvec * std::max<int64_t>(1, s->ndet);
+    const size_t tot = (size_t)nvec * std::max<int64_t>(1, s->nfull);
     gCt.reserve(tot);
     gTt.reserve(tot);
     gfC.reserve(tot);
     gfS.reserve(tot);
     gfCt.reserve(tot);
     gfTt.reserve(tot);
+    if (s->blocked()) {
+        gxC.reserve(tot);
+        gxS.reserve(tot);
+        gxfC.reserve(tot);
+        gxfS.reserve(tot);
+    }
     untimed_nvec = nvec;
 }
 
 void SigmaBuilder::apply_f32(const float* C, float* S, cudaStream_t st, int nvec, bool timed, bool graph) {
-    const int64_t nd = s->ndet;
-    if (nd == 0 || nvec <= 0)
+    const int64_t nd = s->nfull;
+    if (s->ndet == 0 || nvec <= 0)
         return;
     if (!fp32_ready)
         throw Error(1, "apply_f32: FP32 Hamiltonian copies are not ready (select FP32 precision first)");
     const size_t tot = (size_t)nvec * nd;
+    if (s->blocked()) {
+        if (graph && nvec > untimed_nvec)
+            throw Error(2, "apply_f32: more vectors than prepared");
+        float* xc = graph ? gxfC.get() : xfC.reserve(tot);
+        float* xs = graph ? gxfS.get() : xfS.reserve(tot);
+        const DetEnum de = s->dets();
+        blocks_embed<float>(de, nd, C, xc, nvec, st);
+        apply_f32_c1(xc, xs, st, nvec, timed, graph, tot);
+        blocks_extract<float>(de, nd, xs, S, nvec, st);
+        return;
+    }
+    apply_f32_c1(C, S, st, nvec, timed, graph, tot);
+}
+
+void SigmaBuilder::apply_f32_c1(const float* C, float* S, cudaStream_t st, int nvec, bool timed, bool graph,
+                                size_t tot) {
     float *ct, *tt;
     if (graph) {
         if (nvec > untimed_nvec)
@@ -756,6 +778,13 @@ void SigmaBuilder::apply_untimed(const double* C, double* sigma, cudaStream_t st
         throw Error(2, "apply_untimed: more vectors than prepared");
     if (precision == kFP32 && !fp32_ready)
         throw Error(1, "apply_untimed: FP32 Hamiltonian copies are not ready");
+    if (s->blocked()) {
+        const DetEnum de = s->dets();
+        blocks_embed<double>(de, s->nfull, C, gxC.get(), nvec, st);
+        apply_batch(gxC.get(), gxS.get(), st, nvec, false, true);
+        blocks_extract<double>(de, s->nfull, gxS.get(), sigma, nvec, st);
+        return;
+    }
     apply_batch(C, sigma, st, nvec, false, true);
 }
 
@@ -1025,20 +1054,34 @@ void SigmaBuilder::avg_build_time(double* out) {
 constexpr int64_t kBatchElems = int64_t(1) << 24;
 
 int SigmaBuilder::batch_size(int nvec) const {
-    const int64_t nd = std::max<int64_t>(1, s->ndet);
+    const int64_t nd = std::max<int64_t>(1, s->nfull);
     return (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)nvec, kBatchElems / nd, 65535}));
 }
 
 void SigmaBuilder::hamiltonian(const double* C, double* sigma, cudaStream_t st, int nvec) {
     check_memory();
-    const int64_t nd = s->ndet;
+    const int64_t nd = s->ndet, nf = s->nfull;
     if (nd == 0 || nvec <= 0)
         return;
     const int bs = batch_size(nvec);
+    const DetEnum de = s->dets();
     for (int v0 = 0; v0 < nvec; v0 += bs) {
         const int nv = std::min(bs, nvec - v0);
+        const double* c = C + (int64_t)v0 * nd;
+        double* sg = sigma + (int64_t)v0 * nd;
+        if (s->blocked()) {
+            // the space's vectors embedded into C1 vectors (zero elsewhere), sigma read back
+            double* xc = xC.reserve((size_t)nv * nf);
+            double* xs = xS.reserve((size_t)nv * nf);
+            blocks_embed<double>(de, nf, c, xc, nv, st);
+            timer_begin();
+            apply_batch(xc, xs, st, nv, true, false);
+            timer_end(nv);
+            blocks_extract<double>(de, nf, xs, sg, nv, st);
+            continue;
+        }
         timer_begin();
-        apply_batch(C + (int64_t)v0 * nd, sigma + (int64_t)v0 * nd, st, nv, true, false);
+        apply_batch(c, sg, st, nv, true, false);
         timer_end(nv);
     }
 }
@@ -1046,7 +1089,7 @@ void SigmaBuilder::hamiltonian(const double* C, double* sigma, cudaStream_t st, 
 // graph: use the scratch set reserved by prepare_untimed (never reallocated while graphs captured
 // with it exist); otherwise the growable scratch.
 void SigmaBuilder::apply_batch(const double* C, double* sigma, cudaStream_t st, int nvec, bool timed, bool graph) {
-    const int64_t nd = s->ndet;
+    const int64_t nd = s->nfull;
     const size_t tot = (size_t)nvec * nd;
     if (precision == kFP64) {
         double* ct = graph ? gCt.get() : Ct.reserve(tot);
@@ -1066,9 +1109,23 @@ void SigmaBuilder::apply_batch(const double* C, double* sigma, cudaStream_t st, 
 }
 
 void SigmaBuilder::term(int which, const double* C, double* sigma, cudaStream_t st) {
-    const int64_t nd = s->ndet;
-    if (nd == 0)
+    if (s->ndet == 0)
         return;
+    if (s->blocked()) {
+        const DetEnum de = s->dets();
+        double* xc = xC.reserve(s->nfull);
+        double* xs = xS.reserve(s->nfull);
+        blocks_embed<double>(de, s->nfull, C, xc, 1, st);
+        term_c1(which, xc, xs, st);
+        blocks_extract<double>(de, s->nfull, xs, sigma, 1, st);
+        F2G_CUDA(cudaStreamSynchronize(st));
+        return;
+    }
+    term_c1(which, C, sigma, st);
+}
+
+void SigmaBuilder::term_c1(int which, const double* C, double* sigma, cudaStream_t st) {
+    const int64_t nd = s->nfull;
     if (which == 0) {
         k_scale<<<1024, 256, 0, st>>>(nd, E, C, sigma);
         F2G_LAUNCH("k_scale");
@@ -1112,15 +1169,20 @@ void SigmaBuilder::term(int which, const double* C, double* sigma, cudaStream_t 
 // call, so no implicit device synchronisation).
 void SigmaBuilder::det_energies(double* out, cudaStream_t st) {
     const int64_t NA = s->a.N0, NB = s->b.N0;
-    if (NA * NB == 0)
+    if (NA * NB == 0 || s->ndet == 0)
         return;
+    double* full = out;
+    if (s->blocked())
+        full = xS.reserve(NA * NB); // C1 energies, then the space's
     double* ea = eA.reserve(NA);
     double* eb = eB.reserve(NB);
     double* jr = eJ.reserve((size_t)NA * std::max(1, n));
     k_string_energy<<<ceil_div(NA, 128), 128, 0, st>>>(n, NA, s->a.str.get(), dH.get(), dV.get(), ea, jr);
     k_string_energy<<<ceil_div(NB, 128), 128, 0, st>>>(n, NB, s->b.str.get(), dH.get(), dV.get(), eb, nullptr);
-    k_det_energy<<<ceil_div(NA * NB, 256), 256, 0, st>>>(n, NA, NB, E, s->b.str.get(), ea, eb, jr, out);
+    k_det_energy<<<ceil_div(NA * NB, 256), 256, 0, st>>>(n, NA, NB, E, s->b.str.get(), ea, eb, jr, full);
     F2G_LAUNCH("k_det_energy");
+    if (s->blocked())
+        blocks_extract<double>(s->dets(), NA * NB, full, out, 1, st);
 }
 
 } // namespace f2g

@@ -103,6 +103,7 @@ struct SigmaBuilder {
     // FP32 vectors in and out (the mixed mode's CSF-space sigma): timed like hamiltonian, or
     // untimed on the graph scratch
     void apply_f32(const float* C, float* S, cudaStream_t st, int nvec, bool timed, bool graph);
+    // (all public calls take vectors of the space; a blocked space's are embedded into C1 vectors)
     void prepare_untimed(int nvec);
     void apply_untimed(const double* C, double* sigma, cudaStream_t st, int nvec);
     int untimed_nvec = 0;
@@ -111,6 +112,9 @@ struct SigmaBuilder {
     std::shared_ptr<int> graph_users = std::make_shared<int>(0);
     DevBuf<double> gCt, gTt;
     DevBuf<float> gfC, gfS, gfCt, gfTt;
+    // C1-sized copies of a blocked space's vectors (timed / host calls, and the graph scratch)
+    DevBuf<double> xC, xS, gxC, gxS;
+    DevBuf<float> xfC, xfS, gxfC, gxfS;
     // one HZ term into sigma (overwrites): 0 H0, 1 H1 alpha, 2 H1 beta, 3 opposite spin (aabb),
     // 4 alpha same-spin two-electron part alone (aaaa), 5 beta same-spin two-electron part (bbbb)
     void term(int which, const double* C, double* sigma, cudaStream_t st);
@@ -124,6 +128,8 @@ struct SigmaBuilder {
     template <typename T>
     void run(const T* C, T* sig, cudaStream_t st, int mask, bool timed, int nvec, T* Ct_, T* Tt_, bool graph);
     void apply_batch(const double* C, double* sigma, cudaStream_t st, int nvec, bool timed, bool graph);
+    void apply_f32_c1(const float* C, float* S, cudaStream_t st, int nvec, bool timed, bool graph, size_t tot);
+    void term_c1(int which, const double* C, double* sigma, cudaStream_t st);
 };
 
 int ss_row_nnz(int n, int k);

@@ -112,18 +112,50 @@ void SpinStrings::build_up2(const uint64_t* d_binom, cudaStream_t st) {
 }
 
 CIStrings::CIStrings(int na_, int nb_, int norb_) : norb(norb_), na(na_), nb(nb_) {
+    build_c1();
+    blocks.set_c1(na, nb, a.N0, b.N0);
+    ndet = nfull;
+}
+
+CIStrings::CIStrings(int na_, int nb_, int symmetry, const std::vector<std::vector<int>>& orbital_symmetry,
+                     const std::vector<int>& gas_min, const std::vector<int>& gas_max)
+    : na(na_), nb(nb_) {
+    norb = 0;
+    for (const auto& sp : orbital_symmetry)
+        norb += (int)sp.size();
+    build_c1();
+    blocks.build(na, nb, symmetry, orbital_symmetry, gas_min, gas_max);
+    ndet = blocks.ndet;
+    if (blocks.trivial)
+        blocks.set_c1(na, nb, a.N0, b.N0); // the C1 strings themselves, one block
+}
+
+void CIStrings::build_c1() {
     if (norb < 0 || norb > kMaxOrb)
         throw Error(2, "CIStrings: the number of active orbitals must be between 0 and 62");
     std::vector<uint64_t> h(kBinomLd * kBinomLd, 0);
-    for (int a = 0; a < kBinomLd; ++a)
-        for (int b = 0; b < kBinomLd; ++b)
-            h[a * kBinomLd + b] = host_binom(a, b);
+    for (int x = 0; x < kBinomLd; ++x)
+        for (int y = 0; y < kBinomLd; ++y)
+            h[x * kBinomLd + y] = host_binom(x, y);
     binom.reserve(h.size());
     F2G_CUDA(cudaMemcpy(binom.get(), h.data(), h.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
     a.build(norb, na, binom.get(), 0);
     b.build(norb, nb, binom.get(), 0);
     F2G_CUDA(cudaStreamSynchronize(0)); // set-up ran on the legacy stream: wait for it alone
-    ndet = a.N0 * b.N0;
+    nfull = a.N0 * b.N0;
+}
+
+DetEnum CIStrings::dets() const {
+    if (blocked())
+        return blocks.view(b.N0);
+    DetEnum d;
+    d.ndet = nfull;
+    d.nblk = nfull > 0 ? 1 : 0;
+    d.blk = blocks.dblk.get();
+    d.amask = a.str.get();
+    d.bmask = b.str.get();
+    d.N0b = b.N0;
+    return d;
 }
 
 } // namespace f2g

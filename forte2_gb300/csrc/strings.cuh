@@ -3,6 +3,7 @@
 
 #include <vector>
 
+#include "blocks.cuh"
 #include "common.cuh"
 
 namespace f2g {
@@ -21,14 +22,29 @@ struct SpinStrings {
     void build_up2(const uint64_t* d_binom, cudaStream_t st);
 };
 
+// The strings of an active space. The coupling lists and the sigma kernels always cover the C1
+// CAS space of all orbitals (a, b: every string of na / nb electrons, nfull determinants). A
+// space with point-group irreps or GAS restrictions is a set of determinant blocks of it
+// (`blocks`, ndet determinants in the reference's order); its vectors are embedded into C1
+// vectors for the sigma and RDM kernels. A C1 CAS space is one trivial block.
 struct CIStrings {
     int norb, na, nb;
-    int64_t ndet = 0;
+    int64_t ndet = 0;  // determinants of the space
+    int64_t nfull = 0; // determinants of the C1 CAS space (the sigma kernels' vectors)
     DevBuf<uint64_t> binom; // C(a, b) at [a * kBinomLd + b]
     SpinStrings a, b;
+    DetBlocks blocks;
     CIStrings(int na, int nb, int norb);
+    // the reference's CIStrings(na, nb, symmetry, orbital_symmetry, gas_min, gas_max)
+    CIStrings(int na, int nb, int symmetry, const std::vector<std::vector<int>>& orbital_symmetry,
+              const std::vector<int>& gas_min, const std::vector<int>& gas_max);
+    bool blocked() const { return !blocks.trivial; }
+    DetEnum dets() const; // determinant i of the space -> its strings
     const SpinStrings& spin(int s) const { return s == 0 ? a : b; }
     SpinStrings& spin(int s) { return s == 0 ? a : b; }
+
+  private:
+    void build_c1();
 };
 
 } // namespace f2g

@@ -82,6 +82,18 @@ def rotate_integrals(ints: ActiveSpaceIntegrals, seed: int, theta: float = 0.05)
     return ActiveSpaceIntegrals(ints.E, np.ascontiguousarray(h), V, eri)
 
 
+def symmetrize_integrals(ints: ActiveSpaceIntegrals, orbsym) -> ActiveSpaceIntegrals:
+    """The integrals of a molecule with an abelian point group: with irreps ``orbsym[p]`` (0..7,
+    the product of two irreps their XOR), h[p][q] = 0 unless p and q share an irrep and
+    (pq|rs) = 0 unless the product of the four irreps is the totally symmetric one."""
+    g = np.asarray(orbsym, dtype=np.int64)
+    h = np.where(g[:, None] == g[None, :], ints.H, 0.0)
+    allowed = (g[:, None, None, None] ^ g[None, :, None, None] ^ g[None, None, :, None] ^ g[None, None, None, :]) == 0
+    eri = np.where(allowed, ints.eri, 0.0)
+    V = np.ascontiguousarray(eri.transpose(0, 2, 1, 3))
+    return ActiveSpaceIntegrals(ints.E, np.ascontiguousarray(h), V, eri)
+
+
 def random_ci_vector(ndet: int, seed: int) -> np.ndarray:
     """Normalised N(0,1) determinant vector (as in the reference's tests/ci/test_ci_rdms.py:387)."""
     rng = np.random.default_rng(seed)

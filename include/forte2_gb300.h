@@ -33,9 +33,36 @@ const char* f2g_version(void);
  *      (forte2/ci/ci_strings.cc:26-184; binding api/ci_helpers_api.cc:55-86). Strings, 1-hole
  *      and 2-hole lists are built on the device. */
 int f2g_strings_create(int na, int nb, int norb, void** out);
+/* The general constructor: nspace GAS spaces of gas_size[g] orbitals each, orbsym the irreps
+ * (0..7) of all orbitals space after space, gas_min[nmin] / gas_max[nmax] the electron bounds
+ * per space, symmetry the state irrep. The determinants are the reference's blocks in its
+ * order (ci_strings.cc:34-184, ci_occupation.cc:35-142, ci_string_class.cc:7-66,
+ * ci_strings_makers.cc:13-73); the sigma, RDM and CSF calls take vectors of ndet elements in
+ * that order and run the C1 kernels on an embedding into the C1 CAS space of all orbitals. */
+int f2g_strings_create_general(int na, int nb, int symmetry, int nspace, const int* gas_size, const int* orbsym,
+                               int nmin, const int* gas_min, int nmax, const int* gas_max, void** out);
 int f2g_strings_destroy(void* strings);
-/* out[10]: norb, na, nb, nas, nbs, ndet, N1a, N1b, N2a, N2b */
+/* out[10]: norb, na, nb, N0a, N0b (C1 strings), ndet (of the space), N1a, N1b, N2a, N2b */
 int f2g_strings_info(void* strings, int64_t* out);
+/* out[16]: trivial (the C1 space in C1 order), nirrep, GAS spaces, alpha classes, beta
+ * classes, blocks, nas, nbs (strings of all classes), C1 determinants, alpha occupation
+ * patterns, beta patterns, allowed pattern pairs, symmetry, ndet, 0, 0 */
+int f2g_strings_blocks_info(void* strings, int64_t* out);
+/* The same enumeration on the host alone (no device call), for checks: info[16] as
+ * f2g_strings_blocks_info; then, where not NULL, the class strings and classes of both spins
+ * (nas / nbs entries) and the block table (6 per block). */
+int f2g_blocks_enumerate(int na, int nb, int symmetry, int nspace, const int* gas_size, const int* orbsym, int nmin,
+                         const int* gas_min, int nmax, const int* gas_max, int64_t* info, uint64_t* amasks,
+                         int32_t* aclasses, uint64_t* bmasks, int32_t* bclasses, int64_t* blocks);
+/* Strings of one spin in (class, address) order (CIStrings::alpha_strings / beta_strings) and
+ * their class indices. */
+int f2g_strings_class_strings(void* strings, int spin, uint64_t* host_masks, int32_t* host_classes);
+/* Blocks (determinant_classes, ci_string_class.cc:56-65): per block alpha class, beta class,
+ * size, offset, alpha strings, beta strings. */
+int f2g_strings_block_table(void* strings, int64_t* host_out);
+/* Occupation patterns: alpha / beta patterns (6 ints each) and the allowed (alpha, beta) pairs
+ * (gas_alpha_occupations, gas_beta_occupations, gas_occupations); NULL skips an output. */
+int f2g_strings_occupations(void* strings, int32_t* host_aocc, int32_t* host_bocc, int32_t* host_pairs);
 /* Occupation masks (bit p = orbital p) of one spin (0 alpha, 1 beta) in address order. */
 int f2g_strings_masks(void* strings, int spin, uint64_t* host_out);
 /* 1-hole list rows (class_K, K, class_I, sign, p, I), the reference's get_*_1h_list2 content

@@ -240,12 +240,13 @@ def gen_sigma_checksums(out, cases, fname):
 
 
 def reference_casci(na, nb, n, mult, twice_ms, nroot, iseed, e_tol, DavidsonLiuSolver, Params,
-                    maxiter=100, ints=None, solver=None, return_solver=False):
+                    maxiter=100, ints=None, solver=None, return_solver=False, space=None):
     """Drive the reference Davidson exactly as forte2/ci/ci.py:_do_iterative_ci does. With `solver`
     (a DavidsonLiuSolver that has already solved), it continues from that solver's vectors with the
     new integrals, as the reference's MCSCF loop does (ci.py:266-290, mc_optimizer.py:297-328)."""
     ints = make_integrals(n, iseed) if ints is None else ints
-    s = ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
+    # space: (symmetry, orbital_symmetry, gas_min, gas_max) of a blocked space, else C1 CAS
+    s = ref.RefCIStrings(na, nb, *space) if space else ref.RefCIStrings(na, nb, 0, [[0] * n], [], [])
     sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
     sb.set_algorithm("hz")
     sa = ref.RefSpinAdapter(mult - 1, twice_ms, n)
@@ -323,6 +324,95 @@ def gen_davidson(out, ref_root):
         json.dump(meta, f, indent=1)
 
 
+# Spaces with point-group irreps and GAS restrictions (the reference's determinant blocks):
+# (na, nb, symmetry, orbital_symmetry, gas_min, gas_max, integral seed, vector seed, symmetric
+# integrals). The last one has no determinants.
+BLOCK_CASES = [(3, 3, 1, [[0, 0, 1, 2, 3, 0]], [], [], 61, 601, False),
+               (3, 3, 0, [[0, 0, 0], [0, 0, 0]], [4], [6], 62, 602, False),
+               (2, 2, 0, [[0, 0], [0, 0]], [0, 0], [4, 4], 63, 603, False),
+               (4, 3, 3, [[0, 1, 2, 3, 0, 1, 2, 3]], [], [], 64, 604, True),
+               (3, 3, 0, [[0, 1, 0], [1, 0, 1], [0, 0]], [2, 2, 0], [6, 4, 2], 65, 605, True),
+               (4, 4, 2, [[0, 2, 1], [3, 0, 1, 2], [0]], [3, 1], [6, 6, 1], 66, 606, False),
+               (3, 3, 5, [[0, 1, 2, 3, 4, 5, 6, 7]], [], [], 67, 607, True),
+               (4, 4, 0, [[0, 0], [0, 0, 0], [0, 0, 0]], [2, 2, 0], [4, 6, 2], 68, 608, False),
+               (1, 2, 0, [[1, 1, 0]], [], [], 70, 610, False),
+               (5, 4, 1, [[0, 1, 0, 1, 0], [1, 0, 1, 0, 1]], [3], [8], 71, 611, True),
+               (2, 3, 0, [[1, 1, 1, 1]], [], [], 69, 609, False)]
+
+# CASCI in blocked spaces: (na, nb, symmetry, orbital_symmetry, gas_min, gas_max, multiplicity,
+# nroot, integral seed, symmetric integrals)
+BLOCK_CASCI_CASES = [(4, 4, 0, [[0, 1, 2, 3, 0, 1, 2, 3]], [], [], 1, 2, 81, True),
+                     (4, 4, 2, [[0, 1, 2, 3, 0, 1, 2, 3]], [], [], 3, 1, 82, True),
+                     (3, 3, 0, [[0, 0, 0], [0, 0, 0]], [4], [6], 1, 2, 83, False),
+                     (5, 5, 0, [[0, 0, 0, 0, 0], [0, 0, 0, 0, 0]], [6, 0], [10, 4], 1, 3, 84, False),
+                     (5, 4, 1, [[0, 1, 0, 1, 0], [1, 0, 1, 0, 1]], [3], [8], 2, 2, 85, True)]
+
+
+def block_ints(n, iseed, orbsym, symmetric):
+    from forte2_gb300.synthetic import symmetrize_integrals
+
+    ints = make_integrals(n, iseed)
+    return symmetrize_integrals(ints, [x for g in orbsym for x in g]) if symmetric else ints
+
+
+def gen_blocks(out, ref_root):
+    """Blocked spaces: the reference's class strings, blocks, sigma of a seeded vector,
+    determinant energies, CSF couplings and CSF diagonal; CASCI energies from the reference's
+    Davidson on its compiled blocked sigma."""
+    data = {}
+    meta = {"cases": [], "casci": {}}
+    for k, (na, nb, sym, orbsym, gmin, gmax, iseed, cseed, symm) in enumerate(BLOCK_CASES):
+        n = sum(len(g) for g in orbsym)
+        s = ref.RefCIStrings(na, nb, sym, orbsym, gmin, gmax)
+        key = f"b{k}"
+        meta["cases"].append(dict(key=key, na=na, nb=nb, symmetry=sym, orbital_symmetry=orbsym, gas_min=gmin,
+                                  gas_max=gmax, iseed=iseed, cseed=cseed, symmetric=symm, ndet=s.ndet,
+                                  nas=s.nas, nbs=s.nbs, nirrep=s.nirrep))
+        for spin, tag in ((0, "a"), (1, "b")):
+            m, c = s.strings(spin)
+            data[f"{key}_{tag}_strings"] = m
+            data[f"{key}_{tag}_classes"] = c
+        data[f"{key}_blocks"] = s.blocks()
+        data[f"{key}_dets"] = s.determinants()
+        if s.ndet == 0:
+            continue
+        ints = block_ints(n, iseed, orbsym, symm)
+        sb = ref.RefSigmaBuilder(s, ints.E, ints.H, ints.V)
+        sb.set_algorithm("hz")
+        c = random_ci_vector(s.ndet, cseed)
+        sig = np.zeros(s.ndet)
+        sb.Hamiltonian(c, sig)
+        data[f"{key}_sigma"] = sig
+        data[f"{key}_det_energies"] = sb.det_energies()
+        twice_ms = na - nb
+        for twoS in (abs(twice_ms), abs(twice_ms) + 2):
+            sa = ref.RefSpinAdapter(twoS, twice_ms, n)
+            sa.prepare_couplings(s)
+            if sa.ncsf == 0:
+                continue
+            bounds, det_idx, coeff, ranges = sa.couplings()
+            tag = f"{key}_S{twoS}"
+            data[f"{tag}_bounds"] = bounds
+            data[f"{tag}_det_idx"] = det_idx
+            data[f"{tag}_coeff"] = coeff
+            data[f"{tag}_ranges"] = ranges
+            data[f"{tag}_hdiag"] = sb.form_Hdiag_csf(sa)
+        print("blocks", key, s.ndet, flush=True)
+    np.savez_compressed(os.path.join(out, "blocks.npz"), **data)
+    DL, Params = load_davidson(ref_root)
+    for k, (na, nb, sym, orbsym, gmin, gmax, mult, nroot, iseed, symm) in enumerate(BLOCK_CASCI_CASES):
+        n = sum(len(g) for g in orbsym)
+        ints = block_ints(n, iseed, orbsym, symm)
+        r = reference_casci(na, nb, n, mult, na - nb, nroot, iseed, 1e-12, DL, Params, 400, ints=ints,
+                            space=(sym, orbsym, gmin, gmax))
+        r.update(dict(na=na, nb=nb, symmetry=sym, orbital_symmetry=orbsym, gas_min=gmin, gas_max=gmax,
+                      multiplicity=mult, nroot=nroot, iseed=iseed, symmetric=symm))
+        meta["casci"][f"c{k}"] = r
+        print("blocks casci", k, r["evals"], r["iterations"], r["max_dev_vs_lanczos"], flush=True)
+    with open(os.path.join(out, "blocks.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
 # MCSCF-style sequence: (na, nb, norb, multiplicity, nroot, integral seed, rotation seeds, theta, e_tol)
 MCSCF_CASES = [(4, 4, 8, 1, 2, 4100, (4111, 4122), 0.05, 1e-10),
                (5, 5, 10, 1, 1, 4200, (4211, 4222), 0.03, 1e-10),
@@ -369,7 +459,7 @@ def main():
     steps = {"lists": lambda: gen_lists(HERE), "sigma": lambda: gen_sigma(HERE),
              "checksums": lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_CASES, "sigma_checksums.json"),
              "davidson": lambda: gen_davidson(HERE, a.reference), "rdm": lambda: gen_rdm(HERE),
-             "mcscf": lambda: gen_mcscf(HERE, a.reference),
+             "mcscf": lambda: gen_mcscf(HERE, a.reference), "blocks": lambda: gen_blocks(HERE, a.reference),
              "rdm3": lambda: gen_rdm3(HERE)}
     if a.big:
         steps["big"] = lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_BIG, "sigma_checksums_16.json")

@@ -59,10 +59,8 @@ def test_cistrings_input_validation():
         CIStrings(1, -1, 0, [[]], [], [])
     with pytest.raises(TypeError):
         CIStrings(1, 1, 0, [0], [], [])
-    with pytest.raises(NotImplementedError):
-        CIStrings(2, 2, 0, [[0, 0], [0, 0]], [0, 0], [4, 4])
-    with pytest.raises(NotImplementedError):
-        CIStrings(2, 2, 1, [[0, 1, 0, 1]], [], [])
+    with pytest.raises(ValueError):
+        CIStrings(1, 1, 0, [[0, 0]], [0, 0], [])
 
 
 def test_params_validation():
