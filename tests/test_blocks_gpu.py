@@ -91,7 +91,7 @@ def test_blocked_sigma_matches_reference(cuda, gold, case):
     sb.Hamiltonian(c, s32)
     assert np.linalg.norm(s32 - ref) / np.linalg.norm(ref) < 2e-6
     sb.set_precision("fp64")
-    e = sb.det_energies()
+    e = sb.det_energies().cpu().numpy()
     assert np.abs(e - gold[f"{k}_det_energies"]).max() < 1e-12 * max(1.0, np.abs(e).max())
 
 
