@@ -153,6 +153,7 @@ __device__ void jacobi_block(int m, const double* __restrict__ G, int ldg, doubl
     __shared__ int rp[MAXM / 2], rq[MAXM / 2];
     __shared__ double red[2][32];
     __shared__ int order[MAXM];
+    __shared__ int rotated; // a rotation was applied in this sweep
     const int t = threadIdx.x, nt = blockDim.x;
     const int M = m + (m & 1), npair = M / 2;
     // Hermitize on load: A = (G + G^T) / 2 (davidsonliu.py:258)
@@ -188,6 +189,9 @@ __device__ void jacobi_block(int m, const double* __restrict__ G, int ldg, doubl
         __syncthreads();
         if (offsum <= 1e-32 * totsum || offsum == 0.0)
             break;
+        if (t == 0)
+            rotated = 0;
+        __syncthreads();
         for (int step = 0; step < M - 1; ++step) {
             if (t < npair) {
                 // players 0..M-1: 0 stays, 1..M-1 rotate; pair t is (r(t), r(M-1-t))
@@ -197,7 +201,10 @@ __device__ void jacobi_block(int m, const double* __restrict__ G, int ldg, doubl
                 double c = 1.0, sn = 0.0;
                 if (q < m) {
                     const double apq = A[p][q];
-                    if (apq != 0.0) {
+                    // an element below 1e-17 of both diagonal elements moves no eigenvalue or
+                    // vector at FP64 precision: left, so that the sweeps end when none is left
+                    if (apq != 0.0 && !(fabs(apq) <= 1e-17 * fmax(fabs(A[p][p]), fabs(A[q][q])))) {
+                        rotated = 1;
                         const double tau = (A[q][q] - A[p][p]) / (2.0 * apq);
                         const double tt = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
                         c = 1.0 / sqrt(1.0 + tt * tt);
@@ -238,6 +245,8 @@ __device__ void jacobi_block(int m, const double* __restrict__ G, int ldg, doubl
             }
             __syncthreads();
         }
+        if (!rotated)
+            break; // every off-diagonal element is negligible
     }
     // ascending order by rank (ties by index), then gather
     for (int i = t; i < m; i += nt) {
@@ -543,6 +552,7 @@ __global__ void k_dg_reset(DGState* st, DGReset r) {
     st->collapse = 0;
     st->added = 0;
     st->m_eig = 0;
+    st->g_size = 0;
     st->maxiter = r.maxiter;
     st->stall_window = r.stall_window;
     st->e_tol = r.e_tol;
@@ -637,12 +647,14 @@ __global__ void __launch_bounds__(256) k_dg_dots(const DGState* st, int which, c
         return;
     const int i = blockIdx.x / nj, j = blockIdx.x % nj;
     int li = ni, lj = nj;
-    if (which == 0 || which == 1)
+    if (which == 0 || which == 1 || which == 5)
         li = lj = st->m;
     else if (which == 3)
         li = st->m;
     if (i >= li || j >= lj)
         return;
+    if (which == 5 && i < st->g_size && j < st->g_size)
+        return; // still current
     const double* a = A + (int64_t)i * lda;
     const double* bb = B + (int64_t)j * ldb;
     double acc = 0.0;
@@ -667,10 +679,37 @@ __global__ void __launch_bounds__(256) k_dg_dots(const DGState* st, int which, c
 __device__ __forceinline__ void dg_pair_limits(const DGState* st, int which, int ni, int nj, int& li, int& lj) {
     li = ni;
     lj = nj;
-    if (which == 0 || which == 1)
+    if (which == 0 || which == 1 || which == 5)
         li = lj = st->m;
     else if (which == 3)
         li = st->m;
+}
+
+// Pairs of a launch: all li x lj, or for which == 5 (the subspace matrix after new sigma rows)
+// only those outside the g x g block that is still current: rows i < g with j >= g, then every
+// pair of the rows i >= g. Each pair's sum does not depend on which other pairs a launch holds,
+// so the matrix is bitwise the one a full computation gives.
+__device__ __forceinline__ int dg_pair_count(const DGState* st, int which, int li, int lj) {
+    if (which != 5)
+        return li * lj;
+    const int g = min(st->g_size, li);
+    return li * lj - g * g;
+}
+__device__ __forceinline__ void dg_pair(const DGState* st, int which, int pr, int li, int lj, int& i, int& j) {
+    if (which != 5) {
+        i = pr / lj;
+        j = pr % lj;
+        return;
+    }
+    const int g = min(st->g_size, li), w = lj - g;
+    if (pr < g * w) {
+        i = pr / w;
+        j = g + pr % w;
+    } else {
+        pr -= g * w;
+        i = g + pr / lj;
+        j = pr % lj;
+    }
 }
 
 __global__ void __launch_bounds__(256) k_dg_dots_partial(const DGState* st, int which, const double* __restrict__ A,
@@ -682,20 +721,28 @@ __global__ void __launch_bounds__(256) k_dg_dots_partial(const DGState* st, int 
         return;
     int li, lj;
     dg_pair_limits(st, which, ni, nj, li, lj);
-    const int np = li * lj;
+    const int np = dg_pair_count(st, which, li, lj);
     const int64_t e0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, step = (int64_t)gridDim.x * blockDim.x;
     __shared__ double red[8][8];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int p0 = 0; p0 < np; p0 += 8) {
         double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         const int cnt = min(8, np - p0);
+        const double* ap[8];
+        const double* bp[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            int i = 0, j = 0;
+            if (q < cnt)
+                dg_pair(st, which, p0 + q, li, lj, i, j);
+            ap[q] = A + (int64_t)i * lda;
+            bp[q] = B + (int64_t)j * ldb;
+        }
         for (int64_t e = e0; e < n; e += step)
 #pragma unroll
             for (int q = 0; q < 8; ++q)
-                if (q < cnt) {
-                    const int pr = p0 + q, i = pr / lj, j = pr % lj;
-                    a[q] += A[(int64_t)i * lda + e] * B[(int64_t)j * ldb + e];
-                }
+                if (q < cnt)
+                    a[q] += ap[q][e] * bp[q][e];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             double x = a[q];
@@ -725,12 +772,14 @@ __global__ void k_dg_dots_reduce(const DGState* st, int which, int ni, int nj, i
     int li, lj;
     dg_pair_limits(st, which, ni, nj, li, lj);
     const int pr = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pr >= li * lj)
+    if (pr >= dg_pair_count(st, which, li, lj))
         return;
     double t = 0.0;
     for (int bk = 0; bk < nblocks; ++bk)
         t += partial[(int64_t)bk * 4096 + pr];
-    out[(pr / lj) * ldo + pr % lj] = t;
+    int i, j;
+    dg_pair(st, which, pr, li, lj, i, j);
+    out[i * ldo + j] = t;
 }
 
 void dg_dots_long(const DGState* st, int which, const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n,
@@ -779,6 +828,7 @@ __global__ void k_dg_eigh(DGState* st, const double* G, int ldg, double* evals, 
     if (threadIdx.x == 0) {
         st->m_eig = m;
         st->sigma_size = m;
+        st->g_size = m;
     }
 }
 
@@ -954,6 +1004,7 @@ __device__ void dg_orthocheck_body(DGState* st, const DGParams& P, const double*
             st->m = P.collapse_k;
             st->sigma_size = P.collapse_k;
             st->collapse = 0;
+            st->g_size = 0; // a new basis: the next subspace matrix is computed in full
         }
     }
     __syncthreads();
@@ -1331,6 +1382,7 @@ __global__ void __launch_bounds__(256) k_dg_small_iter(DGState* st, DGParams P, 
     if (threadIdx.x == 0) {
         st->m_eig = m;
         st->sigma_size = m;
+        st->g_size = m;
     }
     dg_residual_body(st, P, b, sigma, ld, V, P.maxm, evals, hdiag, r, ldr, norms2);
     if (threadIdx.x == 0) {

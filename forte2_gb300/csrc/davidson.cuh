@@ -29,7 +29,7 @@ struct DGState {
     int32_t m_eig;      // basis size of the last subspace eigenproblem
     int32_t maxiter;    // iteration limit of this solve
     int32_t stall_window;
-    int32_t pad;
+    int32_t g_size;     // leading rows and columns of the subspace matrix still current (0 after a collapse)
     double e_tol, r_tol, stall_floor;
     double max_de, max_r;
     double ortho_dev;   // largest |S - I| of the starting basis (checked at reset when S is given)

@@ -182,7 +182,7 @@ struct DavGraph {
             return;
         }
         dg_unstage(S, stage_s.get(), R, n, sigma, ld, s);
-        dots(0, b, ld, sigma, ld, mm, mm, G.get(), mm);
+        dots(5, b, ld, sigma, ld, mm, mm, G.get(), mm); // the pairs with a new basis or sigma row
         dg_eigh(S, G.get(), mm, evals.get(), V.get(), mm, s);
         dg_residual(S, P, b, sigma, ld, V.get(), mm, evals.get(), hdiag, r, ldr, norms2.get(), partial.get(), s);
         dg_check(S, P, norms2.get(), evals.get(), hist.get(), s);
