@@ -446,9 +446,21 @@ class CASCISolver:
     def make_sf_2cumulant(self, left_root: int, right_root: int | None = None):
         return self._rdm(("sf_2cumulant",), left_root, right_root)
 
+    def make_sd_3rdm(self, left_root: int, right_root: int | None = None):
+        """Spin-dependent 3-RDMs (aaa, aab, abb, bbb) between two roots (ci.py:627-653)."""
+        return self._rdm(("aaa_3rdm", "aab_3rdm", "abb_3rdm", "bbb_3rdm"), left_root, right_root)
+
+    def make_sf_3rdm(self, left_root: int, right_root: int | None = None):
+        return self._rdm(("sf_3rdm",), left_root, right_root)
+
+    def make_sf_3cumulant(self, left_root: int, right_root: int | None = None):
+        return self._rdm(("sf_3cumulant",), left_root, right_root)
+
     make_1rdm = make_sf_1rdm
     make_2rdm = make_sf_2rdm
     make_2cumulant = make_sf_2cumulant
+    make_3rdm = make_sf_3rdm
+    make_3cumulant = make_sf_3cumulant
 
     def rdm_energies(self, root):
         """The root's energy from its RDMs in the three forms the reference checks (ci.py:323-403):

@@ -488,7 +488,16 @@ class CISigmaBuilder:
     # ---- reduced density matrices (ci_sigma_builder_1rdm.cc:9-84, ci_sigma_builder_2rdm.cc:46-282)
 
     _RDM_KINDS = {"a_1rdm": 0, "b_1rdm": 1, "sf_1rdm": 2, "aa_2rdm": 3, "bb_2rdm": 4, "ab_2rdm": 5,
-                  "sf_2rdm": 6, "sf_2cumulant": 7}
+                  "sf_2rdm": 6, "sf_2cumulant": 7, "aaa_3rdm": 8, "bbb_3rdm": 9, "aab_3rdm": 10, "abb_3rdm": 11,
+                  "sf_3rdm": 12, "sf_3cumulant": 13}
+
+    @staticmethod
+    def _rdm_shape(k, n):
+        npair = n * (n - 1) // 2
+        ntrip = n * (n - 1) * (n - 2) // 6
+        return {0: (n, n), 1: (n, n), 2: (n, n), 3: (npair, npair), 4: (npair, npair), 8: (ntrip, ntrip),
+                9: (ntrip, ntrip), 10: (npair, n, npair, n), 11: (n, npair, n, npair), 12: (n,) * 6,
+                13: (n,) * 6}.get(k, (n, n, n, n))
 
     def _rdm(self, kind, C_left, C_right):
         """RDM `kind` between the bra C_left and the ket C_right. numpy vectors give a numpy array
@@ -497,8 +506,7 @@ class CISigmaBuilder:
         torch = _torch()
         n = self.lists.norb
         k = self._RDM_KINDS[kind]
-        npair = n * (n - 1) // 2
-        shape = (n, n) if k <= 2 else (npair, npair) if k <= 4 else (n, n, n, n)
+        shape = self._rdm_shape(k, n)
         size = int(lib().f2g_rdm_size(n, k))
         device = _is_cuda_tensor(C_left)
         if device:
@@ -542,6 +550,29 @@ class CISigmaBuilder:
 
     def sf_2cumulant(self, C_left, C_right):
         return self._rdm("sf_2cumulant", C_left, C_right)
+
+    # three-body RDMs (ci_sigma_builder_3rdm.cc:84-541)
+    def aaa_3rdm(self, C_left, C_right):
+        """Packed alpha 3-RDM [pqr][stu], p > q > r, s > t > u (triplet index
+        p(p-1)(p-2)/6 + q(q-1)/2 + r)."""
+        return self._rdm("aaa_3rdm", C_left, C_right)
+
+    def bbb_3rdm(self, C_left, C_right):
+        return self._rdm("bbb_3rdm", C_left, C_right)
+
+    def aab_3rdm(self, C_left, C_right):
+        """[pq][r][st][u]: alpha pairs pq, st (p > q, s > t), beta r, u."""
+        return self._rdm("aab_3rdm", C_left, C_right)
+
+    def abb_3rdm(self, C_left, C_right):
+        """[p][qr][s][tu]: alpha p, s; beta pairs qr, tu (q > r, t > u)."""
+        return self._rdm("abb_3rdm", C_left, C_right)
+
+    def sf_3rdm(self, C_left, C_right):
+        return self._rdm("sf_3rdm", C_left, C_right)
+
+    def sf_3cumulant(self, C_left, C_right):
+        return self._rdm("sf_3cumulant", C_left, C_right)
 
     # transition 1-RDMs between two wave functions (ci_sigma_builder_1trdm.cc:10-131): both must
     # have the same orbitals and electron counts; in a CAS space they then share one determinant

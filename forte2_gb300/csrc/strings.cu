@@ -78,14 +78,47 @@ __global__ void k_up2(int n, int k, int64_t N2, int m2, const uint64_t* binom, u
     }
 }
 
+// 3-hole list of each (k-3)-electron string K: entries (sign, p, q, r, I), p > q > r,
+// I = K + p + q + r, sign = <K|a_p a_q a_r|I> (r removed first, then q, then p;
+// ci_strings_makers.cc:276-321); ascending r, then q, then p.
+__global__ void k_up3(int n, int k, int64_t N3, int m3, const uint64_t* binom, uint64_t* out) {
+    const int64_t K = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (K >= N3)
+        return;
+    const uint64_t mK = string_unrank((uint64_t)K, n, k - 3, binom);
+    int j = 0;
+    for (int r = 0; r < n; ++r) {
+        if (mK >> r & 1)
+            continue;
+        for (int q = r + 1; q < n; ++q) {
+            if (mK >> q & 1)
+                continue;
+            for (int p = q + 1; p < n; ++p) {
+                if (mK >> p & 1)
+                    continue;
+                const uint64_t mI = mK | (uint64_t(1) << p) | (uint64_t(1) << q) | (uint64_t(1) << r);
+                const uint64_t I = string_rank(mI, n, k, binom);
+                const uint64_t mr = mI & ~(uint64_t(1) << r), mq = mr & ~(uint64_t(1) << q);
+                const int neg = parity_below(mI, r) ^ parity_below(mr, q) ^ parity_below(mq, p);
+                if (j < m3)
+                    out[K * m3 + j] = I | (uint64_t(p) << 32) | (uint64_t(q) << 40) | (uint64_t(r) << 48) |
+                                      (uint64_t(neg) << 56);
+                ++j;
+            }
+        }
+    }
+}
+
 void SpinStrings::build(int norb, int nel, const uint64_t* d_binom, cudaStream_t st) {
     n = norb;
     k = nel;
     N0 = (int64_t)host_binom(n, k);
     N1 = k >= 1 ? (int64_t)host_binom(n, k - 1) : 0;
     N2 = k >= 2 ? (int64_t)host_binom(n, k - 2) : 0;
+    N3 = k >= 3 ? (int64_t)host_binom(n, k - 3) : 0;
     m1 = n - k + 1;
     m2 = (int)host_binom(n - k + 2, 2);
+    m3 = (int)host_binom(n - k + 3, 3);
     if (N0 > (int64_t)kAddrMask)
         throw Error(1, "CIStrings: too many strings for 24-bit string addresses");
     const int T = 256;
@@ -101,6 +134,14 @@ void SpinStrings::build(int norb, int nel, const uint64_t* d_binom, cudaStream_t
         k_down1<<<ceil_div(N0, T), T, 0, st>>>(n, k, N0, d_binom, down1.get());
         F2G_LAUNCH("k_down1");
     }
+}
+
+void SpinStrings::build_up3(const uint64_t* d_binom, cudaStream_t st) {
+    if (!N3 || up3.get())
+        return;
+    up3.reserve(N3 * m3);
+    k_up3<<<ceil_div(N3, 256), 256, 0, st>>>(n, k, N3, m3, d_binom, up3.get());
+    F2G_LAUNCH("k_up3");
 }
 
 void SpinStrings::build_up2(const uint64_t* d_binom, cudaStream_t st) {

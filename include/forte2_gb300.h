@@ -133,7 +133,14 @@ int f2g_sigma_det_energies(void* sigma, double* dev_out, void* stream);
  *   p(p-1)/2 + q, element <L|a+_p a+_q a_s a_r|R> of one spin;
  * 5 ab_2rdm: norb^4, [u][v][x][y] = <L|a+_u(alpha) a+_v(beta) a_y(beta) a_x(alpha)|R>;
  * 6 sf_2rdm: norb^4, ab[p][q][r][s] + ab[q][p][s][r] + the antisymmetric expansion of aa + bb;
- * 7 sf_2cumulant: norb^4, sf_2rdm[p][q][r][s] - G1[p][r] G1[q][s] + G1[p][s] G1[q][r] / 2. */
+ * 7 sf_2cumulant: norb^4, sf_2rdm[p][q][r][s] - G1[p][r] G1[q][s] + G1[p][s] G1[q][r] / 2;
+ * three-body kinds (CISigmaBuilder::compute_*_3rdm, ci_sigma_builder_3rdm.cc:84-541; bound as
+ * aaa_3rdm ... sf_3cumulant, api/ci_helpers_api.cc:115-139):
+ * 8 aaa_3rdm, 9 bbb_3rdm: T^2 with T = norb(norb-1)(norb-2)/6, [pqr][stu] for p > q > r, s > t > u,
+ *   triplet index p(p-1)(p-2)/6 + q(q-1)/2 + r;
+ * 10 aab_3rdm: (P, norb, P, norb) as [pq][r][st][u] (alpha pairs p > q, s > t; beta r, u);
+ * 11 abb_3rdm: (norb, P, norb, P) as [p][qr][s][tu] (alpha p, s; beta pairs q > r, t > u);
+ * 12 sf_3rdm: norb^6; 13 sf_3cumulant: norb^6. The aab/abb kinds need norb <= 23. */
 int64_t f2g_rdm_size(int norb, int kind);
 /* RDM `kind` between the bra dev_C_left and the ket dev_C_right (device FP64, ndet each; the
  * same pointer for both selects the symmetric kernels) into dev_out (f2g_rdm_size doubles,

@@ -134,7 +134,10 @@ def test_pair_list_validation(lib):
     assert lib.f2g_rdm_pair_list(-1, 0, 0, None, None, counts.ctypes.data) == 2
     assert lib.f2g_rdm_pair_list(4, 2, 0, None, None, None) == 2
     assert lib.f2g_rdm_size(6, 0) == 36 and lib.f2g_rdm_size(6, 3) == 225 and lib.f2g_rdm_size(6, 7) == 6 ** 4
-    assert lib.f2g_rdm_size(1, 3) == 0 and lib.f2g_rdm_size(6, 8) == -1
+    assert lib.f2g_rdm_size(1, 3) == 0 and lib.f2g_rdm_size(6, 14) == -1
+    # three-body kinds: (T, T), (P, n, P, n), n^6
+    assert lib.f2g_rdm_size(6, 8) == 20 * 20 and lib.f2g_rdm_size(6, 10) == (15 * 6) ** 2
+    assert lib.f2g_rdm_size(6, 12) == 6 ** 6 and lib.f2g_rdm_size(2, 9) == 0
 
 
 def replay_hole_gram(rows_of_K, ncol, CL, CR, d):
