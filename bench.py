@@ -647,6 +647,25 @@ def run_rdm(a):
            "clocks": clk,
            # per set: k_rdm_hole<1> x2, k_transpose x2, k_rdm_ab, its mirror, k_rdm_hole<2> x2, k_rdm_sf2
            "gpu_launches": 9 * a.steps}
+    # three-body RDMs (make_sf_3rdm / make_sf_3cumulant) at CAS(14e,14o): one warm call, one timed
+    n3 = min(n, 14)
+    na3, nb3, _, _, ndet3 = cas_dims(n3, n3, 0)
+    s3 = CIStrings(na3, nb3, 0, [[0] * n3], [], [])
+    ints3 = make_integrals(n3, 1000 + n3)
+    sb3 = CISigmaBuilder(s3, ints3.E, ints3.H, ints3.V, 0)
+    c3 = torch.from_numpy(random_ci_vector(ndet3, CSEED)).cuda()
+    sb3.sf_3rdm(c3, c3)
+    three = {}
+    for kind in ("aab_3rdm", "aaa_3rdm", "sf_3rdm", "sf_3cumulant"):
+        x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        x0.record(st)
+        getattr(sb3, kind)(c3, c3)
+        x1.record(st)
+        torch.cuda.synchronize()
+        three[kind + "_ms"] = x0.elapsed_time(x1)
+    out["three_body"] = {"workload": f"CAS({n3}e,{n3}o), one seeded vector (bra = ket), {ndet3} determinants",
+                         **three}
+    del sb3, s3
     if not a.no_cpu_baseline:
         v, sample, cores = rdm_cpu_baseline(n, na, nb, c_host, a.cpu_seconds)
         out["cpu_baseline"] = {"value": v, "unit": "RDM sets/s", "cores": cores, "kind": "port", "sample": sample}

@@ -308,9 +308,15 @@ __global__ void __launch_bounds__(128) k_spmm_group(int64_t nrows, int ncols, co
             }
 #pragma unroll
             for (int q = 0; q < kSsUnroll; ++q) {
-                const float4 wa = reinterpret_cast<const float4*>(sval)[(u + q) * 2];
-                const float4 wb = reinterpret_cast<const float4*>(sval)[(u + q) * 2 + 1];
-                const float w[kSsGroup] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+                float w[kSsGroup];
+#pragma unroll
+                for (int h = 0; h < kSsGroup / 4; ++h) {
+                    const float4 t = reinterpret_cast<const float4*>(sval)[(u + q) * (kSsGroup / 4) + h];
+                    w[4 * h] = t.x;
+                    w[4 * h + 1] = t.y;
+                    w[4 * h + 2] = t.z;
+                    w[4 * h + 3] = t.w;
+                }
 #pragma unroll
                 for (int j = 0; j < kSsGroup; ++j)
 #pragma unroll
