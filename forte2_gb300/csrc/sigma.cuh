@@ -30,7 +30,7 @@ struct StringHamiltonian {
     DevBuf<float> gval;
 };
 
-constexpr int kSsGroup = 16;           // rows per group of the grouped FP32 same-spin kernel
+constexpr int kSsGroup = 8;            // rows per group of the grouped FP32 same-spin kernel
 constexpr int64_t kSsGroupMinRows = 2048; // strings per spin from which the FP32 build uses groups
 constexpr int kSsGroupMaxSort = 16384; // kSsGroup * entries per row must fit one block's sort
 
