@@ -428,7 +428,8 @@ class CISigmaBuilder:
         check(lib().f2g_sigma_set_tensor_cores(self.h, int(bool(on)), avail.ctypes.data))
         return bool(avail[0])
 
-    _VARIANTS = {"tensor_cores": 0, "narrow_same_spin": 1, "persistent_opposite": 2, "tc_wait_limit": 3}
+    _VARIANTS = {"tensor_cores": 0, "narrow_same_spin": 1, "persistent_opposite": 2, "tc_wait_limit": 3,
+                 "irrep_blocks": 4}
 
     def set_variant(self, name, value):
         """Select a kernel variant with identical results (see forte2_gb300.autotune)."""

@@ -291,6 +291,39 @@ void DetBlocks::set_c1(int na, int nb, int64_t N0a, int64_t N0b) {
     F2G_CUDA(cudaMemcpy(dblk.get(), one, sizeof(one), cudaMemcpyHostToDevice));
 }
 
+void DetBlocks::build_filter(int64_t N0a, int64_t N0b) {
+    const int nc[2] = {nclass(0), nclass(1)};
+    // allowed (alpha class, beta class) pairs: the non-empty blocks
+    std::vector<uint8_t> allowed((size_t)nc[0] * nc[1], 0);
+    for (int b = 0; b < nblk(); ++b) {
+        const int64_t* r = hblk.data() + 6 * b;
+        if (r[2] > 0)
+            allowed[(size_t)r[0] * nc[1] + r[1]] = 1;
+    }
+    for (int spin = 0; spin < 2; ++spin) {
+        const int64_t N0 = spin == 0 ? N0a : N0b;
+        std::vector<int16_t> cls((size_t)N0, -1);
+        for (int c = 0; c < nc[spin]; ++c)
+            for (int64_t j = cls_off[spin][c]; j < cls_off[spin][c + 1]; ++j)
+                cls[rank[spin][j]] = (int16_t)c;
+        const int m = nc[spin], o = nc[1 - spin];
+        std::vector<uint8_t> compat((size_t)m * m, 0);
+        for (int c = 0; c < m; ++c)
+            for (int c2 = 0; c2 < m; ++c2)
+                for (int x = 0; x < o && !compat[(size_t)c * m + c2]; ++x) {
+                    const bool a1 = spin == 0 ? allowed[(size_t)c * o + x] : allowed[(size_t)x * m + c];
+                    const bool a2 = spin == 0 ? allowed[(size_t)c2 * o + x] : allowed[(size_t)x * m + c2];
+                    compat[(size_t)c * m + c2] = a1 && a2;
+                }
+        dcls[spin].reserve(std::max<int64_t>(1, N0));
+        dcompat[spin].reserve(std::max<size_t>(1, compat.size()));
+        if (N0)
+            F2G_CUDA(cudaMemcpy(dcls[spin].get(), cls.data(), (size_t)N0 * sizeof(int16_t), cudaMemcpyHostToDevice));
+        if (!compat.empty())
+            F2G_CUDA(cudaMemcpy(dcompat[spin].get(), compat.data(), compat.size(), cudaMemcpyHostToDevice));
+    }
+}
+
 DetEnum DetBlocks::view(int64_t N0b_c1) const {
     DetEnum d;
     d.ndet = ndet;

@@ -90,6 +90,13 @@ struct DetBlocks {
     // the C1 CAS space as one trivial block over the C1 strings (host metadata filled in when
     // build() did not run)
     void set_c1(int na, int nb, int64_t N0a, int64_t N0b);
+
+    // Same-spin filter of a blocked space, per spin: the class of every C1 string (-1: in no
+    // class) and compat[c][c'] = 1 when some class of the other spin pairs with both c and c' in a
+    // non-empty block. A same-spin coupling <J|H|I> can reach the space only if compat[cls J][cls I].
+    DevBuf<int16_t> dcls[2];
+    DevBuf<uint8_t> dcompat[2];
+    void build_filter(int64_t N0a, int64_t N0b);
 };
 
 // vectors of the space <-> C1-sized vectors (zero outside the space); nvec vectors back to back

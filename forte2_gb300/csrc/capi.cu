@@ -374,9 +374,11 @@ int f2g_sigma_set_variant(void* sb, int which, int value) {
                 throw Error(2, "tensor-core wait limit must be >= 0");
             b->tc_poll_limit = value;
             F2G_CUDA(cudaMemset(b->tc_err.get(), 0, sizeof(int)));
-        } else
+        } else if (which == 4)
+            b->use_sym = value != 0;
+        else
             throw Error(2, "variant must be 0 (tensor cores), 1 (narrow same-spin tiles), 2 (persistent opposite "
-                           "grid) or 3 (tensor-core wait limit)");
+                           "grid), 3 (tensor-core wait limit) or 4 (irrep-aware opposite-spin kernel)");
     });
 }
 

@@ -29,6 +29,7 @@
 #include <cstring>
 
 #include "sigma.cuh"
+#include "opposite_sym.cuh"
 
 namespace f2g {
 
@@ -560,6 +561,10 @@ SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const dou
             F2G_CUDA(cudaEventCreate(&e));
     tc_err.reserve(1);
     F2G_CUDA(cudaMemsetAsync(tc_err.get(), 0, sizeof(int), 0));
+    if (opposite_sym_supported(s)) {
+        osym = std::make_shared<OppositeSym>();
+        osym->build(s);
+    }
     if (opposite_tc_supported(s)) {
         build_beta_exc(s, beta_exc, 0); // ordered before set_hamiltonian's wait on the legacy stream
         tc_cmax.reserve(2 * 65536);      // one word per vector of a batch (grid y <= 65535), two sets
@@ -583,18 +588,86 @@ SigmaBuilder::~SigmaBuilder() {
                 cudaEventDestroy(e);
 }
 
+// Blocked spaces: the entries of each string-Hamiltonian row that can reach the space (the class
+// pair of row and column is compatible, see DetBlocks::build_filter), in list order, padded to
+// nnz_out with (J, 0) entries; count mode (ocol == nullptr) records the largest kept count.
+template <typename T>
+__global__ void k_filter_ss(int64_t N0, int nnz, const int32_t* __restrict__ col, const T* __restrict__ val,
+                            const int16_t* __restrict__ cls, const uint8_t* __restrict__ compat, int ncls,
+                            int nnz_out, int32_t* __restrict__ ocol, T* __restrict__ oval, int* maxcount) {
+    const int64_t J = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (J >= N0)
+        return;
+    const int cj = cls[J];
+    int cnt = 0;
+    if (cj >= 0) {
+        for (int k = 0; k < nnz; ++k) {
+            const int32_t I = col[J * nnz + k];
+            const int ci = cls[I];
+            if (ci < 0 || !compat[cj * ncls + ci])
+                continue;
+            if (ocol && cnt < nnz_out) {
+                ocol[J * nnz_out + cnt] = I;
+                oval[J * nnz_out + cnt] = val[J * nnz + k];
+            }
+            ++cnt;
+        }
+    }
+    if (maxcount)
+        atomicMax(maxcount, cnt);
+    if (ocol)
+        for (; cnt < nnz_out; ++cnt) {
+            ocol[J * nnz_out + cnt] = (int32_t)J;
+            oval[J * nnz_out + cnt] = T(0);
+        }
+}
+
 void SigmaBuilder::build_string_hamiltonian(int spin, StringHamiltonian& sh, bool with_e0, cudaStream_t st) {
     const SpinStrings& ss = s->spin(spin);
-    sh.nnz = ss_row_nnz(n, ss.k);
-    if (ss.N0 == 0 || sh.nnz == 0)
+    const int nnz_full = ss_row_nnz(n, ss.k);
+    sh.nnz = nnz_full;
+    if (ss.N0 == 0 || nnz_full == 0)
         return;
-    const size_t total = (size_t)ss.N0 * sh.nnz;
-    sh.col.reserve(total);
-    sh.val.reserve(total);
-    k_build_ss<double><<<ceil_div(ss.N0, 128), 128, 0, st>>>(n, ss.k, ss.N0, sh.nnz, ss.str.get(), s->binom.get(),
-                                                            dH.get(), dV.get(), with_e0 ? E : 0.0, 3,
-                                                            sh.col.get(), sh.val.get());
+    const size_t total = (size_t)ss.N0 * nnz_full;
+    if (!s->blocked()) {
+        sh.col.reserve(total);
+        sh.val.reserve(total);
+        k_build_ss<double><<<ceil_div(ss.N0, 128), 128, 0, st>>>(n, ss.k, ss.N0, nnz_full, ss.str.get(),
+                                                                s->binom.get(), dH.get(), dV.get(), with_e0 ? E : 0.0,
+                                                                3, sh.col.get(), sh.val.get());
+        F2G_LAUNCH("k_build_ss");
+        return;
+    }
+    // blocked space: full rows in stream-ordered scratch, then only the couplings the space can use
+    // (a symmetric space keeps about 1/nirrep of them); the layout depends on the strings alone
+    TmpBuf<int32_t> fc(total, st);
+    TmpBuf<double> fv(total, st);
+    k_build_ss<double><<<ceil_div(ss.N0, 128), 128, 0, st>>>(n, ss.k, ss.N0, nnz_full, ss.str.get(), s->binom.get(),
+                                                            dH.get(), dV.get(), with_e0 ? E : 0.0, 3, fc.get(),
+                                                            fv.get());
     F2G_LAUNCH("k_build_ss");
+    const DetBlocks& B = s->blocks;
+    if (ss_nnz_filtered[spin] < 0) {
+        TmpBuf<int> mx(1, st);
+        F2G_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(int), st));
+        k_filter_ss<double><<<ceil_div(ss.N0, 128), 128, 0, st>>>(ss.N0, nnz_full, fc.get(), fv.get(),
+                                                                 B.dcls[spin].get(), B.dcompat[spin].get(),
+                                                                 B.nclass(spin), 0, nullptr, nullptr, mx.get());
+        F2G_LAUNCH("k_filter_ss count");
+        int h = 0;
+        F2G_CUDA(cudaMemcpyAsync(&h, mx.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+        F2G_CUDA(cudaStreamSynchronize(st));
+        ss_nnz_filtered[spin] = std::max(1, h);
+    }
+    sh.nnz = ss_nnz_filtered[spin];
+    const size_t kept = (size_t)ss.N0 * sh.nnz;
+    sh.col.reserve(kept);
+    sh.val.reserve(kept);
+    k_filter_ss<double><<<ceil_div(ss.N0, 128), 128, 0, st>>>(ss.N0, nnz_full, fc.get(), fv.get(),
+                                                             B.dcls[spin].get(), B.dcompat[spin].get(),
+                                                             B.nclass(spin), sh.nnz, sh.col.get(), sh.val.get(),
+                                                             nullptr);
+    F2G_LAUNCH("k_filter_ss");
 }
 
 // FP32 copies of the string-Hamiltonian values, made once per set of integrals on first use.
@@ -981,6 +1054,12 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
                 unsigned int* cmax = tc_cmax.get() + (graph ? 65536 : 0);
                 launch_opposite_tc(s, beta_exc.get(), Vt, tc_vmax.get(), C, sig, cmax, tc_err.get(), tc_poll_limit,
                                    max_ctas, st, nvec);
+                done = true;
+            }
+        }
+        if constexpr (sizeof(T) == 8) {
+            if (!done && use_sym && osym) {
+                launch_opposite_sym(s, *osym, Vt, C, sig, st, nvec, g_opposite_max_ctas);
                 done = true;
             }
         }

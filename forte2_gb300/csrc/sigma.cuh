@@ -42,6 +42,7 @@ struct SigmaBuilder {
     DevBuf<double> dH, dV;
     DevBuf<float> fV;
     StringHamiltonian ha, hb;
+    int ss_nnz_filtered[2] = {-1, -1}; // blocked spaces: kept couplings per string-Hamiltonian row
     int algorithm = 0;       // 0 Knowles-Handy (the C++ default, ci_sigma_builder.h:288),
                              // 1 Harrison-Zarrabian (what the Python driver selects)
     size_t memory = size_t(1) << 30;
@@ -54,6 +55,10 @@ struct SigmaBuilder {
     // FP32 opposite-spin term on the tensor cores (split-FP16 products, opposite_tc.cu) when the
     // space allows it
     bool use_tc = true;
+    // FP64 opposite-spin term of a space blocked by irreps alone through the irrep-aware kernel
+    // (opposite_sym.cu); off: the C1 kernel on the embedding (same sigma up to rounding)
+    bool use_sym = true;
+    std::shared_ptr<struct OppositeSym> osym; // set when the space allows it
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
     DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
     DevBuf<unsigned int> tc_cmax; // per-vector largest |C| of a tensor-core launch (its operand scale)

@@ -169,6 +169,8 @@ CIStrings::CIStrings(int na_, int nb_, int symmetry, const std::vector<std::vect
     ndet = blocks.ndet;
     if (blocks.trivial)
         blocks.set_c1(na, nb, a.N0, b.N0); // the C1 strings themselves, one block
+    else
+        blocks.build_filter(a.N0, b.N0);
 }
 
 void CIStrings::build_c1() {
