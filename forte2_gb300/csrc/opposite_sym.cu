@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(kSymThreads, 1)
     double* row = vs + (size_t)n * ma * n;                      // [N0b]
     uint32_t* ua = reinterpret_cast<uint32_t*>(row + N0b);      // [ma]
     uint32_t* tbl = ua + ((ma + 3) & ~3);                       // [n][kSymThreads]: this thread's 1-hole entries by orbital
+    double* dsm = reinterpret_cast<double*>(tbl + (size_t)n * kSymThreads); // [RM][kSymThreads]: gathered values
     const int tid = threadIdx.x;
     C += blockIdx.y * N0a * N0b;
     sig += blockIdx.y * N0a * N0b;
@@ -97,17 +98,24 @@ __global__ void __launch_bounds__(kSymThreads, 1)
                     const uint32_t negq = (uint32_t)e_neg(eq);
                     const int tq = t ^ os.h[q];
                     const int ns = os.cnt[tq];
+                    // gathers into this thread's column of dsm, then exactly nr x ns multiply-adds
+                    // (warp-uniform trip counts: no predicated-off FP64 instruction)
                     for (int js = 0; js < ns; ++js) {
-                        const int s = os.list[tq][js];
-                        const uint32_t es = tbl[s * kSymThreads + tid];
+                        const uint32_t es = tbl[os.list[tq][js] * kSymThreads + tid];
                         double d = 0.0;
                         if (es != kNoEntry)
                             d = flip_sign(__ldg(crow + e_addr(es)), negq ^ (uint32_t)e_neg(es));
-                        const double* vq = vs + qi * n + s;
+                        dsm[js * kSymThreads + tid] = d;
+                    }
 #pragma unroll
-                        for (int j = 0; j < RM; ++j)
-                            if (j < nr)
-                                acc[j] += vq[os.list[u][j] * (ma * n)] * d;
+                    for (int j = 0; j < RM; ++j) {
+                        if (j < nr) {
+                            const double* vr = vs + ((size_t)os.list[u][j] * ma + qi) * n;
+                            double a = acc[j];
+                            for (int js = 0; js < ns; ++js)
+                                a += vr[os.list[tq][js]] * dsm[js * kSymThreads + tid];
+                            acc[j] = a;
+                        }
                     }
                 }
                 // owner-ordered writes, one phase per created orbital r
@@ -134,9 +142,12 @@ __global__ void __launch_bounds__(kSymThreads, 1)
     }
 }
 
-int64_t opposite_sym_smem(int n, int ma, int64_t N0b) {
-    return (int64_t)n * ma * n * 8 + N0b * 8 + (int64_t)((ma + 3) & ~3) * 4 + (int64_t)n * kSymThreads * 4;
+int64_t opposite_sym_smem(int n, int ma, int64_t N0b, int rm) {
+    return (int64_t)n * ma * n * 8 + N0b * 8 + (int64_t)((ma + 3) & ~3) * 4 + (int64_t)n * kSymThreads * 4 +
+           (int64_t)rm * kSymThreads * 8;
 }
+
+static int sym_rm(int maxper) { return maxper <= 2 ? 2 : maxper <= 4 ? 4 : maxper <= 8 ? 8 : 16; }
 
 bool opposite_sym_supported(const CIStrings* s) {
     const DetBlocks& B = s->blocks;
@@ -153,12 +164,12 @@ bool opposite_sym_supported(const CIStrings* s) {
             c += x == h;
         maxper = std::max(maxper, c);
     }
-    if (maxper > 32)
-        return false;
+    if (maxper > 16)
+        return false; // the per-irrep orbital loops are unrolled up to 16
     int optin = 0, dev = 0;
     F2G_CUDA(cudaGetDevice(&dev));
     F2G_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    return opposite_sym_smem(s->norb, s->a.m1, s->b.N0) <= optin;
+    return opposite_sym_smem(s->norb, s->a.m1, s->b.N0, sym_rm(maxper)) <= optin;
 }
 
 void OppositeSym::build(const CIStrings* s) {
@@ -215,7 +226,7 @@ template <int RM>
 static void launch_sym_rm(const CIStrings* s, const OppositeSym& t, const double* V, const double* C, double* sig,
                           cudaStream_t st, int nvec, int max_ctas) {
     const int n = s->norb, ma = s->a.m1, mb = s->b.m1;
-    const int64_t smem = opposite_sym_smem(n, ma, s->b.N0);
+    const int64_t smem = opposite_sym_smem(n, ma, s->b.N0, RM);
     F2G_CUDA(cudaFuncSetAttribute(k_opposite_sym<RM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int64_t gx = s->a.N0;
     if (max_ctas > 0)
@@ -232,14 +243,14 @@ void launch_opposite_sym(const CIStrings* s, const OppositeSym& t, const double*
         return;
     if (nvec > 65535)
         throw Error(2, "opposite-spin kernel: at most 65535 vectors per launch");
-    if (t.maxper <= 4)
+    if (t.maxper <= 2)
+        launch_sym_rm<2>(s, t, V, C, sig, st, nvec, max_ctas);
+    else if (t.maxper <= 4)
         launch_sym_rm<4>(s, t, V, C, sig, st, nvec, max_ctas);
     else if (t.maxper <= 8)
         launch_sym_rm<8>(s, t, V, C, sig, st, nvec, max_ctas);
-    else if (t.maxper <= 16)
-        launch_sym_rm<16>(s, t, V, C, sig, st, nvec, max_ctas);
     else
-        launch_sym_rm<32>(s, t, V, C, sig, st, nvec, max_ctas);
+        launch_sym_rm<16>(s, t, V, C, sig, st, nvec, max_ctas);
 }
 
 } // namespace f2g

@@ -29,7 +29,7 @@ struct OppositeSym {
 
 // The space is blocked by irreps only (no GAS restriction) and the kernel's shared memory fits.
 bool opposite_sym_supported(const CIStrings* s);
-int64_t opposite_sym_smem(int n, int ma, int64_t N0b);
+int64_t opposite_sym_smem(int n, int ma, int64_t N0b, int rm);
 // sigma += the opposite-spin term for nvec C1-embedded vectors back to back
 void launch_opposite_sym(const CIStrings* s, const OppositeSym& t, const double* V, const double* C, double* sig,
                          cudaStream_t st, int nvec, int max_ctas);
