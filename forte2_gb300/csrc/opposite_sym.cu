@@ -12,7 +12,9 @@
 // padded to whole warps), so t, u and the orbital loops are the same for every lane of a warp and
 // the FP64 pipe runs only the needed multiply-adds; a lane whose string occupies s gathers a zero.
 // Writes follow the C1 kernel's owner-ordered phases (one phase per created orbital r, a_r^+
-// one-to-one on the strings of a round): every sigma element is summed in a fixed order.
+// one-to-one on the strings of a round): every sigma element is summed in a fixed order. With few
+// multiply-adds left per gathered value the kernel is latency-bound, so the sigma row stays in
+// global memory (one CTA owns it) and three 256-thread CTAs share an SM.
 #include "opposite_sym.cuh"
 
 namespace f2g {
@@ -25,12 +27,13 @@ __device__ __forceinline__ double flip_sign(double x, uint32_t neg) {
 }
 
 constexpr uint32_t kNoEntry = 0xffffffffu;
-constexpr int kSymThreads = 512;
+constexpr int kSymThreads = 256;
+constexpr int kSymBlocksPerSM = 3;
 
 } // namespace
 
 template <int RM>
-__global__ void __launch_bounds__(kSymThreads, 1)
+__global__ void __launch_bounds__(kSymThreads, kSymBlocksPerSM)
     k_opposite_sym(int64_t N0a, int n, int na, int N0b, int64_t nkb, int ma, int mb, const uint32_t* __restrict__ down_a,
                    const uint32_t* __restrict__ up_a, const uint32_t* __restrict__ up_b,
                    const int32_t* __restrict__ kb_sorted, const int8_t* __restrict__ kb_h,
@@ -38,18 +41,16 @@ __global__ void __launch_bounds__(kSymThreads, 1)
                    const double* __restrict__ C, double* sig) {
     extern __shared__ unsigned char smem_raw[];
     double* vs = reinterpret_cast<double*>(smem_raw);          // [n][ma][n]: V[p, r, q_i, s]
-    double* row = vs + (size_t)n * ma * n;                      // [N0b]
-    uint32_t* ua = reinterpret_cast<uint32_t*>(row + N0b);      // [ma]
+    uint32_t* ua = reinterpret_cast<uint32_t*>(vs + (size_t)n * ma * n); // [ma]
     uint32_t* tbl = ua + ((ma + 3) & ~3);                       // [n][kSymThreads]: this thread's 1-hole entries by orbital
     double* dsm = reinterpret_cast<double*>(tbl + (size_t)n * kSymThreads); // [RM][kSymThreads]: gathered values
     const int tid = threadIdx.x;
     C += blockIdx.y * N0a * N0b;
     sig += blockIdx.y * N0a * N0b;
     for (int64_t Ja = blockIdx.x; Ja < N0a; Ja += gridDim.x) {
+        // the sigma row stays in global memory (L2): the owner-ordered phases give every element
+        // one writer per phase, so plain read-modify-writes are exact and ordered
         double* srow = sig + Ja * (int64_t)N0b;
-        __syncthreads(); // the previous row is written back
-        for (int c = tid; c < N0b; c += blockDim.x)
-            row[c] = srow[c];
         int hJa = 0;
         for (uint64_t m = astr[Ja]; m; m &= m - 1)
             hJa ^= os.h[__ffsll((long long)m) - 1];
@@ -130,20 +131,19 @@ __global__ void __launch_bounds__(kSymThreads, 1)
                             for (int j = 0; j < RM; ++j)
                                 if (j == jr)
                                     v = acc[j];
-                            atomicAdd(row + e_addr(er), flip_sign(v, negp ^ (uint32_t)e_neg(er)));
+                            double* dst = srow + e_addr(er);
+                            *dst += flip_sign(v, negp ^ (uint32_t)e_neg(er));
                         }
                     }
                 }
             }
         }
-        __syncthreads();
-        for (int c = tid; c < N0b; c += blockDim.x)
-            srow[c] = row[c];
     }
 }
 
 int64_t opposite_sym_smem(int n, int ma, int64_t N0b, int rm) {
-    return (int64_t)n * ma * n * 8 + N0b * 8 + (int64_t)((ma + 3) & ~3) * 4 + (int64_t)n * kSymThreads * 4 +
+    (void)N0b;
+    return (int64_t)n * ma * n * 8 + (int64_t)((ma + 3) & ~3) * 4 + (int64_t)n * kSymThreads * 4 +
            (int64_t)rm * kSymThreads * 8;
 }
 
