@@ -303,9 +303,12 @@ void DetBlocks::build_filter(int64_t N0a, int64_t N0b) {
     for (int spin = 0; spin < 2; ++spin) {
         const int64_t N0 = spin == 0 ? N0a : N0b;
         std::vector<int16_t> cls((size_t)N0, -1);
+        std::vector<int32_t> pos((size_t)N0, -1);
         for (int c = 0; c < nc[spin]; ++c)
-            for (int64_t j = cls_off[spin][c]; j < cls_off[spin][c + 1]; ++j)
+            for (int64_t j = cls_off[spin][c]; j < cls_off[spin][c + 1]; ++j) {
                 cls[rank[spin][j]] = (int16_t)c;
+                pos[rank[spin][j]] = (int32_t)(j - cls_off[spin][c]);
+            }
         const int m = nc[spin], o = nc[1 - spin];
         std::vector<uint8_t> compat((size_t)m * m, 0);
         for (int c = 0; c < m; ++c)
@@ -316,9 +319,12 @@ void DetBlocks::build_filter(int64_t N0a, int64_t N0b) {
                     compat[(size_t)c * m + c2] = a1 && a2;
                 }
         dcls[spin].reserve(std::max<int64_t>(1, N0));
+        dpos[spin].reserve(std::max<int64_t>(1, N0));
         dcompat[spin].reserve(std::max<size_t>(1, compat.size()));
-        if (N0)
+        if (N0) {
             F2G_CUDA(cudaMemcpy(dcls[spin].get(), cls.data(), (size_t)N0 * sizeof(int16_t), cudaMemcpyHostToDevice));
+            F2G_CUDA(cudaMemcpy(dpos[spin].get(), pos.data(), (size_t)N0 * sizeof(int32_t), cudaMemcpyHostToDevice));
+        }
         if (!compat.empty())
             F2G_CUDA(cudaMemcpy(dcompat[spin].get(), compat.data(), compat.size(), cudaMemcpyHostToDevice));
     }
@@ -349,12 +355,16 @@ __global__ void k_embed(DetEnum de, int64_t nfull, const T* __restrict__ sub, T*
 }
 
 template <typename T>
-__global__ void k_extract(DetEnum de, int64_t nfull, const T* __restrict__ full, T* __restrict__ sub) {
+__global__ void k_extract(DetEnum de, int64_t nfull, const T* __restrict__ full, T* __restrict__ sub, int add) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= de.ndet)
         return;
     const int64_t v = blockIdx.y;
-    sub[v * de.ndet + i] = full[v * nfull + de.c1(i)];
+    const T x = full[v * nfull + de.c1(i)];
+    if (add)
+        sub[v * de.ndet + i] += x;
+    else
+        sub[v * de.ndet + i] = x;
 }
 
 template <typename T>
@@ -371,18 +381,18 @@ void blocks_embed(const DetEnum& de, int64_t nfull, const T* sub, T* full, int n
 }
 
 template <typename T>
-void blocks_extract(const DetEnum& de, int64_t nfull, const T* full, T* sub, int nvec, cudaStream_t st) {
+void blocks_extract(const DetEnum& de, int64_t nfull, const T* full, T* sub, int nvec, cudaStream_t st, bool add) {
     if (nvec <= 0 || de.ndet == 0)
         return;
     if (nvec > 65535)
         throw Error(2, "blocks_extract: at most 65535 vectors per call");
-    k_extract<T><<<dim3((unsigned)ceil_div(de.ndet, 256), nvec), 256, 0, st>>>(de, nfull, full, sub);
+    k_extract<T><<<dim3((unsigned)ceil_div(de.ndet, 256), nvec), 256, 0, st>>>(de, nfull, full, sub, add ? 1 : 0);
     F2G_LAUNCH("k_extract");
 }
 
 template void blocks_embed<double>(const DetEnum&, int64_t, const double*, double*, int, cudaStream_t);
 template void blocks_embed<float>(const DetEnum&, int64_t, const float*, float*, int, cudaStream_t);
-template void blocks_extract<double>(const DetEnum&, int64_t, const double*, double*, int, cudaStream_t);
-template void blocks_extract<float>(const DetEnum&, int64_t, const float*, float*, int, cudaStream_t);
+template void blocks_extract<double>(const DetEnum&, int64_t, const double*, double*, int, cudaStream_t, bool);
+template void blocks_extract<float>(const DetEnum&, int64_t, const float*, float*, int, cudaStream_t, bool);
 
 } // namespace f2g

@@ -95,6 +95,7 @@ struct DetBlocks {
     // class) and compat[c][c'] = 1 when some class of the other spin pairs with both c and c' in a
     // non-empty block. A same-spin coupling <J|H|I> can reach the space only if compat[cls J][cls I].
     DevBuf<int16_t> dcls[2];
+    DevBuf<int32_t> dpos[2]; // position of every C1 string inside its class (-1: in no class)
     DevBuf<uint8_t> dcompat[2];
     void build_filter(int64_t N0a, int64_t N0b);
 };
@@ -103,6 +104,7 @@ struct DetBlocks {
 template <typename T>
 void blocks_embed(const DetEnum& de, int64_t nfull, const T* sub, T* full, int nvec, cudaStream_t st);
 template <typename T>
-void blocks_extract(const DetEnum& de, int64_t nfull, const T* full, T* sub, int nvec, cudaStream_t st);
+void blocks_extract(const DetEnum& de, int64_t nfull, const T* full, T* sub, int nvec, cudaStream_t st,
+                    bool add = false);
 
 } // namespace f2g

@@ -361,6 +361,43 @@ __global__ void k_transpose(int64_t rows, int64_t cols, const T* __restrict__ in
     }
 }
 
+// One block of a blocked space's vectors transposed: in (rows x cols, vector z at z * ldv) to
+// out (cols x rows, vector z at z * ldv_out), overwritten
+__global__ void k_transpose_blk(int64_t rows, int64_t cols, const double* __restrict__ in, int64_t ldv,
+                                double* __restrict__ out, int64_t ldv_out) {
+    __shared__ double tile[32][33];
+    in += blockIdx.z * ldv;
+    out += blockIdx.z * ldv_out;
+    const int64_t bx = (int64_t)blockIdx.x * 32, by = (int64_t)blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t r = by + j, c = bx + threadIdx.x;
+        if (r < rows && c < cols)
+            tile[j][threadIdx.x] = in[r * cols + c];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t c = bx + j, r = by + threadIdx.x;
+        if (r < rows && c < cols)
+            out[c * rows + r] = tile[threadIdx.x][j];
+    }
+}
+
+// Class-local string Hamiltonian of a space blocked by irreps: row j is the class string j (classes
+// back to back, the space's string order), its entries the filtered row of its C1 string with the
+// column turned into the position inside the class (a symmetric space keeps same-irrep couplings)
+__global__ void k_ss_local(int64_t nrows, int nnz, const uint32_t* __restrict__ rank, const int32_t* __restrict__ pos,
+                           const int32_t* __restrict__ col, const double* __restrict__ val, int32_t* __restrict__ lcol,
+                           double* __restrict__ lval) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nrows)
+        return;
+    const int64_t J = rank[j];
+    for (int k = 0; k < nnz; ++k) {
+        lcol[j * nnz + k] = pos[col[J * nnz + k]];
+        lval[j * nnz + k] = val[J * nnz + k];
+    }
+}
+
 template <typename TI, typename TO> __global__ void k_convert(int64_t n, const TI* in, TO* out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (TO)in[i];
@@ -670,6 +707,26 @@ void SigmaBuilder::build_string_hamiltonian(int spin, StringHamiltonian& sh, boo
     F2G_LAUNCH("k_filter_ss");
 }
 
+bool SigmaBuilder::blocked_sym_path() const { return osym && use_sym && precision == kFP64; }
+
+void SigmaBuilder::build_local_ss(cudaStream_t st) {
+    if (!osym)
+        return;
+    const DetBlocks& B = s->blocks;
+    for (int spin = 0; spin < 2; ++spin) {
+        const StringHamiltonian& sh = spin == 0 ? ha : hb;
+        const int64_t nrows = B.cls_off[spin].back();
+        if (nrows == 0 || sh.nnz == 0)
+            continue;
+        lcol[spin].reserve((size_t)nrows * sh.nnz);
+        lval[spin].reserve((size_t)nrows * sh.nnz);
+        k_ss_local<<<ceil_div(nrows, 128), 128, 0, st>>>(nrows, sh.nnz, B.drank[spin].get(), B.dpos[spin].get(),
+                                                         sh.col.get(), sh.val.get(), lcol[spin].get(),
+                                                         lval[spin].get());
+        F2G_LAUNCH("k_ss_local");
+    }
+}
+
 // FP32 copies of the string-Hamiltonian values, made once per set of integrals on first use.
 void SigmaBuilder::ensure_fp32() {
     if (fp32_ready)
@@ -744,6 +801,7 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
         opposite_tc_vmax(fV.get(), (int64_t)V.size(), tc_vmax.get(), 0);
     build_string_hamiltonian(0, ha, true, 0);
     build_string_hamiltonian(1, hb, false, 0);
+    build_local_ss(0);
     F2G_CUDA(cudaStreamSynchronize(0)); // set-up ran on the legacy stream: wait for it alone
     fp32_ready = false;
     if (precision == kFP32)
@@ -772,6 +830,7 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
         opposite_tc_vmax(fV.get(), (int64_t)V.size(), tc_vmax.get(), st);
     build_string_hamiltonian(0, ha, true, st);
     build_string_hamiltonian(1, hb, false, st);
+    build_local_ss(st);
     for (StringHamiltonian* sh : {&ha, &hb}) {
         const int s_ = sh == &ha ? 0 : 1;
         const size_t total = (size_t)s->spin(s_).N0 * sh->nnz;
@@ -857,6 +916,10 @@ void SigmaBuilder::apply_untimed(const double* C, double* sigma, cudaStream_t st
         throw Error(2, "apply_untimed: more vectors than prepared");
     if (precision == kFP32 && !fp32_ready)
         throw Error(1, "apply_untimed: FP32 Hamiltonian copies are not ready");
+    if (blocked_sym_path()) {
+        run_blocked_sym(C, sigma, st, nvec, false, true);
+        return;
+    }
     if (s->blocked()) {
         const DetEnum de = s->dets();
         blocks_embed<double>(de, s->nfull, C, gxC.get(), nvec, st);
@@ -1070,6 +1133,71 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
         F2G_CUDA(cudaEventRecord(cur_ev[3], st));
 }
 
+// Row SpMM on raw operands: Y[J] (+)= sum_k val[J][k] X[col[J][k]] for J < nrows, vectors at z * vstride.
+static void spmm_rows_raw(int64_t nrows, int ncols, int nnz, const int32_t* col, const double* val, const double* X,
+                          double* Y, bool accumulate, int64_t vstride, int nvec, cudaStream_t st) {
+    if (nrows == 0 || ncols == 0 || nnz == 0 || nvec <= 0)
+        return;
+    constexpr int VEC = 4;
+    const size_t smem = (size_t)nnz * (sizeof(double) + sizeof(int32_t));
+    if (smem > 48 * 1024)
+        F2G_CUDA(cudaFuncSetAttribute(k_spmm_rows<double, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)nrows, (unsigned)ceil_div(ncols, 128 * VEC), (unsigned)nvec);
+    k_spmm_rows<double, VEC><<<grid, 128, smem, st>>>(nrows, ncols, nnz, col, val, X, Y, accumulate ? 1 : 0, vstride);
+    F2G_LAUNCH("k_spmm_rows block");
+}
+
+// FP64 sigma of a space blocked by irreps alone on its own vectors (ndet elements each): the same-
+// spin terms block by block with the class-local string Hamiltonians (a block's rows only meet the
+// columns of its own beta class: the C1 path reads all of them), the opposite-spin term through
+// the irrep-aware kernel on the embedding. Event slots as in run(): beta, alpha, opposite spin.
+void SigmaBuilder::run_blocked_sym(const double* C, double* S, cudaStream_t st, int nvec, bool timed, bool graph) {
+    const DetBlocks& B = s->blocks;
+    const int64_t nd = s->ndet, nf = s->nfull;
+    double* xc = graph ? gxC.get() : xC.reserve((size_t)nvec * nf);
+    double* xs = graph ? gxS.get() : xS.reserve((size_t)nvec * nf);
+    if (timed)
+        F2G_CUDA(cudaEventRecord(cur_ev[0], st));
+    // beta same spin: per block transpose (Ia x Ib -> Ib x Ia), beta SpMM, transpose back (overwrites S)
+    for (int b = 0; b < B.nblk(); ++b) {
+        const int64_t* r = B.hblk.data() + 6 * b;
+        const int64_t off = r[3], nIa = r[4], nIb = r[5];
+        if (r[2] == 0)
+            continue;
+        const int cb = (int)r[1];
+        k_transpose_blk<<<dim3((unsigned)ceil_div(nIb, 32), (unsigned)ceil_div(nIa, 32), (unsigned)nvec), dim3(32, 8), 0,
+                          st>>>(nIa, nIb, C + off, nd, xc + off, nd);
+        F2G_LAUNCH("k_transpose_blk");
+        spmm_rows_raw(nIb, (int)nIa, hb.nnz, lcol[1].get() + B.cls_off[1][cb] * hb.nnz,
+                      lval[1].get() + B.cls_off[1][cb] * hb.nnz, xc + off, xs + off, false, nd, nvec, st);
+        k_transpose_blk<<<dim3((unsigned)ceil_div(nIa, 32), (unsigned)ceil_div(nIb, 32), (unsigned)nvec), dim3(32, 8), 0,
+                          st>>>(nIb, nIa, xs + off, nd, S + off, nd);
+        F2G_LAUNCH("k_transpose_blk");
+    }
+    if (timed)
+        F2G_CUDA(cudaEventRecord(cur_ev[1], st));
+    // alpha same spin + H0, accumulated
+    for (int b = 0; b < B.nblk(); ++b) {
+        const int64_t* r = B.hblk.data() + 6 * b;
+        const int64_t off = r[3], nIa = r[4], nIb = r[5];
+        if (r[2] == 0)
+            continue;
+        const int ca = (int)r[0];
+        spmm_rows_raw(nIa, (int)nIb, ha.nnz, lcol[0].get() + B.cls_off[0][ca] * ha.nnz,
+                      lval[0].get() + B.cls_off[0][ca] * ha.nnz, C + off, S + off, true, nd, nvec, st);
+    }
+    if (timed)
+        F2G_CUDA(cudaEventRecord(cur_ev[2], st));
+    // opposite spin on the embedding, added into S
+    const DetEnum de = s->dets();
+    blocks_embed<double>(de, nf, C, xc, nvec, st);
+    F2G_CUDA(cudaMemsetAsync(xs, 0, (size_t)nvec * nf * sizeof(double), st));
+    launch_opposite_sym(s, *osym, dV.get(), xc, xs, st, nvec, max_ctas > 0 ? max_ctas : 0);
+    blocks_extract<double>(de, nf, xs, S, nvec, st, true);
+    if (timed)
+        F2G_CUDA(cudaEventRecord(cur_ev[3], st));
+}
+
 // Harvest finished timed builds, oldest first; with wait, all of them.
 void SigmaBuilder::poll_timers(bool wait) {
     while (ev_count > 0) {
@@ -1154,6 +1282,12 @@ void SigmaBuilder::hamiltonian(const double* C, double* sigma, cudaStream_t st, 
         const int nv = std::min(bs, nvec - v0);
         const double* c = C + (int64_t)v0 * nd;
         double* sg = sigma + (int64_t)v0 * nd;
+        if (blocked_sym_path()) {
+            timer_begin();
+            run_blocked_sym(c, sg, st, nv, true, false);
+            timer_end(nv);
+            continue;
+        }
         if (s->blocked()) {
             // the space's vectors embedded into C1 vectors (zero elsewhere), sigma read back
             double* xc = xC.reserve((size_t)nv * nf);

@@ -59,6 +59,13 @@ struct SigmaBuilder {
     // (opposite_sym.cu); off: the C1 kernel on the embedding (same sigma up to rounding)
     bool use_sym = true;
     std::shared_ptr<struct OppositeSym> osym; // set when the space allows it
+    // such a space's same-spin terms on its own vectors: class-local string Hamiltonians (rows in
+    // the space's string order, columns as positions inside the class), rebuilt with the integrals
+    DevBuf<int32_t> lcol[2];
+    DevBuf<double> lval[2];
+    void build_local_ss(cudaStream_t st);
+    bool blocked_sym_path() const;
+    void run_blocked_sym(const double* C, double* S, cudaStream_t st, int nvec, bool timed, bool graph);
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
     DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
     DevBuf<unsigned int> tc_cmax; // per-vector largest |C| of a tensor-core launch (its operand scale)
