@@ -38,7 +38,9 @@ int f2g_strings_create(int na, int nb, int norb, void** out);
  * per space, symmetry the state irrep. The determinants are the reference's blocks in its
  * order (ci_strings.cc:34-184, ci_occupation.cc:35-142, ci_string_class.cc:7-66,
  * ci_strings_makers.cc:13-73); the sigma, RDM and CSF calls take vectors of ndet elements in
- * that order and run the C1 kernels on an embedding into the C1 CAS space of all orbitals. */
+ * that order. The RDMs, the FP32 sigma and the sigma of GAS-restricted spaces run the C1 kernels
+ * on an embedding into the C1 CAS space of all orbitals (zero outside the space); the FP64 sigma
+ * of a space blocked by irreps alone runs on the space's vectors (f2g_sigma_set_variant 4). */
 int f2g_strings_create_general(int na, int nb, int symmetry, int nspace, const int* gas_size, const int* orbsym,
                                int nmin, const int* gas_min, int nmax, const int* gas_max, void** out);
 int f2g_strings_destroy(void* strings);
@@ -103,7 +105,10 @@ int f2g_sigma_set_tensor_cores(void* sigma, int on, int* available);
  * cores (FP32 only), 1 same-spin kernel with half the columns per thread, 2 opposite-spin grid of
  * one thread block per SM. which = 3 sets the polls per bounded wait of the tensor-core kernel
  * (0 = the default, about a second) and clears its error flag; a small value makes the waits give
- * up, which exercises the error path. No reference counterpart. */
+ * up, which exercises the error path. which = 4 (default 1): the FP64 sigma of a space blocked by
+ * irreps alone on its own vectors (irrep-aware opposite-spin kernel, same-spin terms block by
+ * block); 0 runs the C1 kernels on the embedding (same sigma to rounding). No reference
+ * counterpart. */
 int f2g_sigma_set_variant(void* sigma, int which, int value);
 /* 1 if a tensor-core build gave up waiting for its matrix operations (results invalid). */
 int f2g_sigma_tc_error(void* sigma, int* out);
