@@ -539,7 +539,45 @@ def run_davidson(a):
     if "fp64" in res and "mixed" in res:
         out["mixed_vs_fp64_abs_dE"] = [abs(x - y) for x, y in zip(res["mixed"]["energies"], res["fp64"]["energies"])]
         out["speedup_mixed_over_fp64_davidson"] = res["fp64"]["seconds_davidson"] / res["mixed"]["seconds_davidson"]
+    out["csf_transforms"] = csf_transform_roofline(a.norb)
     print(json.dumps(out), flush=True)
+
+
+def csf_transform_roofline(norb):
+    """The FP64 CSF <-> determinant transforms of one singlet vector at CAS(n e, n o), timed alone
+    with CUDA events, against HBM: algorithmic bytes B_csf = 8 (ncsf + ndet) + 12 ncoupling (the two
+    vectors once, every coupling's coefficient and determinant address once) per transform."""
+    import torch
+
+    from forte2_gb300.ci_helpers import CISpinAdapter, CIStrings
+
+    na, nb, _, _, ndet = cas_dims(norb, norb, 0)
+    s = CIStrings(na, nb, 0, [[0] * norb], [], [])
+    sa = CISpinAdapter(0, 0, norb)
+    sa.prepare_couplings(s.make_determinants())
+    csf = torch.from_numpy(random_ci_vector(sa.ncsf, 5)).cuda()
+    det = torch.empty(ndet, dtype=torch.float64, device="cuda")
+    back = torch.empty_like(csf)
+    st = torch.cuda.current_stream()
+    peak = _measured_peaks().get("hbm_gbs") or 6801.7
+    out = {"ncsf": sa.ncsf, "ndet": ndet, "ncoupling": sa.ncoupling,
+           "bytes_per_transform": 8 * (sa.ncsf + ndet) + 12 * sa.ncoupling, "hbm_peak_gbs": peak}
+    for name, f in (("csf_to_det", lambda: sa.csf_C_to_det_C(csf, det)), ("det_to_csf", lambda: sa.det_C_to_csf_C(det, back))):
+        f()
+        f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(5):
+            f()
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        gbs = out["bytes_per_transform"] / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "achieved_gbs": gbs, "frac_of_hbm": gbs / peak}
+    del sa, s
+    torch.cuda.empty_cache()
+    return out
 
 
 def rdm_cpu_baseline(norb, na, nb, c, budget_s):
