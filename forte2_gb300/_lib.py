@@ -28,6 +28,14 @@ def _declare(L):
         "f2g_strings_create": (i32, [i32, i32, i32, pp]),
         "f2g_strings_create_general": (i32, [i32, i32, i32, i32, P, P, i32, P, i32, P, pp]),
         "f2g_strings_blocks_info": (i32, [vp, P]),
+        "f2g_rel_sigma_create": (i32, [vp, d, P, P, pp]),
+        "f2g_rel_sigma_destroy": (i32, [vp]),
+        "f2g_rel_sigma_set_algorithm": (i32, [vp, C.c_char_p]),
+        "f2g_rel_sigma_get_algorithm": (i32, [vp, C.c_char_p, i32]),
+        "f2g_rel_sigma_set_memory": (i32, [vp, i32]),
+        "f2g_rel_sigma_apply": (i32, [vp, P, P, i32, vp]),
+        "f2g_rel_sigma_hdiag": (i32, [vp, P, vp]),
+        "f2g_rel_sigma_element": (i32, [vp, i64, i64, P]),
         "f2g_blocks_enumerate": (i32, [i32, i32, i32, i32, P, P, i32, P, i32, P, P, P, P, P, P, P]),
         "f2g_strings_class_strings": (i32, [vp, i32, P, P]),
         "f2g_strings_block_table": (i32, [vp, P]),

@@ -298,6 +298,90 @@ class CIStrings:
         return out
 
 
+class RelCISigmaBuilder:
+    """Two-component sigma builder (forte2/ci/rel_ci_sigma_builder.cc:15-238,
+    rel_ci_sigma_builder_harrison_zarrabian.cc) on the device: strings with nb == 0, complex H
+    and V. As in the reference the default algorithm is "kh", for which Hamiltonian applies only E;
+    "hz" applies the full operator."""
+
+    def __init__(self, lists: CIStrings, E, H, V, log_level=3):
+        if lists.nb != 0:
+            raise RuntimeError("RelCISigmaBuilder requires nb == 0 (two-component CI treats all electrons as "
+                               "alpha spinors).")
+        n = lists.norb
+        H = np.ascontiguousarray(H, dtype=np.complex128)
+        V = np.ascontiguousarray(V, dtype=np.complex128)
+        if H.ndim != 2:
+            raise RuntimeError("H must be a 2D matrix.")
+        if H.shape != (n, n):
+            raise RuntimeError("H shape does not match the number of orbitals.")
+        if V.ndim != 4:
+            raise RuntimeError("V must be a 4D tensor.")
+        if V.shape != (n, n, n, n):
+            raise RuntimeError("V shape does not match the number of orbitals.")
+        self.lists = lists
+        self.log_level = int(log_level)
+        self.h = None
+        if getattr(lists, "_empty", False):
+            self._E = float(E)
+            return
+        h = C.c_void_p()
+        check(lib().f2g_rel_sigma_create(lists.h, float(E), H.ctypes.data, V.ctypes.data, C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().f2g_rel_sigma_destroy(h)
+            self.h = None
+
+    def set_algorithm(self, algorithm):
+        check(lib().f2g_rel_sigma_set_algorithm(self.h, str(algorithm).encode()))
+
+    def get_algorithm(self):
+        buf = C.create_string_buffer(64)
+        check(lib().f2g_rel_sigma_get_algorithm(self.h, buf, 64))
+        return buf.value.decode()
+
+    def set_memory(self, mb):
+        check(lib().f2g_rel_sigma_set_memory(self.h, int(mb)))
+
+    def Hamiltonian(self, basis, sigma):
+        """sigma <- H basis (overwritten). numpy complex128 vectors, or CUDA complex128 tensors
+        ((ndet,) or (nvec, ndet), contiguous) that stay on the device."""
+        torch = _torch()
+        nd = self.lists.ndet
+        if _is_cuda_tensor(basis) and _is_cuda_tensor(sigma):
+            if basis.dtype != torch.complex128 or sigma.dtype != torch.complex128:
+                raise TypeError("device vectors must be complex128")
+            if not basis.is_contiguous() or not sigma.is_contiguous():
+                raise RuntimeError("device vectors must be contiguous")
+            nvec = 1 if basis.dim() == 1 else basis.shape[0]
+            if basis.numel() != nvec * nd or sigma.numel() != basis.numel():
+                raise RuntimeError("vector length does not match the number of determinants")
+            check(lib().f2g_rel_sigma_apply(self.h, basis.data_ptr(), sigma.data_ptr(), nvec, stream_handle()))
+            return sigma
+        b = np.ascontiguousarray(basis, dtype=np.complex128)
+        if b.shape[0] != nd or np.shape(sigma)[0] != nd:
+            raise RuntimeError("vector length does not match the number of determinants")
+        db = torch.from_numpy(b).cuda()
+        ds = torch.empty_like(db)
+        check(lib().f2g_rel_sigma_apply(self.h, db.data_ptr(), ds.data_ptr(), 1, stream_handle()))
+        sigma[:] = ds.cpu().numpy()
+        return sigma
+
+    def form_Hdiag(self, dets=None):
+        torch = _torch()
+        out = torch.empty(max(1, self.lists.ndet), dtype=torch.complex128, device="cuda")
+        check(lib().f2g_rel_sigma_hdiag(self.h, out.data_ptr(), stream_handle()))
+        return out[: self.lists.ndet].cpu().numpy()
+
+    def slater_rules(self, dets, I, J):
+        out = np.zeros(2)
+        check(lib().f2g_rel_sigma_element(self.h, int(I), int(J), out.ctypes.data))
+        return complex(out[0], out[1])
+
+
 class CISpinAdapter:
     """CSF <-> determinant transforms (forte2/determinant/ci_spin_adapter.cc:55-288) on the device."""
 

@@ -354,6 +354,12 @@ __global__ void k_embed(DetEnum de, int64_t nfull, const T* __restrict__ sub, T*
     full[v * nfull + de.c1(i)] = sub[v * de.ndet + i];
 }
 
+template <typename T> __device__ __forceinline__ void add_to(T& a, const T& b) { a += b; }
+template <> __device__ __forceinline__ void add_to<double2>(double2& a, const double2& b) {
+    a.x += b.x;
+    a.y += b.y;
+}
+
 template <typename T>
 __global__ void k_extract(DetEnum de, int64_t nfull, const T* __restrict__ full, T* __restrict__ sub, int add) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -362,7 +368,7 @@ __global__ void k_extract(DetEnum de, int64_t nfull, const T* __restrict__ full,
     const int64_t v = blockIdx.y;
     const T x = full[v * nfull + de.c1(i)];
     if (add)
-        sub[v * de.ndet + i] += x;
+        add_to(sub[v * de.ndet + i], x);
     else
         sub[v * de.ndet + i] = x;
 }
@@ -392,6 +398,8 @@ void blocks_extract(const DetEnum& de, int64_t nfull, const T* full, T* sub, int
 
 template void blocks_embed<double>(const DetEnum&, int64_t, const double*, double*, int, cudaStream_t);
 template void blocks_embed<float>(const DetEnum&, int64_t, const float*, float*, int, cudaStream_t);
+template void blocks_embed<double2>(const DetEnum&, int64_t, const double2*, double2*, int, cudaStream_t);
+template void blocks_extract<double2>(const DetEnum&, int64_t, const double2*, double2*, int, cudaStream_t, bool);
 template void blocks_extract<double>(const DetEnum&, int64_t, const double*, double*, int, cudaStream_t, bool);
 template void blocks_extract<float>(const DetEnum&, int64_t, const float*, float*, int, cudaStream_t, bool);
 

@@ -9,6 +9,7 @@
 
 #include "../../include/forte2_gb300.h"
 #include "csf.cuh"
+#include "rel.cuh"
 #include "dgraph.cuh"
 #include "rdm.cuh"
 
@@ -346,6 +347,96 @@ int f2g_sigma_set_memory(void* sb, int mb) {
         if (mb < 0)
             throw Error(2, "CI builder memory must be non-negative.");
         static_cast<SigmaBuilder*>(sb)->memory = (size_t)mb * 1024 * 1024;
+    });
+}
+
+// ---- two-component sigma builder (RelCISigmaBuilder) ----
+
+int f2g_rel_sigma_create(void* strings, double E, const double* H, const double* V, void** out) {
+    return guard([&] {
+        need(strings, "strings");
+        need(out, "out");
+        auto* s = static_cast<CIStrings*>(strings);
+        const size_t n = (size_t)s->norb;
+        if (n && (!H || !V))
+            throw Error(2, "NULL integrals");
+        *out = new RelSigmaBuilder(s, E, reinterpret_cast<const std::complex<double>*>(H),
+                                   reinterpret_cast<const std::complex<double>*>(V));
+    });
+}
+
+int f2g_rel_sigma_destroy(void* h) {
+    return guard([&] { delete static_cast<RelSigmaBuilder*>(h); });
+}
+
+int f2g_rel_sigma_set_algorithm(void* h, const char* name) {
+    return guard([&] {
+        need(h, "rel sigma");
+        need(name, "name");
+        const std::string a(name);
+        auto* b = static_cast<RelSigmaBuilder*>(h);
+        if (a == "kh" || a == "knowles-handy")
+            b->algorithm = 0;
+        else if (a == "hz" || a == "harrison-zarrabian")
+            b->algorithm = 1;
+        else
+            throw Error(1, "CI algorithm " + a + " not valid.");
+    });
+}
+
+int f2g_rel_sigma_get_algorithm(void* h, char* buf, int buflen) {
+    return guard([&] {
+        need(h, "rel sigma");
+        need(buf, "buf");
+        if (buflen <= 0)
+            throw Error(2, "buflen must be positive");
+        const char* name = static_cast<RelSigmaBuilder*>(h)->algorithm == 0 ? "Knowles-Handy" : "Harrison-Zarrabian";
+        std::strncpy(buf, name, (size_t)buflen);
+        buf[buflen - 1] = 0;
+    });
+}
+
+int f2g_rel_sigma_set_memory(void* h, int mb) {
+    return guard([&] {
+        need(h, "rel sigma");
+        if (mb < 0)
+            throw Error(2, "CI builder memory must be non-negative.");
+        static_cast<RelSigmaBuilder*>(h)->memory = (size_t)mb * 1024 * 1024;
+    });
+}
+
+int f2g_rel_sigma_apply(void* h, const double* C, double* sigma, int nvec, void* stream) {
+    return guard([&] {
+        need(h, "rel sigma");
+        auto* b = static_cast<RelSigmaBuilder*>(h);
+        if (nvec < 0)
+            throw Error(2, "nvec must be >= 0");
+        if (nvec == 0 || b->s->ndet == 0)
+            return;
+        need(C, "C");
+        need(sigma, "sigma");
+        b->hamiltonian(reinterpret_cast<const double2*>(C), reinterpret_cast<double2*>(sigma), S(stream), nvec);
+    });
+}
+
+int f2g_rel_sigma_hdiag(void* h, double* out, void* stream) {
+    return guard([&] {
+        need(h, "rel sigma");
+        auto* b = static_cast<RelSigmaBuilder*>(h);
+        if (b->s->ndet == 0)
+            return;
+        need(out, "out");
+        b->hdiag(reinterpret_cast<double2*>(out), S(stream));
+    });
+}
+
+int f2g_rel_sigma_element(void* h, int64_t I, int64_t J, double* out) {
+    return guard([&] {
+        need(h, "rel sigma");
+        need(out, "out");
+        const std::complex<double> x = static_cast<RelSigmaBuilder*>(h)->element(I, J);
+        out[0] = x.real();
+        out[1] = x.imag();
     });
 }
 

@@ -727,6 +727,14 @@ void SigmaBuilder::build_local_ss(cudaStream_t st) {
     }
 }
 
+void build_ss_values(int n, int k, int64_t N0, int nnz, const uint64_t* str, const uint64_t* binom, const double* h,
+                     const double* V, double e0, int32_t* col, double* val, cudaStream_t st) {
+    if (N0 == 0 || nnz == 0)
+        return;
+    k_build_ss<double><<<ceil_div(N0, 128), 128, 0, st>>>(n, k, N0, nnz, str, binom, h, V, e0, 3, col, val);
+    F2G_LAUNCH("k_build_ss");
+}
+
 // FP32 copies of the string-Hamiltonian values, made once per set of integrals on first use.
 void SigmaBuilder::ensure_fp32() {
     if (fp32_ready)

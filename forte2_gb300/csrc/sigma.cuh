@@ -145,5 +145,11 @@ struct SigmaBuilder {
 };
 
 int ss_row_nnz(int n, int k);
+// String-Hamiltonian rows (columns and values) of one spin's strings for integrals h, V and
+// diagonal offset e0: the H1 + same-spin H2 operator, nnz = ss_row_nnz(n, k) entries per row,
+// the diagonal first. Every value is a signed sum of integral elements, so complex integrals give
+// the real and imaginary parts from two calls.
+void build_ss_values(int n, int k, int64_t N0, int nnz, const uint64_t* str, const uint64_t* binom, const double* h,
+                     const double* V, double e0, int32_t* col, double* val, cudaStream_t st);
 
 } // namespace f2g

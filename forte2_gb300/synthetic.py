@@ -82,6 +82,30 @@ def rotate_integrals(ints: ActiveSpaceIntegrals, seed: int, theta: float = 0.05)
     return ActiveSpaceIntegrals(ints.E, np.ascontiguousarray(h), V, eri)
 
 
+def make_spinor_integrals(nspinor: int, seed: int, naux: int | None = None):
+    """Seeded complex integrals of a two-component (spinor) active space: E, a Hermitian h
+    (nspinor x nspinor) and physicist V[p][q][r][s] = (pr|qs) with (pr|qs) = sum_Q L_Q[p][r]
+    L_Q[q][s] over Hermitian L_Q, so that V[p][q][r][s] = V[q][p][s][r] and
+    conj(V[p][q][r][s]) = V[r][s][p][q] (a Hermitian two-body operator)."""
+    n = int(nspinor)
+    naux = 3 * n if naux is None else int(naux)
+    rng = np.random.default_rng(seed)
+    eps = np.sort(rng.uniform(-2.0, 1.0, n))
+    A = rng.normal(0.0, 0.05, (n, n)) + 1j * rng.normal(0.0, 0.05, (n, n))
+    h = np.diag(eps).astype(np.complex128) + np.triu(A, 1) + np.triu(A, 1).conj().T
+    L = rng.normal(0.0, 0.1, (naux, n, n)) + 1j * rng.normal(0.0, 0.1, (naux, n, n))
+    L = 0.5 * (L + np.conj(np.transpose(L, (0, 2, 1))))
+    eri = np.einsum("Qpr,Qqs->prqs", L, L, optimize=True)
+    V = np.ascontiguousarray(eri.transpose(0, 2, 1, 3))
+    return 0.25, np.ascontiguousarray(h), V
+
+
+def random_complex_vector(ndet: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    c = rng.normal(size=ndet) + 1j * rng.normal(size=ndet)
+    return c / np.linalg.norm(c)
+
+
 def symmetrize_integrals(ints: ActiveSpaceIntegrals, orbsym) -> ActiveSpaceIntegrals:
     """The integrals of a molecule with an abelian point group: with irreps ``orbsym[p]`` (0..7,
     the product of two irreps their XOR), h[p][q] = 0 unless p and q share an irrep and

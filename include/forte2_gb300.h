@@ -161,6 +161,25 @@ int f2g_sigma_rdm(void* sigma, int kind, const double* dev_C_left, const double*
 int f2g_rdm_pair_list(int norb, int nel, int force_wide, void* host_entries, uint16_t* host_seg_pair,
                       int64_t* host_counts4);
 
+/* ---- two-component (relativistic) sigma builder: replaces RelCISigmaBuilder(lists, E, H, V)
+ *      (forte2/ci/rel_ci_sigma_builder.cc:15-238, rel_ci_sigma_builder_harrison_zarrabian.cc;
+ *      binding api/ci_helpers_api.cc:203-229). The strings must have nb == 0 (every electron an
+ *      alpha spinor). H (norb x norb) and V (norb^4, physicist) are complex, stored as
+ *      interleaved (re, im) doubles, as are the vectors. The default algorithm is Knowles-Handy,
+ *      for which the reference applies only E (its two-component KH branch is empty); "hz" applies
+ *      E + H1 + H2. */
+int f2g_rel_sigma_create(void* strings, double E, const double* host_H, const double* host_V, void** out);
+int f2g_rel_sigma_destroy(void* rel_sigma);
+int f2g_rel_sigma_set_algorithm(void* rel_sigma, const char* name);
+int f2g_rel_sigma_get_algorithm(void* rel_sigma, char* buf, int buflen);
+int f2g_rel_sigma_set_memory(void* rel_sigma, int mb);
+/* sigma <- H C for nvec complex vectors of ndet elements back to back (device, overwritten) */
+int f2g_rel_sigma_apply(void* rel_sigma, const double* dev_C, double* dev_sigma, int nvec, void* stream);
+/* form_Hdiag(dets): the complex diagonal (ndet, device) */
+int f2g_rel_sigma_hdiag(void* rel_sigma, double* dev_out, void* stream);
+/* slater_rules(dets, I, J) = <I|H|J> into host_out[2] */
+int f2g_rel_sigma_element(void* rel_sigma, int64_t I, int64_t J, double* host_out);
+
 /* ---- spin adapter: replaces CISpinAdapter(twoS, twoMs, norb) + prepare_couplings(dets)
  *      (forte2/determinant/ci_spin_adapter.cc:55-235; binding api/ci_helpers_api.cc:190-200). */
 int f2g_spin_adapter_create(void* strings, int twoS, int twoMs, void** out);

@@ -34,6 +34,10 @@ SOURCES=(
     ci/ci_sigma_builder_3rdm.cc
     determinant/slater_rules.cc
     determinant/ci_spin_adapter.cc
+    ci/rel_ci_sigma_builder.cc
+    ci/rel_ci_sigma_builder_harrison_zarrabian.cc
+    ci/rel_ci_sigma_builder_rdm.cc
+    determinant/rel_slater_rules.cc
 )
 OBJS=()
 pids=()

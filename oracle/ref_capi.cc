@@ -26,6 +26,7 @@
 #define private public
 #include "ci/ci_sigma_builder.h"
 #undef private
+#include "ci/rel_ci_sigma_builder.h"
 
 using namespace forte2;
 
@@ -51,6 +52,17 @@ struct RefSigma {
 np_vector vec_view(double* p, size_t n) {
     size_t shape[1] = {n};
     return np_vector(p, 1, shape);
+}
+
+struct RefRelSigma {
+    RelCISigmaBuilder* sb;
+    std::vector<std::complex<double>> H, V;
+    int norb;
+};
+
+np_vector_complex cvec_view(double* p, size_t n) {
+    size_t shape[1] = {n};
+    return np_vector_complex(reinterpret_cast<std::complex<double>*>(p), 1, shape);
 }
 } // namespace
 
@@ -444,6 +456,95 @@ int64_t ref_rdm(void* h, int kind, double* CL, double* CR, int64_t ndet, double*
         case 11: return copy(sb->compute_abb_3rdm(l, r));
         case 12: return copy(sb->compute_sf_3rdm(l, r));
         case 13: return copy(sb->compute_sf_3cumulant(l, r));
+        default: throw std::runtime_error("unknown RDM kind");
+        }
+    } catch (const std::exception& e) {
+        fail(e, 1);
+    }
+    return -1;
+}
+
+/// The reference's two-component sigma builder (rel_ci_sigma_builder*.cc) on a CIStrings with
+/// nb == 0. H (n x n) and V (n^4, physicist) are complex, interleaved (re, im) doubles.
+void* ref_rel_sigma_new(void* hs, double E, const double* H, const double* V, int norb, int log_level) {
+    try {
+        auto* s = static_cast<RefStrings*>(hs);
+        const size_t n2 = (size_t)norb * norb, n4 = n2 * n2;
+        auto* r = new RefRelSigma{nullptr, {}, {}, norb};
+        r->H.resize(n2);
+        r->V.resize(n4);
+        std::memcpy(r->H.data(), H, n2 * sizeof(std::complex<double>));
+        std::memcpy(r->V.data(), V, n4 * sizeof(std::complex<double>));
+        size_t hs2[2] = {(size_t)norb, (size_t)norb};
+        size_t vs4[4] = {(size_t)norb, (size_t)norb, (size_t)norb, (size_t)norb};
+        np_matrix_complex Hm(r->H.data(), 2, hs2);
+        np_tensor4_complex Vt(r->V.data(), 4, vs4);
+        r->sb = new RelCISigmaBuilder(*s->lists, E, Hm, Vt, log_level);
+        return r;
+    } catch (const std::exception& e) {
+        fail(e, 1);
+    }
+    return nullptr;
+}
+
+void ref_rel_sigma_free(void* h) {
+    auto* r = static_cast<RefRelSigma*>(h);
+    delete r->sb;
+    delete r;
+}
+
+int ref_rel_sigma_set_algorithm(void* h, const char* name) {
+    try {
+        static_cast<RefRelSigma*>(h)->sb->set_algorithm(name);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e, 1);
+    }
+}
+
+int ref_rel_sigma_hamiltonian(void* h, double* basis, double* sigma, int64_t ndet) {
+    try {
+        static_cast<RefRelSigma*>(h)->sb->Hamiltonian(cvec_view(basis, ndet), cvec_view(sigma, ndet));
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e, 1);
+    }
+}
+
+/// form_Hdiag(dets) into out (ndet complex, interleaved)
+void ref_rel_form_hdiag(void* h, void* hs, double* out) {
+    auto* r = static_cast<RefRelSigma*>(h);
+    auto* s = static_cast<RefStrings*>(hs);
+    auto v = r->sb->form_Hdiag(s->dets);
+    std::memcpy(out, v.data(), v.size() * sizeof(std::complex<double>));
+}
+
+/// slater_rules(dets, I, J) into out[2]
+void ref_rel_slater_rules(void* h, void* hs, int64_t I, int64_t J, double* out) {
+    auto* r = static_cast<RefRelSigma*>(h);
+    auto* s = static_cast<RefStrings*>(hs);
+    const std::complex<double> x = r->sb->slater_rules(s->dets, (size_t)I, (size_t)J);
+    out[0] = x.real();
+    out[1] = x.imag();
+}
+
+/// spin-orbital RDMs between two complex vectors: kind 0 so_1rdm (n^2), 1 so_2rdm (n^4),
+/// 2 so_2cumulant (n^4), 3 so_3rdm (n^6), 4 so_3cumulant (n^6); interleaved complex output.
+int64_t ref_rel_rdm(void* h, int kind, double* CL, double* CR, int64_t ndet, double* out) {
+    try {
+        auto* sb = static_cast<RefRelSigma*>(h)->sb;
+        auto l = cvec_view(CL, ndet), r = cvec_view(CR, ndet);
+        auto copy = [&](const auto& a) {
+            const size_t n = a.size();
+            std::memcpy(out, a.data(), n * sizeof(std::complex<double>));
+            return (int64_t)n;
+        };
+        switch (kind) {
+        case 0: return copy(sb->compute_1rdm(l, r));
+        case 1: return copy(sb->compute_2rdm(l, r));
+        case 2: return copy(sb->compute_2cumulant(l, r));
+        case 3: return copy(sb->compute_3rdm(l, r));
+        case 4: return copy(sb->compute_3cumulant(l, r));
         default: throw std::runtime_error("unknown RDM kind");
         }
     } catch (const std::exception& e) {

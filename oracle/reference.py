@@ -85,6 +85,15 @@ def lib():
     L.ref_rdm.argtypes = [vp, C.c_int, _f64p, _f64p, C.c_int64, _f64p]
     L.oracle_blas_open.argtypes = [C.c_char_p]
     L.oracle_blas_set_threads.argtypes = [C.c_int]
+    L.ref_rel_sigma_new.restype = vp
+    L.ref_rel_sigma_new.argtypes = [vp, C.c_double, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+    L.ref_rel_sigma_free.argtypes = [vp]
+    L.ref_rel_sigma_set_algorithm.argtypes = [vp, C.c_char_p]
+    L.ref_rel_sigma_hamiltonian.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_int64]
+    L.ref_rel_form_hdiag.argtypes = [vp, vp, C.c_void_p]
+    L.ref_rel_slater_rules.argtypes = [vp, vp, C.c_int64, C.c_int64, C.c_void_p]
+    L.ref_rel_rdm.restype = C.c_int64
+    L.ref_rel_rdm.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     _lib = L
     return L
 
@@ -241,6 +250,63 @@ class RefSigmaBuilder:
 
     def slater_rules_csf(self, spin_adapter, I, J):
         return lib().ref_slater_rules_csf(self.h, spin_adapter.h, self.strings.h, int(I), int(J))
+
+
+class RefRelSigmaBuilder:
+    """The reference's two-component RelCISigmaBuilder (ci/rel_ci_sigma_builder*.cc) on strings
+    with nb == 0: complex H (n, n) and physicist V (n, n, n, n)."""
+
+    RDM_KINDS = ("so_1rdm", "so_2rdm", "so_2cumulant", "so_3rdm", "so_3cumulant")
+
+    def __init__(self, strings: RefCIStrings, E, H, V, log_level=0):
+        self.strings = strings
+        self.norb = strings.norb
+        self._H = np.ascontiguousarray(H, dtype=np.complex128)
+        self._V = np.ascontiguousarray(V, dtype=np.complex128)
+        h = lib().ref_rel_sigma_new(strings.h, float(E), self._H.ctypes.data, self._V.ctypes.data, self.norb,
+                                    log_level)
+        if not h:
+            raise RuntimeError(lib().ref_last_error().decode())
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ref_rel_sigma_free(self.h)
+            self.h = None
+
+    def set_algorithm(self, name):
+        if lib().ref_rel_sigma_set_algorithm(self.h, name.encode()):
+            raise RuntimeError(lib().ref_last_error().decode())
+
+    def Hamiltonian(self, basis, sigma):
+        b = np.ascontiguousarray(basis, dtype=np.complex128)
+        out = np.zeros(self.strings.ndet, dtype=np.complex128)
+        if lib().ref_rel_sigma_hamiltonian(self.h, b.ctypes.data, out.ctypes.data, self.strings.ndet):
+            raise RuntimeError(lib().ref_last_error().decode())
+        sigma[:] = out
+        return sigma
+
+    def form_Hdiag(self):
+        out = np.zeros(self.strings.ndet, dtype=np.complex128)
+        lib().ref_rel_form_hdiag(self.h, self.strings.h, out.ctypes.data)
+        return out
+
+    def slater_rules(self, I, J):
+        out = np.zeros(2)
+        lib().ref_rel_slater_rules(self.h, self.strings.h, int(I), int(J), out.ctypes.data)
+        return complex(out[0], out[1])
+
+    def rdm(self, kind, CL, CR):
+        n = self.norb
+        size = {0: n ** 2, 1: n ** 4, 2: n ** 4, 3: n ** 6, 4: n ** 6}[self.RDM_KINDS.index(kind)]
+        out = np.zeros(max(size, 1), dtype=np.complex128)
+        cl = np.ascontiguousarray(CL, dtype=np.complex128)
+        cr = np.ascontiguousarray(CR, dtype=np.complex128)
+        got = lib().ref_rel_rdm(self.h, self.RDM_KINDS.index(kind), cl.ctypes.data, cr.ctypes.data,
+                                self.strings.ndet, out.ctypes.data)
+        if got < 0:
+            raise RuntimeError(lib().ref_last_error().decode())
+        return out[:got]
 
 
 class RefSpinAdapter:

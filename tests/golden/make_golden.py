@@ -413,6 +413,57 @@ def gen_blocks(out, ref_root):
         json.dump(meta, f, indent=1)
 
 
+# Two-component (spinor) spaces: (spinors, electrons, orbital_symmetry or None, integral seed,
+# vector seed). nb = 0: every electron is an alpha spinor.
+REL_CASES = [(4, 1, None, 91, 901), (6, 0, None, 92, 902), (8, 3, None, 93, 903), (10, 4, None, 94, 904),
+             (12, 5, None, 95, 905), (14, 6, None, 96, 906), (8, 4, [[0, 1, 0, 1, 0, 1, 0, 1]], 97, 907)]
+
+
+def gen_rel(out):
+    """The reference's RelCISigmaBuilder: sigma of a seeded complex vector (hz), the kh result,
+    form_Hdiag, a few slater_rules elements; for the small spaces the lowest eigenvalues of the
+    dense Hamiltonian built from its sigma."""
+    from forte2_gb300.synthetic import make_spinor_integrals, random_complex_vector
+
+    data = {}
+    meta = []
+    for k, (n, ne, orbsym, iseed, cseed) in enumerate(REL_CASES):
+        E, H, V = make_spinor_integrals(n, iseed)
+        space = (1 if orbsym else 0, orbsym, [], []) if orbsym else (0, [[0] * n], [], [])
+        s = ref.RefCIStrings(ne, 0, *space)
+        sb = ref.RefRelSigmaBuilder(s, E, H, V)
+        key = f"r{k}"
+        c = random_complex_vector(s.ndet, cseed)
+        sig_kh = np.zeros(s.ndet, dtype=np.complex128)
+        sb.Hamiltonian(c, sig_kh)  # the default algorithm
+        sb.set_algorithm("hz")
+        sig = np.zeros(s.ndet, dtype=np.complex128)
+        sb.Hamiltonian(c, sig)
+        data[f"{key}_sigma"] = sig
+        data[f"{key}_sigma_kh"] = sig_kh
+        data[f"{key}_hdiag"] = sb.form_Hdiag()
+        rng = np.random.default_rng(cseed)
+        pairs = rng.integers(0, max(1, s.ndet), size=(12, 2))
+        data[f"{key}_pairs"] = pairs
+        data[f"{key}_elements"] = np.array([sb.slater_rules(i, j) for i, j in pairs], dtype=np.complex128)
+        entry = dict(key=key, nspinor=n, nel=ne, orbital_symmetry=orbsym, iseed=iseed, cseed=cseed, ndet=s.ndet)
+        if s.ndet <= 800:
+            Hd = np.zeros((s.ndet, s.ndet), dtype=np.complex128)
+            for i in range(s.ndet):
+                e = np.zeros(s.ndet, dtype=np.complex128)
+                e[i] = 1.0
+                o = np.zeros(s.ndet, dtype=np.complex128)
+                sb.Hamiltonian(e, o)
+                Hd[:, i] = o
+            entry["hermitian_dev"] = float(np.abs(Hd - Hd.conj().T).max())
+            entry["evals"] = [float(x) for x in np.linalg.eigvalsh(0.5 * (Hd + Hd.conj().T))[:4]]
+        meta.append(entry)
+        print("rel", key, s.ndet, flush=True)
+    np.savez_compressed(os.path.join(out, "rel.npz"), **data)
+    with open(os.path.join(out, "rel.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
 # MCSCF-style sequence: (na, nb, norb, multiplicity, nroot, integral seed, rotation seeds, theta, e_tol)
 MCSCF_CASES = [(4, 4, 8, 1, 2, 4100, (4111, 4122), 0.05, 1e-10),
                (5, 5, 10, 1, 1, 4200, (4211, 4222), 0.03, 1e-10),
@@ -460,6 +511,7 @@ def main():
              "checksums": lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_CASES, "sigma_checksums.json"),
              "davidson": lambda: gen_davidson(HERE, a.reference), "rdm": lambda: gen_rdm(HERE),
              "mcscf": lambda: gen_mcscf(HERE, a.reference), "blocks": lambda: gen_blocks(HERE, a.reference),
+             "rel": lambda: gen_rel(HERE),
              "rdm3": lambda: gen_rdm3(HERE)}
     if a.big:
         steps["big"] = lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_BIG, "sigma_checksums_16.json")

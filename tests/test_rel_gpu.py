@@ -1,0 +1,107 @@
+"""Two-component (relativistic) sigma on the GPU against the reference's own RelCISigmaBuilder
+(tests/golden/rel.npz / rel.json, made by make_golden.py --only rel from
+ci/rel_ci_sigma_builder*.cc): sigma (hz and the default kh), the diagonal, matrix elements and
+the lowest eigenvalues of the dense Hamiltonian; complex FP64, tolerance 1e-12 relative."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from forte2_gb300.synthetic import make_spinor_integrals, random_complex_vector
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+with open(os.path.join(GOLD, "rel.json")) as _f:
+    CASES = json.load(_f)
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(os.path.join(GOLD, "rel.npz"))
+
+
+def _builder(case):
+    from forte2_gb300.ci_helpers import CIStrings, RelCISigmaBuilder
+
+    n, ne, orbsym = case["nspinor"], case["nel"], case["orbital_symmetry"]
+    s = CIStrings(ne, 0, 1, orbsym, [], []) if orbsym else CIStrings(ne, 0, 0, [[0] * n], [], [])
+    E, H, V = make_spinor_integrals(n, case["iseed"])
+    return s, RelCISigmaBuilder(s, E, H, V, 0)
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["key"])
+def test_rel_sigma_matches_reference(cuda, gold, case):
+    torch = cuda
+    s, sb = _builder(case)
+    k = case["key"]
+    assert s.ndet == case["ndet"]
+    c = random_complex_vector(s.ndet, case["cseed"])
+    # the reference's default algorithm (Knowles-Handy) applies E only
+    assert sb.get_algorithm() == "Knowles-Handy"
+    out = np.zeros(s.ndet, dtype=np.complex128)
+    sb.Hamiltonian(c, out)
+    assert np.abs(out - gold[f"{k}_sigma_kh"]).max() < 1e-14
+    sb.set_algorithm("hz")
+    assert sb.get_algorithm() == "Harrison-Zarrabian"
+    sb.Hamiltonian(c, out)
+    ref = gold[f"{k}_sigma"]
+    scale = max(1.0, np.abs(ref).max())
+    assert np.abs(out - ref).max() < 1e-12 * scale
+    # device tensors, two vectors at once, twice: the same bits
+    X = torch.as_tensor(np.stack([c, 1j * c]), device="cuda")
+    S1, S2 = torch.empty_like(X), torch.empty_like(X)
+    sb.Hamiltonian(X, S1)
+    sb.Hamiltonian(X, S2)
+    assert torch.equal(S1, S2)
+    assert np.array_equal(S1[0].cpu().numpy(), out)
+    assert np.abs(S1[1].cpu().numpy() - 1j * out).max() < 1e-12 * scale
+    hd = sb.form_Hdiag()
+    assert np.abs(hd - gold[f"{k}_hdiag"]).max() < 1e-12 * max(1.0, np.abs(hd).max())
+    for (i, j), x in zip(gold[f"{k}_pairs"], gold[f"{k}_elements"]):
+        if s.ndet:
+            assert abs(sb.slater_rules(None, int(i), int(j)) - x) < 1e-12 * scale
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if "evals" in c], ids=lambda c: c["key"])
+def test_rel_spectrum_matches_reference(cuda, case):
+    """The dense Hamiltonian from the device sigma is Hermitian and has the reference's lowest
+    eigenvalues."""
+    s, sb = _builder(case)
+    sb.set_algorithm("hz")
+    nd = s.ndet
+    Hd = np.zeros((nd, nd), dtype=np.complex128)
+    e = np.zeros(nd, dtype=np.complex128)
+    o = np.zeros(nd, dtype=np.complex128)
+    for i in range(nd):
+        e[:] = 0.0
+        e[i] = 1.0
+        sb.Hamiltonian(e, o)
+        Hd[:, i] = o
+    assert np.abs(Hd - Hd.conj().T).max() < 1e-12
+    w = np.linalg.eigvalsh(0.5 * (Hd + Hd.conj().T))[: len(case["evals"])]
+    np.testing.assert_allclose(w, case["evals"], rtol=0, atol=1e-10)
+
+
+def test_rel_errors(cuda):
+    from forte2_gb300.ci_helpers import CIStrings, RelCISigmaBuilder
+
+    E, H, V = make_spinor_integrals(6, 1)
+    with pytest.raises(RuntimeError, match="nb == 0"):
+        RelCISigmaBuilder(CIStrings(2, 1, 0, [[0] * 6], [], []), E, H, V)
+    s = CIStrings(3, 0, 0, [[0] * 6], [], [])
+    with pytest.raises(RuntimeError, match="H shape"):
+        RelCISigmaBuilder(s, E, H[:5, :5], V)
+    sb = RelCISigmaBuilder(s, E, H, V, 0)
+    with pytest.raises(RuntimeError, match="not valid"):
+        sb.set_algorithm("fci")
+    with pytest.raises(ValueError):
+        sb.set_memory(-1)
+    sb.set_algorithm("hz")
+    sb.set_memory(0)
+    c = random_complex_vector(s.ndet, 3)
+    with pytest.raises(RuntimeError, match="too small for one complex K-block column of 6 elements"):
+        sb.Hamiltonian(c, np.zeros(s.ndet, dtype=np.complex128))
