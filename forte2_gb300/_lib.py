@@ -36,6 +36,8 @@ def _declare(L):
         "f2g_rel_sigma_apply": (i32, [vp, P, P, i32, vp]),
         "f2g_rel_sigma_hdiag": (i32, [vp, P, vp]),
         "f2g_rel_sigma_element": (i32, [vp, i64, i64, P]),
+        "f2g_rel_rdm_size": (i64, [i32, i32]),
+        "f2g_rel_sigma_rdm": (i32, [vp, i32, P, P, P, vp]),
         "f2g_blocks_enumerate": (i32, [i32, i32, i32, i32, P, P, i32, P, i32, P, P, P, P, P, P, P]),
         "f2g_strings_class_strings": (i32, [vp, i32, P, P]),
         "f2g_strings_block_table": (i32, [vp, P]),

@@ -381,6 +381,57 @@ class RelCISigmaBuilder:
         check(lib().f2g_rel_sigma_element(self.h, int(I), int(J), out.ctypes.data))
         return complex(out[0], out[1])
 
+    _SO_KINDS = {"so_1rdm": 0, "so_2rdm": 1, "so_2cumulant": 2, "so_3rdm": 3, "so_3cumulant": 4}
+
+    def _so_rdm(self, kind, C_left, C_right):
+        """Spin-orbital RDM `kind` between the bra C_left (conjugated) and the ket C_right, complex
+        (rel_ci_sigma_builder_rdm.cc). numpy vectors give a numpy array; CUDA complex128 tensors
+        give a CUDA tensor."""
+        torch = _torch()
+        n = self.lists.norb
+        k = self._SO_KINDS[kind]
+        shape = (n,) * (2, 4, 4, 6, 6)[k]
+        size = int(lib().f2g_rel_rdm_size(n, k))
+        if size < 0:
+            check(-1)
+        device = _is_cuda_tensor(C_left)
+        if device:
+            if not _is_cuda_tensor(C_right):
+                raise TypeError("C_left and C_right must both be CUDA tensors or both numpy arrays")
+            if C_left.dtype != torch.complex128 or C_right.dtype != torch.complex128:
+                raise TypeError("device vectors must be complex128")
+            L, R = C_left.contiguous().view(-1), C_right.contiguous().view(-1)
+        else:
+            L = torch.from_numpy(np.ascontiguousarray(C_left, dtype=np.complex128).reshape(-1)).cuda()
+            R = torch.from_numpy(np.ascontiguousarray(C_right, dtype=np.complex128).reshape(-1)).cuda()
+        if L.numel() != self.lists.ndet or R.numel() != self.lists.ndet:
+            raise RuntimeError("vector length does not match the number of determinants")
+        out = torch.zeros(max(size, 1), dtype=torch.complex128, device="cuda")
+        if self.h is not None:
+            check(lib().f2g_rel_sigma_rdm(self.h, k, L.data_ptr(), R.data_ptr(), out.data_ptr(), stream_handle()))
+        res = out[:size].view(shape)
+        return res if device else res.cpu().numpy()
+
+    def so_1rdm(self, C_left, C_right):
+        """gamma[p][q] = <L| a+_p a_q |R> over spinors (rel_ci_sigma_builder_rdm.cc:14-71)."""
+        return self._so_rdm("so_1rdm", C_left, C_right)
+
+    def so_2rdm(self, C_left, C_right):
+        """gamma[p][q][r][s] = <L| a+_p a+_q a_s a_r |R> (rel_ci_sigma_builder_rdm.cc:73-183)."""
+        return self._so_rdm("so_2rdm", C_left, C_right)
+
+    def so_2cumulant(self, C_left, C_right):
+        """lambda2 = gamma2 - g1[p][r] g1[q][s] + g1[p][s] g1[q][r] (rel_ci_sigma_builder_rdm.cc:185-207)."""
+        return self._so_rdm("so_2cumulant", C_left, C_right)
+
+    def so_3rdm(self, C_left, C_right):
+        """The spin-orbital 3-RDM (n^6) (rel_ci_sigma_builder_rdm.cc:209-365)."""
+        return self._so_rdm("so_3rdm", C_left, C_right)
+
+    def so_3cumulant(self, C_left, C_right):
+        """The spin-orbital 3-cumulant (rel_ci_sigma_builder_rdm.cc:367-404)."""
+        return self._so_rdm("so_3cumulant", C_left, C_right)
+
 
 class CISpinAdapter:
     """CSF <-> determinant transforms (forte2/determinant/ci_spin_adapter.cc:55-288) on the device."""

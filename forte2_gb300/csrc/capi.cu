@@ -440,6 +440,34 @@ int f2g_rel_sigma_element(void* h, int64_t I, int64_t J, double* out) {
     });
 }
 
+int64_t f2g_rel_rdm_size(int nspinor, int kind) {
+    try {
+        if (nspinor < 0 || nspinor > kMaxOrb)
+            throw Error(2, "spin-orbital RDM: need 0 <= nspinor <= 62");
+        return RelSigmaBuilder::rdm_size(nspinor, kind);
+    } catch (const Error& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+int f2g_rel_sigma_rdm(void* h, int kind, const double* CL, const double* CR, double* out, void* stream) {
+    return guard([&] {
+        need(h, "rel sigma");
+        auto* b = static_cast<RelSigmaBuilder*>(h);
+        const int64_t size = RelSigmaBuilder::rdm_size(b->n, kind);
+        if (size == 0)
+            return;
+        need(out, "out");
+        if (b->s->ndet > 0) {
+            need(CL, "CL");
+            need(CR, "CR");
+        }
+        b->rdm(kind, reinterpret_cast<const double2*>(CL), reinterpret_cast<const double2*>(CR),
+               reinterpret_cast<double2*>(out), S(stream));
+    });
+}
+
 int f2g_sigma_reset_build_times(void* sb) {
     return guard([&] {
         need(sb, "sigma");

@@ -100,6 +100,9 @@ struct SigmaBuilder {
     void reset_timers();
 
     SigmaBuilder(CIStrings* s, double E, const double* H, const double* V, int log_level);
+    // A builder without a Hamiltonian: the strings and scratch of the RDM kernels only
+    struct RdmOnly {};
+    SigmaBuilder(CIStrings* s, RdmOnly) : s(s), n(s->norb) {}
     ~SigmaBuilder();
     void set_hamiltonian(double E, const double* H, const double* V);
     void ensure_fp32();

@@ -179,6 +179,14 @@ int f2g_rel_sigma_apply(void* rel_sigma, const double* dev_C, double* dev_sigma,
 int f2g_rel_sigma_hdiag(void* rel_sigma, double* dev_out, void* stream);
 /* slater_rules(dets, I, J) = <I|H|J> into host_out[2] */
 int f2g_rel_sigma_element(void* rel_sigma, int64_t I, int64_t J, double* host_out);
+/* so_1rdm ... so_3cumulant(C_left, C_right) (forte2/ci/rel_ci_sigma_builder_rdm.cc:14-404; binding
+ * api/ci_helpers_api.cc:217-226): kind 0 so_1rdm (n^2), 1 so_2rdm (n^4), 2 so_2cumulant (n^4),
+ * 3 so_3rdm (n^6), 4 so_3cumulant (n^6); complex interleaved, bra conjugated, row-major full
+ * tensors. Vectors and output on the device; f2g_rel_rdm_size gives the complex element count
+ * (-1 and the error text for a bad kind). */
+int64_t f2g_rel_rdm_size(int nspinor, int kind);
+int f2g_rel_sigma_rdm(void* rel_sigma, int kind, const double* dev_CL, const double* dev_CR, double* dev_out,
+                      void* stream);
 
 /* ---- spin adapter: replaces CISpinAdapter(twoS, twoMs, norb) + prepare_couplings(dets)
  *      (forte2/determinant/ci_spin_adapter.cc:55-235; binding api/ci_helpers_api.cc:190-200). */

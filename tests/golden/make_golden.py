@@ -464,6 +464,48 @@ def gen_rel(out):
         json.dump(meta, f, indent=1)
 
 
+# spin-orbital RDM cases: (nspinor, nel, orbital symmetry or None, integral seed, vector seed)
+REL_RDM_CASES = [(6, 3, None, 98, 908), (8, 3, None, 93, 903), (8, 4, [[0, 1, 0, 1, 0, 1, 0, 1]], 97, 907),
+                 (10, 4, None, 94, 904), (4, 1, None, 91, 901), (6, 0, None, 92, 902), (5, 5, None, 99, 909)]
+REL_RDM_SAMPLE = 4096  # sampled entries of a three-body tensor above 6 spinors
+
+
+def gen_rel_rdm(out):
+    """The reference's so_1rdm ... so_3cumulant between two seeded complex vectors (transition
+    RDMs, bra conjugated) and so_1rdm / so_2rdm of one vector with itself. Three-body tensors are
+    stored whole up to 6 spinors; above that, REL_RDM_SAMPLE seeded flat entries and the sum of
+    squared moduli of the whole tensor."""
+    from forte2_gb300.synthetic import make_spinor_integrals, random_complex_vector
+
+    data = {}
+    meta = []
+    for k, (n, ne, orbsym, iseed, cseed) in enumerate(REL_RDM_CASES):
+        E, H, V = make_spinor_integrals(n, iseed)
+        space = (1, orbsym, [], []) if orbsym else (0, [[0] * n], [], [])
+        s = ref.RefCIStrings(ne, 0, *space)
+        sb = ref.RefRelSigmaBuilder(s, E, H, V)
+        key = f"q{k}"
+        cl = random_complex_vector(s.ndet, cseed)
+        cr = random_complex_vector(s.ndet, cseed + 1)
+        entry = dict(key=key, nspinor=n, nel=ne, orbital_symmetry=orbsym, iseed=iseed, cseed=cseed, ndet=s.ndet)
+        for kind in ref.RefRelSigmaBuilder.RDM_KINDS:
+            x = sb.rdm(kind, cl, cr)
+            if kind.startswith("so_3") and n > 6:
+                idx = np.random.default_rng(cseed + 7).integers(0, x.size, size=REL_RDM_SAMPLE)
+                data[f"{key}_{kind}_idx"] = idx
+                data[f"{key}_{kind}"] = x.reshape(-1)[idx]
+                entry[f"{kind}_sumsq"] = float(np.sum(np.abs(x) ** 2))
+            else:
+                data[f"{key}_{kind}"] = x
+        data[f"{key}_so_1rdm_diag"] = sb.rdm("so_1rdm", cl, cl)
+        data[f"{key}_so_2rdm_diag"] = sb.rdm("so_2rdm", cl, cl)
+        meta.append(entry)
+        print("rel rdm", key, s.ndet, flush=True)
+    np.savez_compressed(os.path.join(out, "rel_rdm.npz"), **data)
+    with open(os.path.join(out, "rel_rdm.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
 # MCSCF-style sequence: (na, nb, norb, multiplicity, nroot, integral seed, rotation seeds, theta, e_tol)
 MCSCF_CASES = [(4, 4, 8, 1, 2, 4100, (4111, 4122), 0.05, 1e-10),
                (5, 5, 10, 1, 1, 4200, (4211, 4222), 0.03, 1e-10),
@@ -512,6 +554,7 @@ def main():
              "davidson": lambda: gen_davidson(HERE, a.reference), "rdm": lambda: gen_rdm(HERE),
              "mcscf": lambda: gen_mcscf(HERE, a.reference), "blocks": lambda: gen_blocks(HERE, a.reference),
              "rel": lambda: gen_rel(HERE),
+             "rel_rdm": lambda: gen_rel_rdm(HERE),
              "rdm3": lambda: gen_rdm3(HERE)}
     if a.big:
         steps["big"] = lambda: gen_sigma_checksums(HERE, SIGMA_CHECKSUM_BIG, "sigma_checksums_16.json")

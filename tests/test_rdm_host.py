@@ -138,6 +138,9 @@ def test_pair_list_validation(lib):
     # three-body kinds: (T, T), (P, n, P, n), n^6
     assert lib.f2g_rdm_size(6, 8) == 20 * 20 and lib.f2g_rdm_size(6, 10) == (15 * 6) ** 2
     assert lib.f2g_rdm_size(6, 12) == 6 ** 6 and lib.f2g_rdm_size(2, 9) == 0
+    # spin-orbital (two-component) kinds: full complex tensors n^2, n^4, n^4, n^6, n^6
+    assert [lib.f2g_rel_rdm_size(5, k) for k in range(5)] == [25, 625, 625, 5 ** 6, 5 ** 6]
+    assert lib.f2g_rel_rdm_size(5, 5) == -1 and lib.f2g_rel_rdm_size(-1, 0) == -1
 
 
 def replay_hole_gram(rows_of_K, ncol, CL, CR, d):
