@@ -726,12 +726,20 @@ def run_batched(a):
                                                                       for n in (8, 10, 12)}}}
     for prec in a.precisions.split(","):
         res_b, t_b, rounds = solve_batched(inst, prec)
+        st = {}
+        res_o, t_o, _ = solve_batched(inst, prec, one_launch=True, stats=st)
         res_l, t_l = solve_loop(inst, prec)
         dev = max(max(abs(x - y) for x, y in zip(res_b[i].evals, res_l[i].evals)) for i in range(len(inst)))
+        dev_o = max(max(abs(x - y) for x, y in zip(res_o[i].evals, res_l[i].evals)) for i in range(len(inst)))
         out[prec] = {"batched_s": t_b, "loop_s": t_l, "instances_per_s": len(inst) / t_b,
                      "loop_instances_per_s": len(inst) / t_l, "speedup": t_l / t_b, "rounds": rounds,
                      "all_converged": all(res_b[i].converged for i in range(len(inst))),
-                     "max_abs_dE_batched_vs_loop": dev}
+                     "max_abs_dE_batched_vs_loop": dev,
+                     # every instance's iterations in collective graph launches (one while loop per
+                     # solve inside one graph), set-up on the instances' own streams
+                     "one_launch": {"s": t_o, "instances_per_s": len(inst) / t_o, "speedup": t_l / t_o,
+                                    "all_converged": all(res_o[i].converged for i in range(len(inst))),
+                                    "max_abs_dE_vs_loop": dev_o, **st}}
     print(json.dumps(out), flush=True)
 
 

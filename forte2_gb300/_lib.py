@@ -93,6 +93,11 @@ def _declare(L):
         "f2g_dgraph_state": (i32, [vp, P, P]),
         "f2g_dgraph_ritz": (i32, [vp, P, i64, vp]),
         "f2g_dgraph_history": (i32, [vp, P, i32]),
+        "f2g_dgraph_serial": (i32, [vp, P]),
+        "f2g_dgraph_batch_create": (i32, [P, i32, pp]),
+        "f2g_dgraph_batch_destroy": (i32, [vp]),
+        "f2g_dgraph_batch_launch": (i32, [vp, vp]),
+        "f2g_dgraph_batch_nodes": (i32, [vp, P]),
         "f2g_sigma_set_hamiltonian_async": (i32, [vp, d, P, P, vp]),
         "f2g_probe_dfma": (i32, [i32, i32, i64, P, vp]),
     }

@@ -21,7 +21,9 @@ from math import comb
 
 import numpy as np
 
+from ._lib import check, lib
 from .ci import CASCISolver
+from .davidson import GraphPhase
 from .params import CIParams, DavidsonLiuParams
 from .synthetic import make_integrals
 
@@ -47,10 +49,21 @@ class Job:
 
 
 class StepScheduler:
-    """Event-driven driver of step generators, one CUDA stream per job in flight."""
+    """Event-driven driver of step generators, one CUDA stream per job in flight.
 
-    def __init__(self, nstreams: int = 16, poll_sleep: float = 2e-5):
+    With one_launch=True, jobs whose graph-captured iterations wait for a collective launch
+    (GraphPhase, CASCISolver(one_launch=True)) are parked; when every job in flight is parked, the
+    iterations of all of them run in ONE graph launch (f2g_dgraph_batch_*: one branch per solve,
+    each a device-side while loop that stops at its own convergence), after which they resume."""
+
+    def __init__(self, nstreams: int = 16, poll_sleep: float = 2e-5, one_launch: bool = False):
         torch = _torch()
+        self.one_launch = one_launch
+        self.batch_launches = 0   # collective launches
+        self.batch_solves = 0     # solve phases run inside them
+        self.batch_nodes = 0      # graph nodes of the largest collective launch
+        self._batches = {}        # (serials of the member graphs) -> batch handle
+        self._batch_stream = None
         # free streams by priority class: 0 normal, 1 high (lower CUDA priority value); more are
         # made on demand
         self._free = {0: [torch.cuda.Stream() for _ in range(nstreams)], 1: []}
@@ -90,6 +103,52 @@ class StepScheduler:
                 job.t_done = time.perf_counter()
                 self._free[1 if job.stream.priority < 0 else 0].append(job.stream)
                 return True
+
+    def _launch_parked(self, parked):
+        """One graph launch for the iterations of every parked job; each job resumes when it ends."""
+        import ctypes as C
+
+        torch = _torch()
+        if self._batch_stream is None:
+            self._batch_stream = torch.cuda.Stream()
+        s = self._batch_stream
+        for job in parked:
+            s.wait_event(job.event)  # the job's reset and set-up work comes first
+        handles = [job.request.handle for job in parked]
+        with torch.cuda.stream(s):
+            if len(handles) == 1:
+                check(lib().f2g_dgraph_launch(handles[0], s.cuda_stream))
+            else:
+                serials = []
+                for h in handles:
+                    v = C.c_uint64()
+                    check(lib().f2g_dgraph_serial(h, C.addressof(v)))
+                    serials.append(v.value)
+                key = tuple(serials)
+                b = self._batches.get(key)
+                if b is None:
+                    arr = (C.c_void_p * len(handles))(*[h.value for h in handles])
+                    b = C.c_void_p()
+                    check(lib().f2g_dgraph_batch_create(C.addressof(arr), len(handles), C.byref(b)))
+                    self._batches[key] = b
+                    nodes = C.c_int()
+                    check(lib().f2g_dgraph_batch_nodes(b, C.addressof(nodes)))
+                    self.batch_nodes = max(self.batch_nodes, nodes.value)
+                check(lib().f2g_dgraph_batch_launch(b, s.cuda_stream))
+        ev = torch.cuda.Event()
+        ev.record(s)
+        for job in parked:
+            job.stream.wait_event(ev)
+            job.event = ev
+            job.request = []
+        self.batch_launches += 1
+        self.batch_solves += len(parked)
+
+    def close(self):
+        """Destroy the collective launches' graphs (their member solves must still exist)."""
+        for b in self._batches.values():
+            lib().f2g_dgraph_batch_destroy(b)
+        self._batches = {}
 
     @staticmethod
     def _read(job):
@@ -143,6 +202,9 @@ class StepScheduler:
             still = []
             progressed = False
             for job in active:
+                if isinstance(job.request, GraphPhase):
+                    still.append(job)  # parked until the collective launch
+                    continue
                 if not job.event.query():
                     still.append(job)
                     continue
@@ -156,9 +218,14 @@ class StepScheduler:
                 else:
                     still.append(job)
             active = still
+            parked = [job for job in active if isinstance(job.request, GraphPhase)]
+            if parked and len(parked) == len(active):
+                self._launch_parked(parked)
+                progressed = True
             if not progressed and self.poll_sleep:
                 time.sleep(self.poll_sleep)
         torch.cuda.synchronize()
+        self.close()
         return done
 
 
@@ -180,7 +247,7 @@ def batched_instances(n_inst: int = 64, seed: int = 4000):
 LARGE_NDET = 200_000  # spaces from here on are bound by sigma arithmetic, not by launches
 
 
-def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=2000, autotune=True, ints=None):
+def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=2000, autotune=True, ints=None, one_launch=False):
     """One instance's solver; its sigma kernel variants are autotuned once per shape. Spaces of at
     least LARGE_NDET determinants get the larger Davidson subspace (12 vectors per root, collapse
     to 6, at most 64) in both precisions: the same energies in about a third of the iterations
@@ -192,7 +259,7 @@ def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=2000, autotune=True
         dl = DavidsonLiuParams(e_tol=e_tol, maxiter=maxiter, basis_per_root=bpr, collapse_per_root=min(6, bpr - 1))
     return CASCISolver(norb=inst["norb"], na=inst["na"], nb=inst["nb"], multiplicity=inst["multiplicity"],
                        nroot=inst["nroot"], E=ints.E, H=ints.H, V=ints.V, ci_params=CIParams(precision=precision),
-                       davidson_liu_params=dl, autotune=autotune)
+                       davidson_liu_params=dl, autotune=autotune, one_launch=one_launch)
 
 
 def footprint_bytes(norb: int, na: int, nb: int, nroot: int, basis_per_root: int = 0) -> int:
@@ -212,15 +279,21 @@ def footprint_bytes(norb: int, na: int, nb: int, nroot: int, basis_per_root: int
     return int(ss + det_vectors + csf + davidson + (64 << 20))
 
 
-def solve_batched(instances, precision="fp64", nstreams=16):
-    """Solve all instances concurrently; returns (results by index, seconds, rounds)."""
+def solve_batched(instances, precision="fp64", nstreams=16, one_launch=False, stats=None):
+    """Solve all instances concurrently; returns (results by index, seconds, rounds). With
+    one_launch=True the instances' Davidson iterations run in collective graph launches (one per
+    solve phase: set-up and any host-side steps of each instance stay on its own stream); stats,
+    a dict, receives the scheduler's launch counts."""
     torch = _torch()
-    sched = StepScheduler(nstreams)
+    sched = StepScheduler(nstreams, one_launch=one_launch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    jobs = [(i, make_solver(inst, precision).run_steps()) for i, inst in enumerate(instances)]
+    jobs = [(i, make_solver(inst, precision, one_launch=one_launch).run_steps()) for i, inst in enumerate(instances)]
     done = sched.run(jobs)
     dt = time.perf_counter() - t0
+    if stats is not None:
+        stats.update(batch_launches=sched.batch_launches, batch_solves=sched.batch_solves,
+                     batch_nodes=sched.batch_nodes)
     return {j.key: j.result for j in done}, dt, sched.rounds
 
 

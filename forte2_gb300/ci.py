@@ -63,6 +63,9 @@ class CASCISolver:
     gas_max: list = field(default_factory=list)
     # graph-captured Davidson iterations: None = automatic (small CSF spaces), True/False = force
     use_graph: bool = None
+    # graph-captured iterations wait for a collective launch: run_steps yields GraphPhase and a
+    # StepScheduler(one_launch=True) runs the iterations of many solves in one graph launch
+    one_launch: bool = False
     # cap on the opposite-spin kernel's thread blocks (0 = none); see CISigmaBuilder.set_max_blocks
     sigma_max_blocks: int = 0
     # pick the fastest sigma kernel variants for this shape before solving (forte2_gb300.autotune)
@@ -214,6 +217,7 @@ class CASCISolver:
                                                  energy_shift=self.ci_params.energy_shift,
                                                  log_level=self.log_level, seed=self.seed,
                                                  use_graph=self.use_graph)
+        self.eigensolver.collective = self.one_launch
         self.eigensolver.add_h_diag(hdiag)
         if self.rebuild_guess:
             self._build_guess(hdiag)

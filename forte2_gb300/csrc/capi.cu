@@ -982,6 +982,45 @@ int f2g_dgraph_history(void* g, double* host_out, int count) {
     });
 }
 
+int f2g_dgraph_serial(void* g, uint64_t* out) {
+    return guard([&] {
+        need(g, "dgraph");
+        need(out, "out");
+        *out = static_cast<DavGraph*>(g)->serial;
+    });
+}
+
+int f2g_dgraph_batch_create(void* const* graphs, int count, void** out) {
+    return guard([&] {
+        need(graphs, "graphs");
+        need(out, "out");
+        std::vector<DavGraph*> v((size_t)std::max(count, 0));
+        for (int i = 0; i < count; ++i)
+            v[(size_t)i] = static_cast<DavGraph*>(graphs[i]);
+        auto b = std::make_unique<DavBatch>(v.data(), count);
+        *out = b.release();
+    });
+}
+
+int f2g_dgraph_batch_destroy(void* b) {
+    return guard([&] { delete static_cast<DavBatch*>(b); });
+}
+
+int f2g_dgraph_batch_launch(void* b, void* stream) {
+    return guard([&] {
+        need(b, "dgraph batch");
+        static_cast<DavBatch*>(b)->launch(S(stream));
+    });
+}
+
+int f2g_dgraph_batch_nodes(void* b, int* out) {
+    return guard([&] {
+        need(b, "dgraph batch");
+        need(out, "out");
+        *out = static_cast<DavBatch*>(b)->nodes;
+    });
+}
+
 int f2g_sigma_set_hamiltonian_async(void* sb, double E, const double* H, const double* V, void* stream) {
     return guard([&] {
         need(sb, "sigma");

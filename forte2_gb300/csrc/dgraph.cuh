@@ -15,6 +15,7 @@
 // diagonal and guess written to the same buffers, and dg_reset.
 #pragma once
 
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -66,6 +67,13 @@ inline cudaStream_t capture_stream(std::unique_lock<std::mutex>& lock) {
     return st;
 }
 
+// Serial numbers of captured iteration contents: a new one at creation and whenever the captured
+// work changes (a new defect correction), so a batch built from older contents is never reused.
+inline uint64_t next_graph_serial() {
+    static std::atomic<uint64_t> c{0};
+    return ++c;
+}
+
 struct DavGraph {
     SigmaBuilder* sb;
     SpinAdapter* sa;
@@ -90,6 +98,7 @@ struct DavGraph {
 
     cudaGraphExec_t exec = nullptr;
     std::shared_ptr<int> users; // the sigma builder's count of graphs using its graph scratch
+    uint64_t serial = next_graph_serial();
 
     DavGraph(SigmaBuilder* sb_, SpinAdapter* sa_, const DGParams& p, int iters_, double* b_, double* sigma_, double* r_,
              double* tmp_, int64_t ld_, int64_t ldr_, int64_t ldt_, const double* hdiag_)
@@ -149,6 +158,7 @@ struct DavGraph {
             cB.reserve((size_t)k * R);
         }
         drop();
+        serial = next_graph_serial();
     }
 
     void drop() {
@@ -256,6 +266,8 @@ struct DavGraph {
         F2G_CUDA(cudaGraphLaunch(exec, s));
     }
 
+    const DGState* state_dev() const { return st.get(); }
+
     void ritz(double* out, int64_t ldo, cudaStream_t s) { dg_ritz(st.get(), P, b, ld, V.get(), P.maxm, out, ldo, s); }
 
     void history(double* host_out, int count) {
@@ -264,6 +276,30 @@ struct DavGraph {
         if (count)
             F2G_CUDA(cudaMemcpy(host_out, hist.get(), (size_t)4 * count * sizeof(double), cudaMemcpyDeviceToHost));
     }
+};
+
+// Many solves' iterations in ONE graph launch. The parent graph holds one branch per solve: a
+// memset of the branch's loop counter, then a conditional WHILE node whose body is one captured
+// iteration of that solve followed by k_dg_continue, which keeps the loop going while the solve's
+// state says it is running (and the counter is below the iteration limit + 2, so every loop ends
+// even if a state were never set), then a copy of the state to the solve's pinned host slot.
+// Branches are independent, so the solves run concurrently and each stops at its own
+// convergence; the launch ends when the last one has stopped. The solves must use distinct sigma
+// builders (each branch uses its builder's scratch).
+struct DavBatch {
+    std::vector<DavGraph*> g;
+    std::vector<uint64_t> serials;
+    DevBuf<int32_t> loops;
+    cudaGraphExec_t exec = nullptr;
+    int nodes = 0; // kernel, memset and memcpy nodes captured (for reporting)
+
+    DavBatch(DavGraph* const* graphs, int count);
+    ~DavBatch() {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+    }
+    void build();
+    void launch(cudaStream_t s);
 };
 
 } // namespace f2g

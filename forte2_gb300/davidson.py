@@ -54,12 +54,27 @@ def to_device(a):
     return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).pin_memory().to("cuda", non_blocking=True)
 
 
+class GraphPhase:
+    """Yielded by a graph-captured solve whose iterations wait for a collective launch: a
+    scheduler launches the iterations of all waiting solves in one graph (f2g_dgraph_batch_*);
+    resumed with [] once that launch has completed."""
+
+    __slots__ = ("handle",)
+
+    def __init__(self, handle):
+        self.handle = handle
+
+
 def drive(gen):
-    """Run a step generator to completion on the current stream; returns its return value."""
+    """Run a step generator to completion on the current stream; returns its return value. A
+    GraphPhase is launched alone."""
     torch = _torch()
     try:
         req = next(gen)
         while True:
+            if isinstance(req, GraphPhase):
+                check(lib().f2g_dgraph_launch(req.handle, stream_handle()))
+                req = []
             torch.cuda.current_stream().synchronize()
             req = gen.send([t.cpu().numpy() for t in req])
     except StopIteration as e:
@@ -133,6 +148,8 @@ class DavidsonLiuSolver:
         self._graphs = {}
         self._tmp2 = None
         self.used_graph = False
+        # graph iterations wait for a collective launch (GraphPhase) instead of launching themselves
+        self.collective = False
         self._G = None  # subspace matrix B S^T, valid for the first _g_size rows and columns
         self._g_size = 0
 
@@ -431,8 +448,12 @@ class DavidsonLiuSolver:
         ints = np.zeros(8, dtype=np.int32)
         dbl = np.zeros(131, dtype=np.float64)
         while True:
-            check(L.f2g_dgraph_launch(g, stream_handle()))
-            yield []
+            if self.collective:
+                # the scheduler launches the iterations of every waiting solve in one graph
+                yield GraphPhase(g)
+            else:
+                check(L.f2g_dgraph_launch(g, stream_handle()))
+                yield []
             check(L.f2g_dgraph_state(g, ints.ctypes.data, dbl.ctypes.data))
             if ints[3] != 0:
                 break

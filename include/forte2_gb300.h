@@ -298,6 +298,18 @@ int f2g_dgraph_state(void* dgraph, int32_t* host_ints8, double* host_doubles131)
 int f2g_dgraph_ritz(void* dgraph, double* dev_out, int64_t ldo, void* stream);
 /* Per-iteration {mean root energy, max |dE|, max |r|, basis size} of the current solve (blocking). */
 int f2g_dgraph_history(void* dgraph, double* host_out, int count);
+/* Many solves in ONE graph launch (batched CASCI, no reference counterpart: the reference solves
+ * instances one after the other). The batch graph has one branch per dgraph: a conditional WHILE
+ * node whose body is one iteration of that solve, looping until its state stops (or its
+ * maxiter_cap + 2 loops), then the state copy to its host slot. Every dgraph must be reset first
+ * and use its own sigma builder. f2g_dgraph_serial changes when a dgraph's captured work changes
+ * (f2g_dgraph_set_correction); a batch launch rebuilds itself when one of its serials changed.
+ * f2g_dgraph_batch_nodes: nodes captured into the batch. */
+int f2g_dgraph_serial(void* dgraph, uint64_t* host_out);
+int f2g_dgraph_batch_create(void* const* dgraphs, int count, void** out);
+int f2g_dgraph_batch_destroy(void* batch);
+int f2g_dgraph_batch_launch(void* batch, void* stream);
+int f2g_dgraph_batch_nodes(void* batch, int* host_out);
 /* set_hamiltonian ordered on a stream, with no device-wide synchronisation; buffers keep their
  * addresses for the same orbital count, so graphs captured on this builder stay valid. */
 int f2g_sigma_set_hamiltonian_async(void* sigma, double E, const double* host_H, const double* host_V,

@@ -21,6 +21,48 @@ def test_batched_equals_loop(cuda):
         np.testing.assert_allclose(batched[i].evals, loop[i].evals, rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_one_launch_batch_equals_solo(cuda, precision):
+    """The instances' Davidson iterations in collective graph launches (one conditional while loop
+    per solve in one graph): every instance converges to the energies of its solo solve, which
+    runs the same kernels in the same order (1e-12 Eh)."""
+    from forte2_gb300.batch import batched_instances, make_solver, solve_batched
+
+    inst = batched_instances(6, seed=12)
+    for x in inst:
+        x["norb"] = min(x["norb"], 8)
+        x["na"] = x["nb"] = x["norb"] // 2
+    stats = {}
+    res, _, _ = solve_batched(inst, precision, nstreams=4, one_launch=True, stats=stats)
+    assert stats["batch_launches"] >= 1 and stats["batch_solves"] >= len(inst) and stats["batch_nodes"] > 0
+    for i, x in enumerate(inst):
+        solo = make_solver(x, precision).run()
+        assert res[i].converged and solo.converged
+        np.testing.assert_allclose(res[i].evals, solo.evals, rtol=0, atol=1e-12)
+
+
+def test_one_launch_batch_rejects_a_shared_sigma_builder(cuda):
+    import ctypes as C
+
+    import torch
+
+    from forte2_gb300._lib import lib
+    from forte2_gb300.batch import make_solver
+    from forte2_gb300.davidson import GraphPhase
+
+    x = dict(norb=6, na=3, nb=3, multiplicity=1, nroot=1, iseed=5)
+    solver = make_solver(x, "fp64", one_launch=True)
+    gen = solver.run_steps()
+    req = next(gen)
+    while not isinstance(req, GraphPhase):
+        torch.cuda.synchronize()
+        req = gen.send([t.cpu().numpy() for t in req])
+    arr = (C.c_void_p * 2)(req.handle.value, req.handle.value)
+    b = C.c_void_p()
+    assert lib().f2g_dgraph_batch_create(C.addressof(arr), 2, C.byref(b)) == 2
+    assert "own sigma builder" in lib().f2g_last_error().decode()
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
 def test_serving_results_equal_solo(cuda, precision, tol):
     from forte2_gb300.batch import make_solver
