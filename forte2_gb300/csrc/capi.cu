@@ -495,9 +495,16 @@ int f2g_sigma_set_variant(void* sb, int which, int value) {
             F2G_CUDA(cudaMemset(b->tc_err.get(), 0, sizeof(int)));
         } else if (which == 4)
             b->use_sym = value != 0;
-        else
+        else if (which == 5) {
+            b->use_tma_b = value != 0;
+            if (b->use_tma_b && b->precision == kFP32) {
+                b->prepare_tma_b(0);
+                F2G_CUDA(cudaStreamSynchronize(0));
+            }
+        } else
             throw Error(2, "variant must be 0 (tensor cores), 1 (narrow same-spin tiles), 2 (persistent opposite "
-                           "grid), 3 (tensor-core wait limit) or 4 (irrep-aware opposite-spin kernel)");
+                           "grid), 3 (tensor-core wait limit), 4 (irrep-aware opposite-spin kernel) or 5 "
+                           "(TMA-fed tensor-core B tiles)");
     });
 }
 

@@ -45,10 +45,15 @@
 // sets the error flag and the CTA leaves its loops, waits (bounded again) for the MMAs it has
 // committed and releases its tensor memory. An error flag of 1 means that the sigma of that call
 // is not valid.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
 #include <cmath>
 #include <cstdint>
+#include <memory>
+#include <mutex>
+#include <string>
 
 #include "sigma.cuh"
 
@@ -185,7 +190,7 @@ struct TcShared {
     const float* rowp[kTcMaxK]; // row of C of alpha excitation k
     float sfa[kTcMaxK];         // its sign times the C scale 2^ea
     int pk[kTcMaxK], qk[kTcMaxK];
-    alignas(8) uint64_t a_full, a_empty, acc_full[2], acc_empty[2];
+    alignas(8) uint64_t a_full, a_empty, b_full, acc_full[2], acc_empty[2];
     uint32_t tmem_base;
     volatile int abort;
 };
@@ -205,7 +210,55 @@ __device__ __forceinline__ void split_store(const float (&x)[8], __half* hi_dst,
     *reinterpret_cast<uint4*>(lo_dst) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// B = V'[(s, r)][k] 2^eb of the K excitations (pk[k], qk[k]) of one alpha string (zero outside the
+// space), K-major core matrices, by the threads of one block
+__device__ __forceinline__ void build_b(int n, int K, int kp, float fb, const float* __restrict__ V, const int* pk,
+                                        const int* qk, __half* b_hi, __half* b_lo, int tid, int nthreads) {
+    for (int t = tid; t < kTcN * (kp >> 3); t += nthreads) {
+        const int nn = t / (kp >> 3), k0 = (t % (kp >> 3)) * 8;
+        const int s = nn >> 4, r = nn & 15;
+        float x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int kk = k0 + j;
+            x[j] = (kk < K && s < n && r < n) ? fb * V[(((size_t)pk[kk] * n + r) * n + qk[kk]) * n + s] : 0.0f;
+        }
+        const uint32_t off = kmajor_off(nn, k0, kp) >> 1;
+        split_store(x, b_hi + off, b_lo + off);
+    }
+}
+
+// 2D tensor copy of one box into shared memory, completing on an mbarrier (transaction bytes)
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t mbar) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+                 : "memory");
+}
+
 } // namespace
+
+// The B operands of every alpha string (the tensor-core kernel's B tiles, fed to it by TMA):
+// out[Ja] = {hi, lo}, each kTcN * kp halves in the kernel's shared-memory layout.
+__global__ void k_build_bops(int n, int na, int ma, int64_t N0a, const uint32_t* __restrict__ down_a,
+                             const uint32_t* __restrict__ up_a, const float* __restrict__ V,
+                             const unsigned int* __restrict__ vmax, __half* __restrict__ out) {
+    __shared__ int pk[kTcMaxK], qk[kTcMaxK];
+    const int K = na * ma, kp = (K + 15) & ~15;
+    const float fb = pow2f(split_exponent(__uint_as_float(vmax[0])));
+    for (int64_t Ja = blockIdx.x; Ja < N0a; Ja += gridDim.x) {
+        __syncthreads(); // the previous string's excitations are no longer read
+        if ((int)threadIdx.x < K) {
+            const int pi = threadIdx.x / ma, qi = threadIdx.x % ma;
+            const uint32_t ep = down_a[Ja * na + pi];
+            const uint32_t eq = up_a[(int64_t)e_addr(ep) * ma + qi];
+            pk[threadIdx.x] = e_orb(ep);
+            qk[threadIdx.x] = e_orb(eq);
+        }
+        __syncthreads();
+        __half* hi = out + (size_t)Ja * 2 * kTcN * kp;
+        build_b(n, K, kp, fb, V, pk, qk, hi, hi + (size_t)kTcN * kp, threadIdx.x, blockDim.x);
+    }
+}
 
 // exc[Ib][i][r] for the i-th occupied orbital s of Ib and r < 16: Jb | negative << 31 for the beta
 // string Jb = Ib - s + r (r not in Ib - s), 0x00FFFFFF otherwise.
@@ -264,7 +317,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                   const uint32_t* __restrict__ exc_b, const float* __restrict__ V,
                   const unsigned int* __restrict__ vmax, const unsigned int* __restrict__ cmax,
                   const float* __restrict__ C, float* __restrict__ sig, int* __restrict__ err,
-                  long long poll_limit) {
+                  long long poll_limit, const __grid_constant__ CUtensorMap bmap, int tma_b) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TcShared& sh = *reinterpret_cast<TcShared*>(smem_raw);
     // sigma(Ja, :) in fixed point: high and low 32-bit parts, N0b elements each
@@ -282,7 +335,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int eb = split_exponent(__uint_as_float(vmax[0]));
     const float fa = pow2f(ea), fb = pow2f(eb);
     const float unscale0 = pow2f(-7), unscale1 = pow2f(-ea), unscale2 = pow2f(-eb);
-    const uint32_t a_full = smem_u32(&sh.a_full), a_empty = smem_u32(&sh.a_empty);
+    const uint32_t a_full = smem_u32(&sh.a_full), a_empty = smem_u32(&sh.a_empty), b_full = smem_u32(&sh.b_full);
     const uint32_t acc_full[2] = {smem_u32(&sh.acc_full[0]), smem_u32(&sh.acc_full[1])};
     const uint32_t acc_empty[2] = {smem_u32(&sh.acc_empty[0]), smem_u32(&sh.acc_empty[1])};
     const uint32_t lbo = 128, sbo = (uint32_t)(kp >> 3) * 128;
@@ -290,6 +343,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (tid == 0) {
         mbar_init(a_full, kProdWarps * 32);
         mbar_init(a_empty, 1);
+        mbar_init(b_full, 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(acc_full[b], 1);
             mbar_init(acc_empty[b], kScatWarps);
@@ -315,6 +369,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
     long long g0 = 0;      // tiles of this CTA before the current alpha string
     long long last_g = -1; // MMA thread: last tile whose MMAs were committed
+    uint32_t b_phase = 0;   // thread 0: parity of the b_full phase of the last B copy issued
+    bool b_pending = false; // thread 0: a B copy was issued and its completion not yet seen
+    int nja = 0;            // alpha strings of this CTA so far
     for (int64_t Ja = blockIdx.x; Ja < N0a && !sh.abort; Ja += gridDim.x) {
         float* srow = sig + Ja * (int64_t)N0b;
         // ---- alpha string set-up (all warps): excitations k = pi * ma + qi, B, zero row
@@ -334,24 +391,29 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         for (int c = tid; c < N0b; c += kTcThreads)
             row_hi[c] = row_lo[c] = 0;
-        __syncthreads();
-        // B = V'[(s, r)][k] 2^eb (zero outside the space); one 16-byte row of 8 k per task
-        for (int t = tid; t < kTcN * (kp >> 3); t += kTcThreads) {
-            const int nn = t / (kp >> 3), k0 = (t % (kp >> 3)) * 8;
-            const int s = nn >> 4, r = nn & 15;
-            float x[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int kk = k0 + j;
-                x[j] = (kk < K && s < n && r < n) ? fb * V[(((size_t)sh.pk[kk] * n + r) * n + sh.qk[kk]) * n + s]
-                                                  : 0.0f;
+        if (tma_b) {
+            // B of Ja from the prebuilt operands (k_build_bops): two boxes of kp rows x 256 halves,
+            // copied by TMA while the producers gather the first A tile; the MMA thread waits for
+            // them. The previous string's MMAs are complete (every tile was scattered).
+            if (tid == 0) {
+                const uint32_t bytes = 2u * kTcN * (uint32_t)kp * 2u;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b_full), "r"(bytes)
+                             : "memory");
+                const int y = (int)(Ja * 2 * kp);
+                tma_load_2d(smem_u32(sh.b_hi), &bmap, 0, y, b_full);
+                tma_load_2d(smem_u32(sh.b_lo), &bmap, 0, y + kp, b_full);
+                b_phase = (uint32_t)(nja & 1);
+                b_pending = true;
             }
-            const uint32_t off = kmajor_off(nn, k0, kp) >> 1;
-            split_store(x, sh.b_hi + off, sh.b_lo + off);
+            __syncthreads();
+        } else {
+            __syncthreads();
+            // B = V'[(s, r)][k] 2^eb (zero outside the space); one 16-byte row of 8 k per task
+            build_b(n, K, kp, fb, V, sh.pk, sh.qk, sh.b_hi, sh.b_lo, tid, kTcThreads);
+            // make the generic-proxy shared-memory writes visible to the tensor cores
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
         }
-        // make the generic-proxy shared-memory writes visible to the tensor cores
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
 
         if (warp < kProdWarps) {
             // ---- producer: half h of row m of A (k in [40 h, 40 h + 40)) for every tile of Ja
@@ -393,6 +455,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         (g >= 2 && !mbar_wait(acc_empty[buf], (uint32_t)(((g >> 1) - 1) & 1), poll_limit, &sh.abort))) {
                         give_up();
                         break;
+                    }
+                    if (b_pending) { // the B tiles of this alpha string have landed
+                        if (!mbar_wait(b_full, b_phase, poll_limit, &sh.abort)) {
+                            give_up();
+                            break;
+                        }
+                        b_pending = false;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t ahi = smem_u32(sh.a_hi), alo = smem_u32(sh.a_lo);
@@ -489,8 +558,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 srow[c] += x;
             }
         g0 += ntile;
+        ++nja;
         __syncthreads();
     }
+    // a B copy still in flight after an abort lands before the CTA leaves (bounded wait)
+    if (tid == 0 && b_pending)
+        (void)mbar_wait(b_full, b_phase, (1ll << 26));
     // after an abort, MMAs may still be running: wait (bounded) for the last commit before the tensor
     // memory they write is released (a no-op when every tile was scattered)
     if (tid == 0 && last_g >= 0)
@@ -504,6 +577,64 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 size_t opposite_tc_smem(int N0b) { return sizeof(TcShared) + (size_t)N0b * 2 * sizeof(int); }
+
+// The prebuilt B operands of every alpha string and the tensor map the kernel's TMA copies read:
+// a 2D FP16 tensor of rows of kTcN halves (512 B), 2 kp rows per alpha string (hi, then lo).
+struct TcBOperands {
+    CUtensorMap map{};
+    DevBuf<uint16_t> buf;
+    int kp = 0;
+    int64_t N0a = 0;
+};
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// (Re)build the B operands for the integrals V (FP32) and their largest magnitude vmax, on st. The
+// first call allocates them (N0a x 2 x kTcN x kp halves: 1.05 GB at CAS(16,16)) and encodes the
+// tensor map; later calls (new integrals) refill the same buffer, so captured graphs stay valid.
+void opposite_tc_build_b(const CIStrings* s, const float* V, const unsigned int* vmax,
+                         std::shared_ptr<TcBOperands>& tb, cudaStream_t st) {
+    const int na = s->na, ma = s->a.m1, K = na * ma, kp = (K + 15) & ~15;
+    const int64_t N0a = s->a.N0;
+    if (!tb) {
+        PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+        if (!encode)
+            throw Error(3, "tensor-core sigma: the driver offers no cuTensorMapEncodeTiled");
+        auto t = std::make_shared<TcBOperands>();
+        t->kp = kp;
+        t->N0a = N0a;
+        t->buf.reserve((size_t)N0a * 2 * kTcN * kp);
+        const cuuint64_t dims[2] = {(cuuint64_t)kTcN, (cuuint64_t)N0a * 2 * kp};
+        const cuuint64_t strides[1] = {(cuuint64_t)kTcN * sizeof(uint16_t)};
+        const cuuint32_t box[2] = {(cuuint32_t)kTcN, (cuuint32_t)kp};
+        const cuuint32_t estr[2] = {1, 1};
+        const CUresult r = encode(&t->map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, t->buf.get(), dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            throw Error(3, "tensor-core sigma: cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+        tb = t;
+    }
+    if (tb->kp != kp || tb->N0a != N0a)
+        throw Error(1, "tensor-core sigma: B operands of another space");
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(N0a, 1216));
+    k_build_bops<<<grid, 256, 0, st>>>(s->norb, na, ma, N0a, s->a.down1.get(), s->a.up1.get(), V, vmax,
+                                       reinterpret_cast<__half*>(tb->buf.get()));
+    F2G_LAUNCH("k_build_bops");
+}
 
 bool opposite_tc_supported(const CIStrings* s) {
     const int n = s->norb;
@@ -533,9 +664,10 @@ void opposite_tc_vmax(const float* V, int64_t count, unsigned int* vmax, cudaStr
 
 // vmax: the integrals' largest magnitude (opposite_tc_vmax); cmax: nvec words of scratch for the
 // per-vector largest |C|, written here before the kernel runs.
+// tb: the prebuilt B operands (TMA-fed B tiles), or nullptr (each CTA builds B itself; same sigma).
 void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, const unsigned int* vmax,
                         const float* C, float* sig, unsigned int* cmax, int* err, long long poll_limit, int max_ctas,
-                        cudaStream_t st, int nvec) {
+                        cudaStream_t st, int nvec, const TcBOperands* tb) {
     const int64_t nd = s->a.N0 * s->b.N0;
     F2G_CUDA(cudaMemsetAsync(cmax, 0, (size_t)nvec * sizeof(unsigned int), st));
     k_absmax<<<dim3(256, (unsigned)nvec), 256, 0, st>>>(nd, C, cmax);
@@ -550,7 +682,8 @@ void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V,
         gx = std::min<int64_t>(gx, max_ctas);
     k_opposite_tc<<<dim3((unsigned)gx, (unsigned)nvec), kTcThreads, smem, st>>>(
         s->norb, s->na, s->nb, s->a.m1, s->a.N0, (int)s->b.N0, s->a.down1.get(), s->a.up1.get(), s->b.str.get(), exc,
-        V, vmax, cmax, C, sig, err, poll_limit > 0 ? poll_limit : (1ll << 26));
+        V, vmax, cmax, C, sig, err, poll_limit > 0 ? poll_limit : (1ll << 26), tb ? tb->map : CUtensorMap{},
+        tb ? 1 : 0);
     F2G_LAUNCH("k_opposite_tc");
 }
 

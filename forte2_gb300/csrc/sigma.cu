@@ -589,7 +589,9 @@ void build_beta_exc(const CIStrings* s, DevBuf<uint32_t>& exc, cudaStream_t st);
 void opposite_tc_vmax(const float* V, int64_t count, unsigned int* vmax, cudaStream_t st);
 void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V, const unsigned int* vmax,
                         const float* C, float* sig, unsigned int* cmax, int* err, long long poll_limit, int max_ctas,
-                        cudaStream_t st, int nvec);
+                        cudaStream_t st, int nvec, const TcBOperands* tb);
+void opposite_tc_build_b(const CIStrings* s, const float* V, const unsigned int* vmax,
+                         std::shared_ptr<TcBOperands>& tb, cudaStream_t st);
 
 SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const double* V_, int ll)
     : s(s_), n(s_->norb), log_level(ll) {
@@ -736,7 +738,19 @@ void build_ss_values(int n, int k, int64_t N0, int nnz, const uint64_t* str, con
 }
 
 // FP32 copies of the string-Hamiltonian values, made once per set of integrals on first use.
+// The TMA-fed B operands of the tensor-core kernel, when it is in use and they are not current.
+void SigmaBuilder::prepare_tma_b(cudaStream_t st) {
+    if (!use_tc || !use_tma_b || !tensor_cores_available() || tc_b_ready)
+        return;
+    opposite_tc_build_b(s, fV.get(), tc_vmax.get(), tc_b, st);
+    tc_b_ready = true;
+}
+
 void SigmaBuilder::ensure_fp32() {
+    if (!tc_b_ready && use_tc && use_tma_b && tensor_cores_available()) {
+        prepare_tma_b(0);
+        F2G_CUDA(cudaStreamSynchronize(0)); // built on the legacy stream: wait for it alone
+    }
     if (fp32_ready)
         return;
     for (StringHamiltonian* sh : {&ha, &hb}) {
@@ -807,6 +821,9 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
     }
     if (tc_vmax.get())
         opposite_tc_vmax(fV.get(), (int64_t)V.size(), tc_vmax.get(), 0);
+    tc_b_ready = false;
+    if (tc_b) // built before: refilled in place for the new integrals
+        prepare_tma_b(0);
     build_string_hamiltonian(0, ha, true, 0);
     build_string_hamiltonian(1, hb, false, 0);
     build_local_ss(0);
@@ -836,6 +853,9 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
     }
     if (tc_vmax.get())
         opposite_tc_vmax(fV.get(), (int64_t)V.size(), tc_vmax.get(), st);
+    tc_b_ready = false;
+    if (tc_b) // built before: refilled in place, in stream order, so captured graphs follow
+        prepare_tma_b(st);
     build_string_hamiltonian(0, ha, true, st);
     build_string_hamiltonian(1, hb, false, st);
     build_local_ss(st);
@@ -1124,7 +1144,7 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
                 // direct call on the same builder never share it
                 unsigned int* cmax = tc_cmax.get() + (graph ? 65536 : 0);
                 launch_opposite_tc(s, beta_exc.get(), Vt, tc_vmax.get(), C, sig, cmax, tc_err.get(), tc_poll_limit,
-                                   max_ctas, st, nvec);
+                                   max_ctas, st, nvec, (use_tma_b && tc_b_ready) ? tc_b.get() : nullptr);
                 done = true;
             }
         }

@@ -66,6 +66,12 @@ struct SigmaBuilder {
     void build_local_ss(cudaStream_t st);
     bool blocked_sym_path() const;
     void run_blocked_sym(const double* C, double* S, cudaStream_t st, int nvec, bool timed, bool graph);
+    // the tensor-core kernel's B tiles prebuilt for every alpha string and fed to it by TMA
+    // (k_build_bops, rebuilt with the integrals); off: each CTA builds B itself (same sigma)
+    bool use_tma_b = true;
+    bool tc_b_ready = false;
+    std::shared_ptr<struct TcBOperands> tc_b;
+    void prepare_tma_b(cudaStream_t st);
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
     DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
     DevBuf<unsigned int> tc_cmax; // per-vector largest |C| of a tensor-core launch (its operand scale)

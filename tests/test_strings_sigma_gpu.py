@@ -288,6 +288,23 @@ def test_fp32_tensor_core_opposite_spin(cuda, na, nb, n):
         e_tc = rel(tc[i].cpu().numpy(), ref[i].cpu().numpy())
         e_cc = rel(cc[i].cpu().numpy(), ref[i].cpu().numpy())
         assert e_tc < 2e-6 and e_tc < 3 * e_cc + 1e-7
+    # the B tiles fed by TMA from the prebuilt operands (default) and built by each CTA give the
+    # same bits, also after new integrals (the operands are rebuilt in place, in stream order)
+    sb.set_variant("tma_b", False)
+    own = torch.empty_like(c)
+    sb.Hamiltonian(c, own)
+    assert torch.equal(own, tc)
+    sb.set_variant("tma_b", True)
+    ints2 = make_integrals(n, 700 + n)
+    for update in (sb.update_integrals, sb.set_Hamiltonian):
+        update(ints2.E, ints2.H, ints2.V)
+        t1, t2 = torch.empty_like(c), torch.empty_like(c)
+        sb.Hamiltonian(c, t1)
+        sb.set_variant("tma_b", False)
+        sb.Hamiltonian(c, t2)
+        sb.set_variant("tma_b", True)
+        assert sb.tensor_core_error() == 0
+        assert torch.equal(t1, t2) and not torch.equal(t1, tc)
 
 
 @pytest.mark.parametrize("precision,n", [("fp64", 12), ("fp32", 12), ("fp32", 14)])
