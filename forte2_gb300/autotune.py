@@ -4,7 +4,8 @@ code path).
 
 Variants: the same-spin kernel's columns per thread (default or half), the opposite-spin grid
 (one thread block per alpha string, or one per SM looping over them), and in FP32 the
-opposite-spin term on the tensor cores or the CUDA cores. Each candidate builds sigma for one
+opposite-spin term on the tensor cores or the CUDA cores and the same-spin terms as sparse row
+products or dense tensor-core GEMMs. Each candidate builds sigma for one
 seeded vector `reps` times after a warm-up; times come from CUDA events on the current stream.
 Choices are cached per (norb, na, nb, precision) for the process, so a pool of solvers of one
 shape tunes once.
@@ -34,6 +35,15 @@ def candidates(sb, precision):
     opts = {"narrow_same_spin": (0, 1), "persistent_opposite": (0, 1)}
     if precision == "fp32" and sb.set_tensor_cores(True):
         opts["tensor_cores"] = (1, 0)
+    if precision == "fp32":
+        # same-spin terms as dense tensor-core GEMMs, where the space allows them
+        try:
+            sb.set_variant("dense_same_spin", 0)
+            sb.set_variant("dense_same_spin", 1)
+            opts["dense_same_spin"] = (0, 1)
+        except ValueError:
+            pass
+        sb.set_variant("dense_same_spin", 0)
     names = list(opts)
     return [dict(zip(names, vals)) for vals in itertools.product(*(opts[n] for n in names))]
 

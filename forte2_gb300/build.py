@@ -65,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc, "-shared", *ARCH, "-o", LIB_PATH, *objs, "-lcudart"]
+        cmd = [nvcc, "-shared", *ARCH, "-o", LIB_PATH, *objs, "-lcudart", "-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

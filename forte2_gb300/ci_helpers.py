@@ -564,7 +564,7 @@ class CISigmaBuilder:
         return bool(avail[0])
 
     _VARIANTS = {"tensor_cores": 0, "narrow_same_spin": 1, "persistent_opposite": 2, "tc_wait_limit": 3,
-                 "irrep_blocks": 4, "tma_b": 5}
+                 "irrep_blocks": 4, "tma_b": 5, "dense_same_spin": 6}
 
     def set_variant(self, name, value):
         """Select a kernel variant with identical results (see forte2_gb300.autotune)."""

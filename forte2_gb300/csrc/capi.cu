@@ -501,10 +501,16 @@ int f2g_sigma_set_variant(void* sb, int which, int value) {
                 b->prepare_tma_b(0);
                 F2G_CUDA(cudaStreamSynchronize(0));
             }
+        } else if (which == 6) {
+            if (value && !b->dense_ss_supported())
+                throw Error(2, "dense same-spin GEMMs need at most 4096 strings per spin");
+            b->use_dense_ss = value != 0;
+            if (b->use_dense_ss && b->precision == kFP32)
+                b->ensure_fp32();
         } else
             throw Error(2, "variant must be 0 (tensor cores), 1 (narrow same-spin tiles), 2 (persistent opposite "
-                           "grid), 3 (tensor-core wait limit), 4 (irrep-aware opposite-spin kernel) or 5 "
-                           "(TMA-fed tensor-core B tiles)");
+                           "grid), 3 (tensor-core wait limit), 4 (irrep-aware opposite-spin kernel), 5 "
+                           "(TMA-fed tensor-core B tiles) or 6 (FP32 same-spin terms as dense GEMMs)");
     });
 }
 

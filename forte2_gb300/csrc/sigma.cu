@@ -592,6 +592,11 @@ void launch_opposite_tc(const CIStrings* s, const uint32_t* exc, const float* V,
                         cudaStream_t st, int nvec, const TcBOperands* tb);
 void opposite_tc_build_b(const CIStrings* s, const float* V, const unsigned int* vmax,
                          std::shared_ptr<TcBOperands>& tb, cudaStream_t st);
+void dense_ss_build(const CIStrings* s, const StringHamiltonian* sh[2], std::shared_ptr<DenseSameSpin>& d,
+                    cudaStream_t st);
+void dense_ss_split(const CIStrings* s, DenseSameSpin& d, const float* C, int nvec, int set, cudaStream_t st);
+void dense_ss_term(const CIStrings* s, DenseSameSpin& d, float* sig, int spin, bool accumulate, int nvec, int set,
+                   cudaStream_t st);
 
 SigmaBuilder::SigmaBuilder(CIStrings* s_, double E_, const double* H_, const double* V_, int ll)
     : s(s_), n(s_->norb), log_level(ll) {
@@ -746,13 +751,32 @@ void SigmaBuilder::prepare_tma_b(cudaStream_t st) {
     tc_b_ready = true;
 }
 
+bool SigmaBuilder::dense_ss_supported() const {
+    return s->a.N0 <= kDenseSsMaxStrings && s->b.N0 <= kDenseSsMaxStrings && s->a.N0 * s->b.N0 > 0;
+}
+
+// The dense split string Hamiltonians, when the dense same-spin GEMMs are in use and they are not
+// current (needs the FP32 rows).
+void SigmaBuilder::prepare_dense_ss(cudaStream_t st) {
+    if (!use_dense_ss || dss_ready || !fp32_ready)
+        return;
+    const StringHamiltonian* sh[2] = {&ha, &hb};
+    dense_ss_build(s, sh, dss, st);
+    dss_ready = true;
+}
+
 void SigmaBuilder::ensure_fp32() {
     if (!tc_b_ready && use_tc && use_tma_b && tensor_cores_available()) {
         prepare_tma_b(0);
         F2G_CUDA(cudaStreamSynchronize(0)); // built on the legacy stream: wait for it alone
     }
-    if (fp32_ready)
+    if (fp32_ready) {
+        if (use_dense_ss && !dss_ready) {
+            prepare_dense_ss(0);
+            F2G_CUDA(cudaStreamSynchronize(0));
+        }
         return;
+    }
     for (StringHamiltonian* sh : {&ha, &hb}) {
         const int s_ = sh == &ha ? 0 : 1;
         const size_t total = (size_t)s->spin(s_).N0 * sh->nnz;
@@ -765,6 +789,10 @@ void SigmaBuilder::ensure_fp32() {
     }
     F2G_CUDA(cudaStreamSynchronize(0)); // the conversions ran on the legacy stream: wait for them alone
     fp32_ready = true;
+    if (use_dense_ss && !dss_ready) {
+        prepare_dense_ss(0);
+        F2G_CUDA(cudaStreamSynchronize(0));
+    }
 }
 
 // The grouped layout of one spin's FP32 string Hamiltonian, for spaces of kSsGroupMinRows strings
@@ -829,8 +857,9 @@ void SigmaBuilder::set_hamiltonian(double E_, const double* H_, const double* V_
     build_local_ss(0);
     F2G_CUDA(cudaStreamSynchronize(0)); // set-up ran on the legacy stream: wait for it alone
     fp32_ready = false;
-    if (precision == kFP32)
-        ensure_fp32();
+    dss_ready = false;
+    if (precision == kFP32 || (dss && use_dense_ss))
+        ensure_fp32(); // (dense same-spin operands built before are refilled in place)
 }
 
 // Same result as set_hamiltonian, ordered on stream st: the host arrays are copied into the
@@ -870,6 +899,9 @@ void SigmaBuilder::set_hamiltonian_async(double E_, const double* H_, const doub
         build_groups(s_, *sh, st);
     }
     fp32_ready = true;
+    dss_ready = false;
+    if (dss) // built before: refilled in place, in stream order, so captured graphs follow
+        prepare_dense_ss(st);
 }
 
 // Reserves the graph scratch for nvec vectors in both precisions. Captured graphs hold its
@@ -1121,18 +1153,36 @@ void SigmaBuilder::run(const T* C, T* sig, cudaStream_t st, int mask, bool timed
     }
     if (timed)
         F2G_CUDA(cudaEventRecord(cur_ev[0], st));
+    bool dense = false;
+    if constexpr (sizeof(T) == 4) {
+        if (use_dense_ss && dss_ready && (mask & 3)) {
+            // same-spin terms as dense tensor-core GEMMs on split FP16 operands
+            const int set = graph ? 1 : 0;
+            dense_ss_split(s, *dss, C, nvec, set, st);
+            if ((mask & 2) && s->nb >= 1)
+                dense_ss_term(s, *dss, sig, 1, false, nvec, set, st);
+            else
+                F2G_CUDA(cudaMemsetAsync(sig, 0, (size_t)nvec * nd * sizeof(T), st));
+            if (timed)
+                F2G_CUDA(cudaEventRecord(cur_ev[1], st));
+            if (mask & 1)
+                dense_ss_term(s, *dss, sig, 0, true, nvec, set, st);
+            dense = true;
+        }
+    }
     // beta same spin: sigma = (Hbb C^T)^T
-    if ((mask & 2) && s->nb >= 1) {
+    if (dense) {
+    } else if ((mask & 2) && s->nb >= 1) {
         launch_transpose<T>(NA, NB, C, Ct_, st, nvec);
         launch_spmm<T>(hb, valb, NB, (int)NA, Ct_, Tt_, false, st, nvec);
         launch_transpose<T>(NB, NA, Tt_, sig, st, nvec);
     } else {
         F2G_CUDA(cudaMemsetAsync(sig, 0, (size_t)nvec * nd * sizeof(T), st));
     }
-    if (timed)
+    if (timed && !dense)
         F2G_CUDA(cudaEventRecord(cur_ev[1], st));
     // alpha same spin + H0
-    if (mask & 1)
+    if ((mask & 1) && !dense)
         launch_spmm<T>(ha, vala, NA, (int)NB, C, sig, true, st, nvec);
     if (timed)
         F2G_CUDA(cudaEventRecord(cur_ev[2], st));

@@ -33,6 +33,7 @@ struct StringHamiltonian {
 constexpr int kSsGroup = 8;            // rows per group of the grouped FP32 same-spin kernel
 constexpr int64_t kSsGroupMinRows = 2048; // strings per spin from which the FP32 build uses groups
 constexpr int kSsGroupMaxSort = 16384; // kSsGroup * entries per row must fit one block's sort
+constexpr int64_t kDenseSsMaxStrings = 4096; // dense same-spin GEMMs up to this many strings per spin
 
 struct SigmaBuilder {
     CIStrings* s;
@@ -72,6 +73,13 @@ struct SigmaBuilder {
     bool tc_b_ready = false;
     std::shared_ptr<struct TcBOperands> tc_b;
     void prepare_tma_b(cudaStream_t st);
+    // FP32 same-spin terms as dense GEMMs on the tensor cores (dense_ss.cu; split FP16, three
+    // products), chosen by the autotuner for spaces of at most kDenseSsMaxStrings strings per spin
+    bool use_dense_ss = false;
+    bool dss_ready = false;
+    std::shared_ptr<struct DenseSameSpin> dss;
+    bool dense_ss_supported() const;
+    void prepare_dense_ss(cudaStream_t st);
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
     DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
     DevBuf<unsigned int> tc_cmax; // per-vector largest |C| of a tensor-core launch (its operand scale)

@@ -47,7 +47,7 @@ def test_autotune_picks_and_caches(cuda):
     r64 = autotune_sigma(sb, 8, 4, 4, "fp64")
     r32 = autotune_sigma(sb, 8, 4, 4, "fp32")
     assert r64["ms"] <= r64["default_ms"] + 1e-9 and len(r64["timings"]) == 4
-    assert len(r32["timings"]) == 8  # tensor cores available for this space
+    assert len(r32["timings"]) == 16  # tensor cores and the dense same-spin GEMMs available for this space
     assert cached_choice(8, 4, 4, "fp64") == r64["choice"]
     # a second builder of the same shape takes the cached choice without timing
     s2, sb2 = _builder(4, 4, 8, 32)

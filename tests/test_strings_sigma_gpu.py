@@ -359,3 +359,50 @@ def test_tensor_core_wait_limit_reports_error_and_recovers(cuda):
     sb.Hamiltonian(dc, out)
     assert sb.tensor_core_error() == 0
     assert rel(out.cpu().numpy(), ref.cpu().numpy()) < 2e-6
+
+
+@pytest.mark.parametrize("na,nb,n", [(3, 3, 6), (4, 3, 7), (5, 5, 10), (6, 6, 12), (7, 7, 14)])
+def test_fp32_dense_same_spin(cuda, na, nb, n):
+    """FP32 sigma with the same-spin terms as dense tensor-core GEMMs (split FP16, three cuBLAS
+    products): FP32 accuracy against the FP64 sigma, the same bits call after call and for a vector
+    alone or in a batch, and new integrals (in place, in stream order) give the sigma of a fresh
+    builder with those integrals."""
+    torch = cuda
+    from forte2_gb300.ci_helpers import CISigmaBuilder
+
+    s = make(na, nb, n)
+    ints = make_integrals(n, 800 + n)
+    sb = CISigmaBuilder(s, ints.E, ints.H, ints.V, 0)
+    c = torch.as_tensor(np.stack([random_ci_vector(s.ndet, 5 + n), random_ci_vector(s.ndet, 6 + n)]), device="cuda")
+    ref = torch.empty_like(c)
+    sb.Hamiltonian(c, ref)
+    sb.set_precision("fp32")
+    sparse = torch.empty_like(c)
+    sb.Hamiltonian(c, sparse)
+    sb.set_variant("dense_same_spin", 1)
+    dense = torch.empty_like(c)
+    sb.Hamiltonian(c, dense)
+    again = torch.empty_like(c)
+    sb.Hamiltonian(c, again)
+    assert torch.equal(dense, again)
+    one = torch.empty_like(c[1])
+    sb.Hamiltonian(c[1].contiguous(), one)
+    assert torch.equal(one, dense[1])
+    for i in range(2):
+        e_d = rel(dense[i].cpu().numpy(), ref[i].cpu().numpy())
+        e_s = rel(sparse[i].cpu().numpy(), ref[i].cpu().numpy())
+        assert e_d < 2e-6 and e_d < 4 * e_s + 1e-7
+    ints2 = make_integrals(n, 900 + n)
+    fresh = CISigmaBuilder(s, ints2.E, ints2.H, ints2.V, 0)
+    fresh.set_precision("fp32")
+    fresh.set_variant("dense_same_spin", 1)
+    want = torch.empty_like(c)
+    fresh.Hamiltonian(c, want)
+    for update in (sb.update_integrals, sb.set_Hamiltonian):
+        update(ints2.E, ints2.H, ints2.V)
+        got = torch.empty_like(c)
+        sb.Hamiltonian(c, got)
+        assert torch.equal(got, want)
+    big = make_integrals(15, 1)  # C(15, 7) = 6,435 strings per spin: above the dense limit
+    with pytest.raises(ValueError):
+        CISigmaBuilder(make(7, 7, 15), big.E, big.H, big.V, 0).set_variant("dense_same_spin", 1)
