@@ -386,6 +386,7 @@ def run_gb300(a):
                          "algorithmic_bytes": 24 * ndet,
                          "traffic_over_algorithmic": opposite_traffic(a.norb, na, nb) / (24 * ndet)},
             "terms_ms": {"total": 1e3 * tot, "aabb": 1e3 * t_ab, "aaaa_h1a_h0": 1e3 * t_aa, "bbbb_h1b": 1e3 * t_bb},
+            "same_spin": same_spin_rates(a.norb, na, nb, ndet, t_aa, t_bb),
             "hz_dense_flops": f_hz, "sparse_flops": f_sp,
             "autotune": None if tuned is None else {p: {"choice": r["choice"], "ms": r["ms"], "default_ms": r["default_ms"]}
                                                     for p, r in tuned.items()},
@@ -515,6 +516,23 @@ def casci_time_to_solution(norb, nroot, prec, e_tol, maxiter, iseed, basis_per_r
     del sol
     torch.cuda.empty_cache()
     return r
+
+
+def same_spin_rates(norb, na, nb, ndet, t_aa, t_bb):
+    """The FP64 same-spin terms: FP64 rate of their string-Hamiltonian products, and HBM rate of
+    their algorithmic bytes (24 B per determinant per term pass: read C, read and write sigma; the
+    beta term also transposes C and sigma, two more passes)."""
+    from math import comb
+
+    peak = _measured_peaks().get("hbm_gbs") or 6801.7
+    out = {"hbm_peak_gbs": peak, "bound": "fp64 pipe (the products), the passes are HBM"}
+    for spin, k, t in (("alpha_h1a_h0", na, t_aa), ("beta_h1b", nb, t_bb)):
+        nnz = 1 + k * (norb - k) + comb(k, 2) * comb(norb - k, 2)
+        flops = 2 * ndet * (nnz - 1)
+        b = 24 * ndet
+        out[spin] = {"ms": 1e3 * t, "flops": flops, "tflops": flops / t / 1e12, "algorithmic_bytes": b,
+                     "achieved_gbs": b / t / 1e9, "frac_of_hbm": b / t / 1e9 / peak}
+    return out
 
 
 def run_davidson(a):
