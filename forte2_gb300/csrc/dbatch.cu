@@ -38,6 +38,7 @@ void DavBatch::build() {
     for (DavGraph* d : g) {
         if (!d->exec)
             d->capture(); // the solve's set-up (scratch, FP32 tables) and its own graph
+        d->prepare();     // current kernel variants' scratch (they may have changed since)
         serials.push_back(d->serial);
     }
     std::unique_lock<std::mutex> lock;

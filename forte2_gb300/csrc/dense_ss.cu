@@ -202,16 +202,23 @@ void dense_ss_build(const CIStrings* s, const StringHamiltonian* sh[2], std::sha
     }
 }
 
+// Scratch of dense_ss_split / dense_ss_term for nvec vectors of one set (graph captures must not
+// allocate: the set of captured graphs is reserved before a capture)
+void dense_ss_reserve(const CIStrings* s, DenseSameSpin& d, int nvec, int set) {
+    const int64_t NA = s->a.N0, ldb = d.ld[1];
+    d.chi[set].reserve((size_t)std::max<int64_t>(1, nvec * NA * ldb));
+    d.clo[set].reserve((size_t)std::max<int64_t>(1, nvec * NA * ldb));
+    d.cmax[set].reserve((size_t)std::max(1, nvec));
+    d.alpha[set].reserve((size_t)2 * std::max(1, nvec));
+}
+
 // The split parts of nvec vectors of the C1 space (scales and alpha values in device memory), for
 // the GEMMs of dense_ss_term. set: 0 direct calls, 1 captured graphs (separate scratch).
 void dense_ss_split(const CIStrings* s, DenseSameSpin& d, const float* C, int nvec, int set, cudaStream_t st) {
     const int64_t NA = s->a.N0, NB = s->b.N0, nd = NA * NB, ldb = d.ld[1];
     if (nvec > 1024)
         throw Error(2, "dense same-spin sigma: at most 1024 vectors per call");
-    d.chi[set].reserve((size_t)std::max<int64_t>(1, nvec * NA * ldb));
-    d.clo[set].reserve((size_t)std::max<int64_t>(1, nvec * NA * ldb));
-    d.cmax[set].reserve((size_t)nvec);
-    d.alpha[set].reserve((size_t)2 * nvec);
+    dense_ss_reserve(s, d, nvec, set);
     F2G_CUDA(cudaMemsetAsync(d.cmax[set].get(), 0, (size_t)nvec * sizeof(unsigned int), st));
     if (nd == 0)
         return;

@@ -209,16 +209,21 @@ struct DavGraph {
             dg_gs(S, P, b, ld, r, ldr, s);
     }
 
-    void capture() {
-        drop();
+    // everything a capture of the iterations needs allocated and current (a capture cannot allocate)
+    void prepare() {
         sb->prepare_untimed(R);
         if (sb->precision == kFP32) {
-            sb->ensure_fp32();
+            sb->prepare_graph_fp32(R);
             sa->ensure_fp32_tables(0);
         }
         scr.reserve(*sb, *sa, R);
         F2G_CUDA(cudaStreamSynchronize(0)); // set-up work of the legacy stream done before the capture
         sb->flush_timers();
+    }
+
+    void capture() {
+        drop();
+        prepare();
         std::unique_lock<std::mutex> lock;
         cudaStream_t cap = capture_stream(lock);
         F2G_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));

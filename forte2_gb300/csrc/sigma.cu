@@ -595,6 +595,7 @@ void opposite_tc_build_b(const CIStrings* s, const float* V, const unsigned int*
 void dense_ss_build(const CIStrings* s, const StringHamiltonian* sh[2], std::shared_ptr<DenseSameSpin>& d,
                     cudaStream_t st);
 void dense_ss_split(const CIStrings* s, DenseSameSpin& d, const float* C, int nvec, int set, cudaStream_t st);
+void dense_ss_reserve(const CIStrings* s, DenseSameSpin& d, int nvec, int set);
 void dense_ss_term(const CIStrings* s, DenseSameSpin& d, float* sig, int spin, bool accumulate, int nvec, int set,
                    cudaStream_t st);
 
@@ -927,6 +928,14 @@ void SigmaBuilder::prepare_untimed(int nvec) {
         gxfS.reserve(tot);
     }
     untimed_nvec = nvec;
+}
+
+// Before a capture of FP32 sigma builds of nvec vectors: the dense same-spin operands and their
+// graph scratch (a capture cannot allocate)
+void SigmaBuilder::prepare_graph_fp32(int nvec) {
+    ensure_fp32();
+    if (use_dense_ss && dss)
+        dense_ss_reserve(s, *dss, std::max(1, nvec), 1);
 }
 
 void SigmaBuilder::apply_f32(const float* C, float* S, cudaStream_t st, int nvec, bool timed, bool graph) {

@@ -80,6 +80,7 @@ struct SigmaBuilder {
     std::shared_ptr<struct DenseSameSpin> dss;
     bool dense_ss_supported() const;
     void prepare_dense_ss(cudaStream_t st);
+    void prepare_graph_fp32(int nvec);
     DevBuf<uint32_t> beta_exc; // beta single excitations per string for its scatter
     DevBuf<int> tc_err;        // set by the tensor-core kernel if a bounded wait gave up
     DevBuf<unsigned int> tc_cmax; // per-vector largest |C| of a tensor-core launch (its operand scale)

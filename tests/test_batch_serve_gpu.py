@@ -87,3 +87,30 @@ def test_serving_admission_respects_budget(cuda):
     stats, lat, _ = serve(reqs, hbm_budget=2 * one, nstreams=4)
     assert stats["peak_footprint_gb"] * 2**30 <= 2 * one + 1
     assert len(lat) == 12
+
+
+def test_one_launch_batch_with_dense_same_spin(cuda):
+    """The collective launch captures cuBLAS GEMMs inside its conditional loop bodies: mixed solves
+    whose FP32 same-spin terms run as dense tensor-core GEMMs (forced through the autotuner's
+    cache) converge in one-launch batches to the energies of their solo solves."""
+    from forte2_gb300 import autotune
+    from forte2_gb300.batch import make_solver, solve_batched
+
+    inst = [dict(norb=n, na=n // 2, nb=n // 2, multiplicity=m, nroot=r, iseed=70 + i)
+            for i, (n, m, r) in enumerate([(8, 1, 2), (10, 3, 1), (8, 3, 1), (10, 1, 2)])]
+    autotune.clear_cache()
+    dense = {"narrow_same_spin": 0, "persistent_opposite": 0, "tensor_cores": 1, "dense_same_spin": 1}
+    for n in (8, 10):
+        autotune._CACHE[(n, n // 2, n // 2, "fp32")] = {"choice": dict(dense), "ms": 0.0, "default_ms": 0.0,
+                                                         "timings": []}
+    try:
+        stats = {}
+        res, _, _ = solve_batched(inst, "mixed", nstreams=4, one_launch=True, stats=stats)
+        assert stats["batch_launches"] >= 1 and stats["batch_solves"] >= len(inst)
+        for i, x in enumerate(inst):
+            solo = make_solver(x, "mixed").run()
+            assert res[i].converged and solo.converged
+            assert res[i].sigma_builder._tuned["fp32"]["dense_same_spin"] == 1
+            np.testing.assert_allclose(res[i].evals, solo.evals, rtol=0, atol=1e-12)
+    finally:
+        autotune.clear_cache()
