@@ -34,6 +34,7 @@ constexpr int kSsGroup = 8;            // rows per group of the grouped FP32 sam
 constexpr int64_t kSsGroupMinRows = 2048; // strings per spin from which the FP32 build uses groups
 constexpr int kSsGroupMaxSort = 16384; // kSsGroup * entries per row must fit one block's sort
 constexpr int64_t kDenseSsMaxStrings = 4096; // dense same-spin GEMMs up to this many strings per spin
+constexpr int64_t kDenseSsMinStrings = 512;  // ... and by default from this many
 
 struct SigmaBuilder {
     CIStrings* s;
@@ -74,7 +75,8 @@ struct SigmaBuilder {
     std::shared_ptr<struct TcBOperands> tc_b;
     void prepare_tma_b(cudaStream_t st);
     // FP32 same-spin terms as dense GEMMs on the tensor cores (dense_ss.cu; split FP16, three
-    // products), chosen by the autotuner for spaces of at most kDenseSsMaxStrings strings per spin
+    // products) for spaces of kDenseSsMinStrings to kDenseSsMaxStrings strings per spin by default;
+    // the autotuner times both
     bool use_dense_ss = false;
     bool dss_ready = false;
     std::shared_ptr<struct DenseSameSpin> dss;

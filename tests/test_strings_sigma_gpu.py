@@ -377,6 +377,7 @@ def test_fp32_dense_same_spin(cuda, na, nb, n):
     ref = torch.empty_like(c)
     sb.Hamiltonian(c, ref)
     sb.set_precision("fp32")
+    sb.set_variant("dense_same_spin", 0)  # (the default from 512 strings per spin)
     sparse = torch.empty_like(c)
     sb.Hamiltonian(c, sparse)
     sb.set_variant("dense_same_spin", 1)
