@@ -109,9 +109,9 @@ int f2g_sigma_set_tensor_cores(void* sigma, int on, int* available);
  * irreps alone on its own vectors (irrep-aware opposite-spin kernel, same-spin terms block by
  * block); 0 runs the C1 kernels on the embedding (same sigma to rounding). which = 5 (default 1):
  * the tensor-core kernel's B tiles are prebuilt for every alpha string and fed by TMA; 0 builds
- * them in each thread block (the same sigma bits). which = 6 (default 0): the FP32 same-spin terms
- * as dense tensor-core GEMMs (split FP16, three products; spaces of at most 4096 strings per spin,
- * else error 2). No reference counterpart. */
+ * them in each thread block (the same sigma bits). which = 6: the FP32 same-spin terms as dense
+ * tensor-core GEMMs (split FP16, three products; spaces of at most 4096 strings per spin, else
+ * error 2; default 1 from 512 strings per spin). No reference counterpart. */
 int f2g_sigma_set_variant(void* sigma, int which, int value);
 /* 1 if a tensor-core build gave up waiting for its matrix operations (results invalid). */
 int f2g_sigma_tc_error(void* sigma, int* out);
