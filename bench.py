@@ -348,8 +348,10 @@ def run_gb300(a):
                        "peak_source": "MEASURED_PEAKS.json bf16_tflops (dense FP16 runs at the BF16 rate)"}
         sb.set_precision("fp64")
     davidson = None
+    serving = None
     if rank == 0 and world == 1 and not a.no_davidson and a.norb == NORB:
         davidson = davidson_acceptance()
+        serving = serving_sample()
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         v, sample, cores = cpu_baseline(a.norb, a.cpu_seconds, na, nb, ints, c_host)
@@ -391,6 +393,7 @@ def run_gb300(a):
             "autotune": None if tuned is None else {p: {"choice": r["choice"], "ms": r["ms"], "default_ms": r["default_ms"]}
                                                     for p, r in tuned.items()},
             "davidson": davidson,
+            "serving": serving,
             "mixed_fp32_sigma_builds_per_s": mixed,
             "tensor_core_roofline": tc_roof,
             "mixed_fp32_terms_ms": mixed_terms,
@@ -516,6 +519,22 @@ def casci_time_to_solution(norb, nroot, prec, e_tol, maxiter, iseed, basis_per_r
     del sol
     torch.cuda.empty_cache()
     return r
+
+
+def serving_sample(n_requests=1000, rate=200.0):
+    """The metric's latency part in the default line: a 1,000-request Poisson stream of the serving
+    workload's distribution ((6e,6o)-(16e,16o) weighted 1/Ndet, 200 requests/s, seed 5), served by
+    continuous batching in both precisions; p50/p99 from arrival to result and solves/s. The
+    10,000-request stream runs with --mode serve."""
+    from forte2_gb300.serve import default_prewarm, poisson_stream, serve
+
+    out = {"workload": f"{n_requests} requests, Poisson {rate}/s, (6e,6o)-(16e,16o) weight 1/Ndet, multiplicity "
+                       "1/3, 1-3 roots, e_tol 1e-10 (the full 10,000-request stream: --mode serve)"}
+    for prec in ("fp64", "mixed"):
+        stats, _, _ = serve(poisson_stream(n_requests, rate=rate), precision=prec, prewarm=default_prewarm())
+        out[prec] = {k: stats[k] for k in ("solves_per_s", "p50_latency_s", "p99_latency_s", "mean_latency_s",
+                                            "wall_s", "max_inflight", "sizes")}
+    return out
 
 
 def same_spin_rates(norb, na, nb, ndet, t_aa, t_bb):
