@@ -2,7 +2,7 @@
 ``oracle/port/ci_port.cc``.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use this
-module, always as the checker or the timed CPU baseline, never as a product path. The library
+module, always as the parity reference or the timed CPU baseline, never as a product path. The library
 is compiled by ``build_port()`` (called from ``__graft_entry__.build()``) on the machine that
 runs it.
 """
