@@ -107,6 +107,20 @@ def test_new_entry_points_validate_handles_without_gpu(libpath):
     assert L.f2g_sigma_set_max_blocks(None, 4) == 2
     assert L.f2g_sigma_set_tensor_cores(None, 1, None) == 2
     assert L.f2g_dav_gs_append(None, 10, 4, 0, None, 10, 1, 10, 1e-8, 1e-12, 1, 1, None, None) == 2
+    # one-launch batches of graph solves: NULL handles and empty batches are refused on the host
+    arr = (ctypes.c_void_p * 2)(None, None)
+    assert L.f2g_dgraph_batch_create(None, 2, ctypes.byref(out)) == 2
+    assert L.f2g_dgraph_batch_create(ctypes.addressof(arr), 0, ctypes.byref(out)) == 2
+    assert b"at least one" in L.f2g_last_error()
+    assert L.f2g_dgraph_batch_create(ctypes.addressof(arr), 2, ctypes.byref(out)) == 2
+    assert b"NULL graph" in L.f2g_last_error()
+    assert L.f2g_dgraph_batch_launch(None, None) == 2
+    assert L.f2g_dgraph_batch_nodes(None, None) == 2
+    serial = ctypes.c_uint64()
+    assert L.f2g_dgraph_serial(None, ctypes.addressof(serial)) == 2
+    # two-component builder and its RDMs
+    assert L.f2g_rel_sigma_rdm(None, 0, None, None, None, None) == 2
+    assert L.f2g_rel_sigma_apply(None, None, None, 1, None) == 2
 
 
 def test_davidson_and_sigma_entry_points_validate_sizes_without_gpu(libpath):
