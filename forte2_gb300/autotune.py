@@ -31,11 +31,13 @@ def _apply(sb, choice):
         sb.set_variant(name, value)
 
 
-def candidates(sb, precision):
+def candidates(sb, precision, fixed=None):
+    """Variant combinations to time; names in `fixed` keep their given value."""
+    fixed = fixed or {}
     opts = {"narrow_same_spin": (0, 1), "persistent_opposite": (0, 1)}
     if precision == "fp32" and sb.set_tensor_cores(True):
         opts["tensor_cores"] = (1, 0)
-    if precision == "fp32":
+    if precision == "fp32" and "dense_same_spin" not in fixed:
         # same-spin terms as dense tensor-core GEMMs, where the space allows them
         try:
             sb.set_variant("dense_same_spin", 0)
@@ -44,14 +46,17 @@ def candidates(sb, precision):
         except ValueError:
             pass
         sb.set_variant("dense_same_spin", 0)
+    for name, value in fixed.items():
+        opts[name] = (value,)
     names = list(opts)
     return [dict(zip(names, vals)) for vals in itertools.product(*(opts[n] for n in names))]
 
 
-def autotune_sigma(sb, norb, na, nb, precision="fp64", reps=2, seed=17):
-    """Time every variant on this builder and apply the fastest. Returns
-    {"choice": {...}, "ms": best, "default_ms": first candidate, "timings": [(choice, ms), ...]}."""
-    key = (norb, na, nb, precision)
+def autotune_sigma(sb, norb, na, nb, precision="fp64", reps=2, seed=17, fixed=None):
+    """Time every variant on this builder and apply the fastest; variants named in `fixed` keep
+    their values. Returns {"choice": {...}, "ms": best, "default_ms": first candidate,
+    "timings": [(choice, ms), ...]}."""
+    key = (norb, na, nb, precision) if not fixed else (norb, na, nb, precision, tuple(sorted(fixed.items())))
     if not hasattr(sb, "_tuned"):
         sb._tuned = {}
     if key in _CACHE:
@@ -67,7 +72,7 @@ def autotune_sigma(sb, norb, na, nb, precision="fp64", reps=2, seed=17):
     c = torch.rand(ndet, generator=g, dtype=torch.float64, device="cuda") - 0.5
     out = torch.empty_like(c)
     timings = []
-    for choice in candidates(sb, precision):
+    for choice in candidates(sb, precision, fixed):
         _apply(sb, choice)
         sb.Hamiltonian(c, out)  # warm-up (kernel attributes, scratch)
         a = torch.cuda.Event(enable_timing=True)

@@ -247,7 +247,8 @@ def batched_instances(n_inst: int = 64, seed: int = 4000):
 LARGE_NDET = 200_000  # spaces from here on are bound by sigma arithmetic, not by launches
 
 
-def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=2000, autotune=True, ints=None, one_launch=False):
+def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=2000, autotune=True, ints=None, one_launch=False,
+                sigma_variants=None):
     """One instance's solver; its sigma kernel variants are autotuned once per shape. Spaces of at
     least LARGE_NDET determinants get the larger Davidson subspace (12 vectors per root, collapse
     to 6, at most 64) in both precisions: the same energies in about a third of the iterations
@@ -259,7 +260,8 @@ def make_solver(inst, precision="fp64", e_tol=1e-10, maxiter=2000, autotune=True
         dl = DavidsonLiuParams(e_tol=e_tol, maxiter=maxiter, basis_per_root=bpr, collapse_per_root=min(6, bpr - 1))
     return CASCISolver(norb=inst["norb"], na=inst["na"], nb=inst["nb"], multiplicity=inst["multiplicity"],
                        nroot=inst["nroot"], E=ints.E, H=ints.H, V=ints.V, ci_params=CIParams(precision=precision),
-                       davidson_liu_params=dl, autotune=autotune, one_launch=one_launch)
+                       davidson_liu_params=dl, autotune=autotune, one_launch=one_launch,
+                       sigma_variants=sigma_variants)
 
 
 def footprint_bytes(norb: int, na: int, nb: int, nroot: int, basis_per_root: int = 0) -> int:

@@ -70,6 +70,9 @@ class CASCISolver:
     sigma_max_blocks: int = 0
     # pick the fastest sigma kernel variants for this shape before solving (forte2_gb300.autotune)
     autotune: bool = False
+    # kernel variants fixed for this solver ({name: value} of CISigmaBuilder.set_variant), applied
+    # after the autotuner and over its choices
+    sigma_variants: dict = None
     # after the solve, check every root's energy against its RDMs (ci.py:203-204, 323-403)
     do_test_rdms: bool = False
 
@@ -191,11 +194,21 @@ class CASCISolver:
         if alg == "exact":
             return self._exact()
         self.sigma_builder.set_algorithm(alg)
+        for name, value in (self.sigma_variants or {}).items():
+            self.sigma_builder.set_variant(name, value)
         if self.autotune:
             from .autotune import autotune_sigma
 
             for prec in ("fp64", "fp32") if self.ci_params.precision == "mixed" else ("fp64",):
-                autotune_sigma(self.sigma_builder, self.norb, self.na, self.nb, prec)
+                autotune_sigma(self.sigma_builder, self.norb, self.na, self.nb, prec, fixed=self.sigma_variants)
+        if self.sigma_variants:
+            sb = self.sigma_builder
+            if not hasattr(sb, "_tuned"):
+                sb._tuned = {}
+            for prec in ("fp64", "fp32"):
+                sb._tuned.setdefault(prec, {}).update(self.sigma_variants)
+            for name, value in self.sigma_variants.items():
+                sb.set_variant(name, value)
         hdiag = self.sigma_builder.hdiag_csf_device(self.spin_adapter)
         self.timings["setup"] = time.perf_counter() - t0
         if self.ndet == 1:

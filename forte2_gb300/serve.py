@@ -97,7 +97,14 @@ class SolverPool:
             self.reused += 1
             return solver
         self.created += 1
-        return make_solver(r.inst, self.prec(r), e_tol=self.e_tol, ints=r.integrals())
+        return make_solver(r.inst, self.prec(r), e_tol=self.e_tol, ints=r.integrals(),
+                           sigma_variants=self.variants(r))
+
+    def variants(self, r):
+        """Kernel variants of a new solver made while the server runs: the FP32 options whose
+        operands are allocated on first use (TMA-fed B tiles, dense same-spin GEMMs) stay off, since
+        allocating device memory synchronises the device under every solve in flight."""
+        return {"tma_b": 0, "dense_same_spin": 0} if self.prec(r) == "mixed" else None
 
     def has_idle(self, r):
         return bool(self.idle.get(self.key(r)))
