@@ -52,3 +52,44 @@ def test_batched_instances_and_prewarm_shapes():
     assert all(x["na"] == x["nb"] == x["norb"] // 2 and 1 <= x["nroot"] <= 4 for x in inst)
     shapes = default_prewarm()
     assert len(shapes) == 18 and sum(c for *_, c in shapes) == 6 * (16 + 6 + 2)
+
+
+def test_server_solvers_keep_allocating_fp32_options_off():
+    from forte2_gb300.serve import Request, SolverPool
+
+    pool = SolverPool("mixed", 1e-10)
+    assert pool.variants(Request(0, 0.0, 12, 1, 1, 1)) == {"tma_b": 0, "dense_same_spin": 0}
+    assert pool.variants(Request(1, 0.0, 8, 1, 1, 1)) is None  # FP64 below the mixed threshold
+    assert SolverPool("fp64", 1e-10).variants(Request(2, 0.0, 12, 1, 1, 1)) is None
+
+
+class _FakeBuilder:
+    """The two calls the autotuner's candidate list makes, recorded."""
+
+    def __init__(self, dense_ok=True):
+        self.calls = []
+        self.dense_ok = dense_ok
+
+    def set_tensor_cores(self, on=True):
+        return True
+
+    def set_variant(self, name, value):
+        if name == "dense_same_spin" and value and not self.dense_ok:
+            raise ValueError("dense same-spin GEMMs need at most 4096 strings per spin")
+        self.calls.append((name, value))
+
+
+def test_autotune_candidates_honour_fixed_variants():
+    from forte2_gb300.autotune import candidates
+
+    sb = _FakeBuilder()
+    full = candidates(sb, "fp32")
+    assert len(full) == 16 and {c["dense_same_spin"] for c in full} == {0, 1}
+    sb = _FakeBuilder()
+    fixed = candidates(sb, "fp32", {"tma_b": 0, "dense_same_spin": 0})
+    assert len(fixed) == 8
+    assert all(c["tma_b"] == 0 and c["dense_same_spin"] == 0 for c in fixed)
+    assert ("dense_same_spin", 1) not in sb.calls  # a fixed option is never switched on to probe it
+    sb = _FakeBuilder(dense_ok=False)
+    assert all("dense_same_spin" not in c for c in candidates(sb, "fp32"))
+    assert len(candidates(_FakeBuilder(), "fp64")) == 4
