@@ -69,3 +69,31 @@ def test_block_enumeration_errors():
         enumerate_blocks(2, 2, 4, [[0, 1, 0, 1]], [], [])  # state irrep outside the orbitals' group
     with pytest.raises((ValueError, RuntimeError)):
         enumerate_blocks(2, 2, 0, [[0]] * 7, [], [])  # more than six GAS spaces
+
+
+@pytest.mark.parametrize("case", [c for c in _cases() if c["ndet"] > 0], ids=lambda c: c["key"])
+def test_port_sigma_on_the_embedding_is_the_reference_blocked_sigma(gold, case):
+    """The design's premise, on the CPU: the reference's sigma of a blocked space (irreps and/or
+    GAS bounds, its own block loops) equals the oracle port's C1 sigma of the vector embedded in
+    the C1 CAS space of the same orbitals, read back on the space's determinants (P H P)."""
+    from forte2_gb300.synthetic import make_integrals, random_ci_vector, symmetrize_integrals
+    from oracle.port import PortCI
+
+    k = case["key"]
+    orbsym = [x for g in case["orbital_symmetry"] for x in g]
+    n, na, nb = len(orbsym), case["na"], case["nb"]
+    ints = make_integrals(n, case["iseed"])
+    if case["symmetric"]:
+        ints = symmetrize_integrals(ints, orbsym)
+    port = PortCI(n, na, nb)
+    port.set_hamiltonian(ints.E, ints.H, ints.V)
+    ia = {int(m): i for i, m in enumerate(port.strings(0))}
+    ib = {int(m): i for i, m in enumerate(port.strings(1))}
+    dets = gold[f"{k}_dets"].reshape(-1, 2)
+    pos = np.array([ia[int(a)] * port.nbs + ib[int(b)] for a, b in dets])
+    c = random_ci_vector(case["ndet"], case["cseed"])
+    full = np.zeros(port.ndet)
+    full[pos] = c
+    got = port.sigma(full)[pos]
+    ref = gold[f"{k}_sigma"]
+    assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
