@@ -18,8 +18,9 @@
 // FP32 evaluation (1e-7 relative).
 //
 // Determinism: sigma(Ja, :) is accumulated in shared memory in fixed point, as two 32-bit integer
-// rows. Every product sum is bounded by construction (|A|, |B| < 2^15, K <= 72, so |U| < 2^37 in
-// scaled units) and is rounded to a multiple of 2^-7 scaled units, split exactly into a high part
+// rows. Every product sum is bounded by construction (|A|, |B| <= 2^15 with FP16 low parts below
+// 2^-10 of that, K <= 72, so |U| < 72 2^30 (1 + 2^-9) < 2^36.2 in scaled units) and is rounded to
+// a multiple of 2^-7 scaled units, split exactly into a high part
 // (units of 2^15) and a low part (units of 2^-7), each below 2^21.2 in magnitude; at most
 // nb (n - nb + 1) <= 72 of them reach one element, so both sums stay below 2^28 and are exact.
 // Integer addition does not depend on the order of the shared-memory atomics: the sigma of a vector
@@ -166,7 +167,7 @@ __device__ __forceinline__ int split_exponent(float m) {
     return e < -120 ? -120 : (e > 120 ? 120 : e);
 }
 
-// Adds x (FP32 bits, |x| < 2^37 in scaled units; sign flipped when neg is 1) to the fixed-point
+// Adds x (FP32 bits, |x| < 2^36.2 in scaled units; sign flipped when neg is 1) to the fixed-point
 // element jb as two exact integers: hi = round(x / 2^15) into row_hi and lo = round((x - hi 2^15)
 // 2^7) into row_lo, so the element holds (hi 2^22 + lo) 2^-7. Both parts come from FP32
 // multiply-adds on a 1.5 2^23 offset (the float bits of C + y are C's bits + y for an integer
